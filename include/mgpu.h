@@ -1,0 +1,169 @@
+/*
+ * mgpu.h -- C ABI of the GB300 path-tracer hot path (libmgpu.so).
+ *
+ * This is the drop-in boundary beneath Milton's renderer plugin: plain pointers, sizes and
+ * status codes, no C++ or torch types.  Every call returns MGPU_OK (0) or a negative
+ * MGPU_E_* code; mgpu_last_error() returns a thread-local message for the last failure, the
+ * way Milton's SharedLibraryManager::getLastError reports plugin failures
+ * (mlt/src/milton/dynamic/SharedLibraryManager.cpp:66-68).
+ *
+ * Streams are passed as `void*` holding a cudaStream_t (NULL = legacy default stream).
+ * Calls on one scene are stream-ordered and not re-entrant across host threads; a scene
+ * belongs to the device that was current when it was created.
+ *
+ * Scene geometry is a world-space triangle soup: Milton's ShapeSet flattened through every
+ * shape's transform (mlt/src/milton/shapes/ShapeSet.cpp:36-80, Mesh.cpp:211-251,
+ * Transformable.inl:18-48).  The global primitive id of a triangle is its index in that soup:
+ * the prefix offset of its shape in ShapeSet order plus its index inside the shape, the pair
+ * (pt.shape, pt.index) that kdTreeAccel::getIntersection reports (kdTreeAccel.cpp:991-993).
+ */
+#ifndef MGPU_H_
+#define MGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGPU_OK 0
+#define MGPU_E_INVALID (-1)  /* bad argument */
+#define MGPU_E_CUDA (-2)     /* CUDA runtime error */
+#define MGPU_E_NOMEM (-3)    /* allocation failed (host or device) */
+#define MGPU_E_BUDGET (-4)   /* request exceeds the memory budget it was admitted under */
+#define MGPU_E_STATE (-5)    /* call not valid in the object's current state */
+#define MGPU_E_DEVICE (-6)   /* a kernel reported a fault it guarded against (bounds, stack) */
+
+/* triangle flags */
+#define MGPU_TRI_CULLED 1u   /* back-face culled, Milton `Triangle` (Triangle.cpp:245-272); else two-sided `MeshTriangle` */
+
+/* material types (Material::getBSDF, Material.cpp:67-92) */
+#define MGPU_MAT_DIFFUSE 0
+#define MGPU_MAT_PHONG 1
+#define MGPU_MAT_DIELECTRIC 2
+
+typedef struct mgpu_accel mgpu_accel; /* host-side SAH kd-tree, flattened */
+typedef struct mgpu_scene mgpu_scene; /* device-resident scene: tree, triangles, materials, lights */
+
+/* kd-tree build parameters; defaults are Milton's (kdTreeAccel.h:97-104):
+ * min_prims 3, max_depth 24, cost_traversal 1, empty_bias 0.9.  threads 0 = all cores. */
+typedef struct {
+  uint32_t min_prims;
+  uint32_t max_depth;
+  double cost_traversal;
+  double empty_bias;
+  uint32_t threads;
+} mgpu_kd_params;
+
+/* Milton's kd build log (kdTreeAccel.cpp:460-471), sums instead of averages */
+typedef struct {
+  uint64_t no_internal, no_leaves, min_depth, max_depth, sum_depth, min_prims, max_prims, sum_prims;
+  uint64_t node_pairs, refs, bytes_nodes, bytes_refs;
+  double build_seconds;
+} mgpu_kd_stats;
+
+/* Scene description, all host pointers.
+ *   tri_v      ntri*9 floats, world-space vertices (v0,v1,v2)
+ *   tri_n      ntri*9 floats, per-vertex shading normals (unit); NULL = face normals
+ *   tri_mat    ntri material indices
+ *   tri_light  ntri light indices (-1 = not an emitter); NULL = none
+ *   tri_flags  ntri MGPU_TRI_* flags; NULL = all two-sided
+ *   materials  nmat*16 floats: type, kd[3], ks[3], n, ior, transparency, 0...
+ *   lights     nlight*16 floats: center[3], ex[3], ez[3], normal[3], area, Le[3]
+ *              (a Milton `Plane` under a transform: getPosition(u,v) = center + (u-.5)ex + (v-.5)ez,
+ *               Plane.cpp:91-93; Le = power / (area * pi), Emitter.cpp:34-50)              */
+typedef struct {
+  int64_t ntri;
+  const float *tri_v;
+  const float *tri_n;
+  const int32_t *tri_mat;
+  const int32_t *tri_light;
+  const uint32_t *tri_flags;
+  int32_t nmat;
+  const float *materials;
+  int32_t nlight;
+  const float *lights;
+} mgpu_scene_desc;
+
+/* Render parameters.  Defaults mirror Milton's PathTracer/DirectIllumination keys:
+ * noDirectSamples 1, efficientDirect 1, no maximum depth, Russian roulette from depth 2
+ * (PathTracer.cpp:88-89).  max_depth > 0 caps the number of path vertices.
+ * camera: eye[3], look[3] (unit), up[3], heightAngle (degrees), aspectRatio (ThinLensCamera).
+ * Sample passes [sample_begin, sample_begin + sample_count) of spp are rendered and added to
+ * the film (progressive refinement = further calls with later passes).                    */
+typedef struct {
+  int32_t width, height;
+  int32_t spp;            /* noSuperSamples: sets the stratification side floor(sqrt(spp)) */
+  int32_t sample_begin;
+  int32_t sample_count;
+  int32_t no_direct_samples;
+  int32_t max_depth;      /* 0 = unlimited (hard cap 1024, counted) */
+  int32_t rr_start_depth; /* Russian roulette applies at depth >= this */
+  int32_t efficient_direct;
+  int32_t wave_paths;     /* paths in flight per wave; 0 = automatic */
+  uint64_t seed;
+  uint32_t stream_id;     /* decorrelates independent replicas / jobs */
+  float camera[11];
+} mgpu_render_params;
+
+typedef struct {
+  uint64_t paths, extension_rays, shadow_rays, truncated_paths, bounces, kernel_launches;
+} mgpu_render_stats;
+
+/* ---------------------------------------------------------------------------------------- */
+const char *mgpu_last_error(void);
+int mgpu_version(void);
+
+/* Host SAH kd-tree build over the scene's triangles; replaces kdTreeAccel::init
+ * (kdTreeAccel.cpp:403-472) for the flattened soup.  Deterministic for any thread count. */
+int mgpu_accel_build(const mgpu_scene_desc *desc, const mgpu_kd_params *params, mgpu_accel **out);
+int mgpu_accel_stats(const mgpu_accel *accel, mgpu_kd_stats *out);
+/* Depth-first (left before right) serialisation for node-by-node comparison:
+ * kind 0..2 = split axis, 3 = leaf; split = stored float split; count = leaf prim count;
+ * prims = leaf prim lists in Milton's stored order.  Pass NULL arrays to query sizes.    */
+int mgpu_accel_serialize(const mgpu_accel *accel, int32_t *kind, float *split, int32_t *count, int32_t *prims,
+                         int64_t *n_nodes, int64_t *n_prims);
+int mgpu_accel_destroy(mgpu_accel *accel);
+
+/* Upload accel + scene to the current device (stream-ordered copies from host memory). */
+int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void *stream, mgpu_scene **out);
+int mgpu_scene_destroy(mgpu_scene *scene);
+int mgpu_scene_bytes(const mgpu_scene *scene, uint64_t *out);
+
+/* Ray queries on device buffers (Scene::getIntersection / Scene::intersects).
+ *   rays: n * 8 floats  (origin xyz, tmin, direction xyz, tmax)
+ *   hits: n * 4 floats  (t, prim id as int bits, b1, b2); t = +inf and prim = -1 on a miss
+ *   occluded: n bytes   (1 if any hit with tmin < t < tmax)                               */
+int mgpu_trace_closest(const mgpu_scene *scene, const float *d_rays, float *d_hits, int64_t n, void *stream);
+int mgpu_trace_any(const mgpu_scene *scene, const float *d_rays, uint8_t *d_occluded, int64_t n, void *stream);
+/* Same queries with per-ray traversal counters written to d_counts (n * 4 uint32:
+ * nodes visited, leaf refs read, triangles tested, max stack depth) -- measurement only. */
+int mgpu_trace_closest_counted(const mgpu_scene *scene, const float *d_rays, float *d_hits, uint32_t *d_counts,
+                               int64_t n, void *stream);
+
+/* Film: compensated FP32 sums per pixel (rgb sum, count, rgb compensation).                */
+typedef struct mgpu_film mgpu_film;
+int mgpu_film_create(int32_t width, int32_t height, void *stream, mgpu_film **out);
+int mgpu_film_clear(mgpu_film *film, void *stream);
+int mgpu_film_destroy(mgpu_film *film);
+/* Per-pixel mean in FP64: out = host array of width*height*3 doubles (synchronises). */
+int mgpu_film_read(mgpu_film *film, double *out_mean, void *stream);
+/* Raw device film: 2 float4 per pixel (sum.rgb + count, compensation.rgb) -> host floats. */
+int mgpu_film_read_raw(mgpu_film *film, float *out8, void *stream);
+
+/* PathTracer::render over the requested sample passes (PathTracer.cpp:28-116 per path). */
+int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream);
+/* Render and also write every path's radiance (after Milton's specular channel masking)
+ * to d_path_L: (pixel * sample_count + sample) * 4 floats.  Test/measurement helper.     */
+int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,
+                      void *stream);
+int mgpu_render_stats_get(mgpu_render_stats *out); /* stats of the last render on this thread (synchronises) */
+
+/* Kernel launches issued by this library since load (for launch accounting). */
+uint64_t mgpu_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MGPU_H_ */

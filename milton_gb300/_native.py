@@ -1,0 +1,120 @@
+"""ctypes binding of libmgpu.so (include/mgpu.h, include/milton_plugin.h).
+
+There is no fallback: if the in-tree library is missing, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libmgpu.so"
+
+MGPU_OK = 0
+ERRORS = {-1: "MGPU_E_INVALID", -2: "MGPU_E_CUDA", -3: "MGPU_E_NOMEM", -4: "MGPU_E_BUDGET", -5: "MGPU_E_STATE",
+          -6: "MGPU_E_DEVICE"}
+
+
+class MgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class KdParams(C.Structure):
+    _fields_ = [("min_prims", C.c_uint32), ("max_depth", C.c_uint32), ("cost_traversal", C.c_double),
+                ("empty_bias", C.c_double), ("threads", C.c_uint32)]
+
+
+class KdStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("no_internal", "no_leaves", "min_depth", "max_depth", "sum_depth",
+                                          "min_prims", "max_prims", "sum_prims", "node_pairs", "refs",
+                                          "bytes_nodes", "bytes_refs")] + [("build_seconds", C.c_double)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("ntri", C.c_int64), ("tri_v", C.c_void_p), ("tri_n", C.c_void_p), ("tri_mat", C.c_void_p),
+                ("tri_light", C.c_void_p), ("tri_flags", C.c_void_p), ("nmat", C.c_int32),
+                ("materials", C.c_void_p), ("nlight", C.c_int32), ("lights", C.c_void_p)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("sample_begin", C.c_int32),
+                ("sample_count", C.c_int32), ("no_direct_samples", C.c_int32), ("max_depth", C.c_int32),
+                ("rr_start_depth", C.c_int32), ("efficient_direct", C.c_int32), ("wave_paths", C.c_int32),
+                ("seed", C.c_uint64), ("stream_id", C.c_uint32), ("camera", C.c_float * 11)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("paths", "extension_rays", "shadow_rays", "truncated_paths", "bounces",
+                                          "kernel_launches")]
+
+
+# (name, restype, argtypes) for every exported entry point; the ABI test checks this list
+# against include/*.h.
+SIGNATURES = [
+    ("mgpu_last_error", C.c_char_p, []),
+    ("mgpu_version", C.c_int, []),
+    ("mgpu_accel_build", C.c_int, [C.POINTER(SceneDesc), C.POINTER(KdParams), C.POINTER(C.c_void_p)]),
+    ("mgpu_accel_stats", C.c_int, [C.c_void_p, C.POINTER(KdStats)]),
+    ("mgpu_accel_serialize", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("mgpu_accel_destroy", C.c_int, [C.c_void_p]),
+    ("mgpu_scene_create", C.c_int, [C.POINTER(SceneDesc), C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("mgpu_scene_destroy", C.c_int, [C.c_void_p]),
+    ("mgpu_scene_bytes", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    ("mgpu_trace_closest", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("mgpu_trace_any", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("mgpu_trace_closest_counted", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                             C.c_void_p]),
+    ("mgpu_film_create", C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("mgpu_film_clear", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("mgpu_film_destroy", C.c_int, [C.c_void_p]),
+    ("mgpu_film_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mgpu_film_read_raw", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mgpu_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
+    ("mgpu_render_paths", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mgpu_render_stats_get", C.c_int, [C.POINTER(RenderStats)]),
+    ("mgpu_launch_count", C.c_uint64, []),
+    ("plugin_type", C.c_int, []),
+    ("plugin_new", C.c_void_p, []),
+    ("plugin_delete", None, [C.c_void_p]),
+    ("mgpu_renderer_set_value", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    ("mgpu_renderer_get_value", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_size_t]),
+    ("mgpu_renderer_set_scene", C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
+    ("mgpu_renderer_set_camera", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("mgpu_renderer_set_output", C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    ("mgpu_renderer_init", C.c_int, [C.c_void_p]),
+    ("mgpu_renderer_render", C.c_int, [C.c_void_p]),
+    ("mgpu_renderer_get_output", C.c_int, [C.c_void_p, C.c_void_p]),
+]
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+                          "(there is no CPU fallback for the GPU path)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != MGPU_OK:
+        msg = load().mgpu_last_error()
+        raise MgpuError(rc, msg.decode() if msg else "")
+
+
+def ptr(a) -> int:
+    """Address of a numpy array's data (or None)."""
+    if a is None:
+        return None
+    return a.ctypes.data

@@ -1,0 +1,304 @@
+// api.cu -- error reporting, host kd-tree objects, scene upload and film objects of libmgpu.
+#include <string.h>
+
+#include <cmath>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+
+namespace mgpu {
+
+static thread_local std::string t_last_error;
+std::atomic<uint64_t> g_launches{0};
+
+void set_error(const std::string &msg) { t_last_error = msg; }
+int fail(int code, const std::string &msg) {
+  t_last_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+  t_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? MGPU_E_NOMEM : MGPU_E_CUDA;
+}
+
+int device_sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace mgpu
+
+using namespace mgpu;
+
+extern "C" {
+
+const char *mgpu_last_error(void) { return t_last_error.c_str(); }
+int mgpu_version(void) { return 1; }
+uint64_t mgpu_launch_count(void) { return g_launches.load(); }
+
+int mgpu_accel_build(const mgpu_scene_desc *desc, const mgpu_kd_params *params, mgpu_accel **out) {
+  if (!desc || !out) return fail(MGPU_E_INVALID, "mgpu_accel_build: null argument");
+  if (desc->ntri < 0 || (desc->ntri > 0 && !desc->tri_v)) return fail(MGPU_E_INVALID, "mgpu_accel_build: bad geometry");
+  KdParams p;
+  if (params) {
+    p.min_prims = params->min_prims;
+    p.max_depth = params->max_depth;
+    p.cost_traversal = params->cost_traversal;
+    p.empty_bias = params->empty_bias;
+    p.threads = params->threads;
+  }
+  mgpu_accel *a = new (std::nothrow) mgpu_accel();
+  if (!a) return fail(MGPU_E_NOMEM, "mgpu_accel_build: out of host memory");
+  const char *err = nullptr;
+  try {
+    if (!kd_build(desc->tri_v, desc->ntri, p, a->tree, &err)) {
+      delete a;
+      return fail(MGPU_E_INVALID, std::string("mgpu_accel_build: ") + err);
+    }
+  } catch (const std::bad_alloc &) {
+    delete a;
+    return fail(MGPU_E_NOMEM, "mgpu_accel_build: out of host memory");
+  }
+  a->ntri = desc->ntri;
+  *out = a;
+  return MGPU_OK;
+}
+
+int mgpu_accel_stats(const mgpu_accel *a, mgpu_kd_stats *o) {
+  if (!a || !o) return fail(MGPU_E_INVALID, "mgpu_accel_stats: null argument");
+  const KdLog &l = a->tree.log;
+  o->no_internal = l.no_internal;
+  o->no_leaves = l.no_leaves;
+  o->min_depth = l.min_depth;
+  o->max_depth = l.max_depth;
+  o->sum_depth = l.sum_depth;
+  o->min_prims = l.min_prims;
+  o->max_prims = l.max_prims;
+  o->sum_prims = l.sum_prims;
+  o->node_pairs = a->tree.pairs.size();
+  o->refs = a->tree.refs.size();
+  o->bytes_nodes = a->tree.pairs.size() * sizeof(Pair);
+  o->bytes_refs = a->tree.refs.size() * sizeof(uint32_t);
+  o->build_seconds = a->tree.build_seconds;
+  return MGPU_OK;
+}
+
+int mgpu_accel_serialize(const mgpu_accel *a, int32_t *kind, float *split, int32_t *count, int32_t *prims,
+                         int64_t *n_nodes, int64_t *n_prims) {
+  if (!a) return fail(MGPU_E_INVALID, "mgpu_accel_serialize: null accel");
+  kd_serialize(a->tree, kind, split, count, prims, n_nodes, n_prims);
+  return MGPU_OK;
+}
+
+int mgpu_accel_destroy(mgpu_accel *a) {
+  delete a;
+  return MGPU_OK;
+}
+
+int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void *stream, mgpu_scene **out) {
+  if (!desc || !accel || !out) return fail(MGPU_E_INVALID, "mgpu_scene_create: null argument");
+  if (desc->ntri != accel->ntri) return fail(MGPU_E_INVALID, "mgpu_scene_create: accel built for another triangle count");
+  if (desc->ntri > 0 && (!desc->tri_v || !desc->tri_mat)) return fail(MGPU_E_INVALID, "mgpu_scene_create: missing arrays");
+  if (desc->nmat <= 0 || !desc->materials) return fail(MGPU_E_INVALID, "mgpu_scene_create: at least one material required");
+  if (desc->nlight < 0 || (desc->nlight > 0 && !desc->lights)) return fail(MGPU_E_INVALID, "mgpu_scene_create: bad lights");
+  const int64_t T = desc->ntri;
+  for (int64_t t = 0; t < T; ++t) {
+    if (desc->tri_mat[t] < 0 || desc->tri_mat[t] >= desc->nmat)
+      return fail(MGPU_E_INVALID, "mgpu_scene_create: material index out of range at triangle " + std::to_string(t));
+    if (desc->tri_light && (desc->tri_light[t] < -1 || desc->tri_light[t] >= desc->nlight))
+      return fail(MGPU_E_INVALID, "mgpu_scene_create: light index out of range at triangle " + std::to_string(t));
+  }
+  for (int i = 0; i < desc->nmat; ++i) {
+    float ty = desc->materials[16 * i];
+    if (!(ty == 0.0f || ty == 1.0f || ty == 2.0f))
+      return fail(MGPU_E_INVALID, "mgpu_scene_create: unknown material type at material " + std::to_string(i));
+  }
+  const KdTree &tr = accel->tree;
+  // host staging: triangles (3 x float4) and shading records (3 x float4)
+  std::vector<F4> tris((size_t)T * 3);
+  std::vector<float4> shade((size_t)T * 3);
+  for (int64_t t = 0; t < T; ++t) {
+    const float *v = desc->tri_v + t * 9;
+    uint32_t fl = desc->tri_flags ? desc->tri_flags[t] : 0u;
+    for (int k = 0; k < 3; ++k) {
+      F4 q; q.x = v[3 * k]; q.y = v[3 * k + 1]; q.z = v[3 * k + 2]; q.w = 0.0f;
+      if (k == 0) memcpy(&q.w, &fl, 4);
+      tris[3 * t + k] = q;
+    }
+    V3 e1 = v3(v[3] - v[0], v[4] - v[1], v[5] - v[2]);
+    V3 e2 = v3(v[6] - v[0], v[7] - v[1], v[8] - v[2]);
+    V3 fn = normalize(cross(e1, e2));
+    int32_t mat = desc->tri_mat[t];
+    int32_t li = desc->tri_light ? desc->tri_light[t] : -1;
+    for (int k = 0; k < 3; ++k) {
+      float4 q;
+      if (desc->tri_n) {
+        const float *n = desc->tri_n + t * 9 + 3 * k;
+        q = make_float4(n[0], n[1], n[2], 0.0f);
+      } else {
+        q = make_float4(fn.x, fn.y, fn.z, 0.0f);
+      }
+      if (k == 0) memcpy(&q.w, &mat, 4);
+      if (k == 1) memcpy(&q.w, &li, 4);
+      shade[3 * t + k] = q;
+    }
+  }
+  size_t off_pairs = 0;
+  size_t sz_pairs = tr.pairs.size() * sizeof(Pair);
+  size_t off_refs = align_up(off_pairs + sz_pairs, 256);
+  size_t sz_refs = std::max<size_t>(tr.refs.size(), 1) * sizeof(uint32_t);
+  size_t off_tris = align_up(off_refs + sz_refs, 256);
+  size_t sz_tris = std::max<size_t>(tris.size(), 1) * sizeof(F4);
+  size_t off_shade = align_up(off_tris + sz_tris, 256);
+  size_t sz_shade = std::max<size_t>(shade.size(), 1) * sizeof(float4);
+  size_t off_mats = align_up(off_shade + sz_shade, 256);
+  size_t sz_mats = (size_t)desc->nmat * 16 * sizeof(float);
+  size_t off_lights = align_up(off_mats + sz_mats, 256);
+  size_t sz_lights = std::max<size_t>((size_t)desc->nlight, 1) * 16 * sizeof(float);
+  size_t off_err = align_up(off_lights + sz_lights, 256);
+  size_t total = off_err + 256;
+
+  mgpu_scene *s = new (std::nothrow) mgpu_scene();
+  if (!s) return fail(MGPU_E_NOMEM, "mgpu_scene_create: out of host memory");
+  cudaGetDevice(&s->device);
+  cudaError_t e = cudaMalloc(&s->d_block, total);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_fail(e, "mgpu_scene_create: cudaMalloc");
+  }
+  char *base = (char *)s->d_block;
+  cudaStream_t st = as_stream(stream);
+  auto up = [&](size_t off, const void *src, size_t n) -> cudaError_t {
+    if (n == 0) return cudaSuccess;
+    return cudaMemcpyAsync(base + off, src, n, cudaMemcpyHostToDevice, st);
+  };
+  e = up(off_pairs, tr.pairs.data(), sz_pairs);
+  if (e == cudaSuccess) e = up(off_refs, tr.refs.data(), tr.refs.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = up(off_tris, tris.data(), tris.size() * sizeof(F4));
+  if (e == cudaSuccess) e = up(off_shade, shade.data(), shade.size() * sizeof(float4));
+  if (e == cudaSuccess) e = up(off_mats, desc->materials, sz_mats);
+  if (e == cudaSuccess && desc->nlight > 0) e = up(off_lights, desc->lights, (size_t)desc->nlight * 16 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + off_err, 0, 256, st);
+  // the staging vectors die at return: wait for the copies
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaFree(s->d_block);
+    delete s;
+    return cuda_fail(e, "mgpu_scene_create: upload");
+  }
+  s->view.pairs = (const Pair *)(base + off_pairs);
+  s->view.refs = (const uint32_t *)(base + off_refs);
+  s->view.tris = (const F4 *)(base + off_tris);
+  for (int k = 0; k < 3; ++k) { s->view.bmin[k] = (float)tr.bmin[k]; s->view.bmax[k] = (float)tr.bmax[k]; }
+  s->view.ntri = T;
+  s->view.npairs = tr.pairs.size();
+  s->view.nrefs = tr.refs.size();
+  s->d_shade = (float4 *)(base + off_shade);
+  s->d_mats = (float *)(base + off_mats);
+  s->d_lights = (float *)(base + off_lights);
+  s->nmat = desc->nmat;
+  s->nlight = desc->nlight;
+  s->top_pairs = tr.top_pairs;
+  s->d_err = (uint32_t *)(base + off_err);
+  s->bytes = total;
+  *out = s;
+  return MGPU_OK;
+}
+
+int mgpu_scene_destroy(mgpu_scene *s) {
+  if (!s) return MGPU_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != s->device) cudaSetDevice(s->device);
+  cudaError_t e = cudaFree(s->d_block);
+  if (cur != s->device) cudaSetDevice(cur);
+  delete s;
+  if (e != cudaSuccess) return cuda_fail(e, "mgpu_scene_destroy: cudaFree");
+  return MGPU_OK;
+}
+
+int mgpu_scene_bytes(const mgpu_scene *s, uint64_t *out) {
+  if (!s || !out) return fail(MGPU_E_INVALID, "mgpu_scene_bytes: null argument");
+  *out = s->bytes;
+  return MGPU_OK;
+}
+
+int mgpu_film_create(int32_t width, int32_t height, void *stream, mgpu_film **out) {
+  if (!out || width <= 0 || height <= 0 || (int64_t)width * height > (int64_t)1 << 31)
+    return fail(MGPU_E_INVALID, "mgpu_film_create: bad size");
+  mgpu_film *f = new (std::nothrow) mgpu_film();
+  if (!f) return fail(MGPU_E_NOMEM, "mgpu_film_create: out of host memory");
+  cudaGetDevice(&f->device);
+  f->width = width;
+  f->height = height;
+  size_t n = (size_t)width * height;
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, 2 * n * sizeof(float4));
+  if (e != cudaSuccess) {
+    delete f;
+    return cuda_fail(e, "mgpu_film_create: cudaMalloc");
+  }
+  f->d_sum = (float4 *)p;
+  f->d_c = f->d_sum + n;
+  e = cudaMemsetAsync(p, 0, 2 * n * sizeof(float4), as_stream(stream));
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    delete f;
+    return cuda_fail(e, "mgpu_film_create: clear");
+  }
+  *out = f;
+  return MGPU_OK;
+}
+
+int mgpu_film_clear(mgpu_film *f, void *stream) {
+  if (!f) return fail(MGPU_E_INVALID, "mgpu_film_clear: null film");
+  MGPU_CUDA(cudaMemsetAsync(f->d_sum, 0, 2 * (size_t)f->width * f->height * sizeof(float4), as_stream(stream)));
+  return MGPU_OK;
+}
+
+int mgpu_film_destroy(mgpu_film *f) {
+  if (!f) return MGPU_OK;
+  cudaError_t e = cudaFree(f->d_sum);
+  delete f;
+  if (e != cudaSuccess) return cuda_fail(e, "mgpu_film_destroy: cudaFree");
+  return MGPU_OK;
+}
+
+int mgpu_film_read_raw(mgpu_film *f, float *out8, void *stream) {
+  if (!f || !out8) return fail(MGPU_E_INVALID, "mgpu_film_read_raw: null argument");
+  size_t n = (size_t)f->width * f->height;
+  cudaStream_t st = as_stream(stream);
+  MGPU_CUDA(cudaMemcpyAsync(out8, f->d_sum, 2 * n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  MGPU_CUDA(cudaStreamSynchronize(st));
+  return MGPU_OK;
+}
+
+// mean = (sum - compensation) / count in FP64 (ProgressiveFilterValue::getValue,
+// ProgressiveFilterValue.h:26-31; a pixel with no samples reads as black)
+int mgpu_film_read(mgpu_film *f, double *out_mean, void *stream) {
+  if (!f || !out_mean) return fail(MGPU_E_INVALID, "mgpu_film_read: null argument");
+  size_t n = (size_t)f->width * f->height;
+  std::vector<float4> raw(2 * n);
+  int rc = mgpu_film_read_raw(f, (float *)raw.data(), stream);
+  if (rc != MGPU_OK) return rc;
+  for (size_t i = 0; i < n; ++i) {
+    const float4 s = raw[i], c = raw[n + i];
+    double cnt = s.w;
+    if (cnt > 0) {
+      out_mean[3 * i + 0] = ((double)s.x - (double)c.x) / cnt;
+      out_mean[3 * i + 1] = ((double)s.y - (double)c.y) / cnt;
+      out_mean[3 * i + 2] = ((double)s.z - (double)c.z) / cnt;
+    } else {
+      out_mean[3 * i + 0] = out_mean[3 * i + 1] = out_mean[3 * i + 2] = 0.0;
+    }
+  }
+  return MGPU_OK;
+}
+
+}  // extern "C"

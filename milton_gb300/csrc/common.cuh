@@ -1,0 +1,62 @@
+// common.cuh -- internal declarations shared by the libmgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+
+#include "../../include/mgpu.h"
+#include "hd_shade.h"
+#include "hd_trace.h"
+#include "kdbuild.h"
+
+namespace mgpu {
+
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+extern std::atomic<uint64_t> g_launches;
+
+#define MGPU_CUDA(call)                                  \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+  } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// device-side error word bits (kernels set a bit and skip the access instead of faulting)
+constexpr uint32_t kErrStack = 1u;
+constexpr uint32_t kErrIndex = 2u;
+
+int device_sm_count();
+
+}  // namespace mgpu
+
+struct mgpu_accel {
+  mgpu::KdTree tree;
+  int64_t ntri = 0;
+};
+
+struct mgpu_scene {
+  int device = 0;
+  mgpu::SceneView view{};       // device pointers
+  float4 *d_shade = nullptr;    // 3 per triangle: (n0, mat), (n1, light), (n2, 0)
+  float *d_mats = nullptr;
+  float *d_lights = nullptr;
+  int32_t nmat = 0, nlight = 0;
+  uint32_t top_pairs = 0;
+  void *d_block = nullptr;      // one allocation holding everything above
+  uint64_t bytes = 0;
+  uint32_t *d_err = nullptr;    // device error word
+};
+
+struct mgpu_film {
+  int device = 0;
+  int32_t width = 0, height = 0;
+  float4 *d_sum = nullptr;  // rgb sum + sample count
+  float4 *d_c = nullptr;    // Kahan compensation
+};

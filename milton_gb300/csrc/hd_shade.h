@@ -1,0 +1,258 @@
+// hd_shade.h -- camera rays, Milton's BSDFs and emitters, area-light sampling (host/device).
+//
+// FP32 restatement of the shading half of PathTracer::_evaluate.  Each function names the
+// Milton routine whose behaviour it reproduces; lobe choice and pdf follow the reference
+// exactly (including its quirks), only the precision differs.
+#pragma once
+
+#include "hd_math.h"
+
+namespace mgpu {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kEps = 1e-7f;      // Milton's EPSILON, used where it shapes sampling (Phong lobe pick)
+constexpr float kAir = 1.0003f;    // IndexOfRefraction::AIR (IndexOfRefraction.cpp:16)
+
+// Material record (16 floats, 4 x float4 in device memory)
+struct Material {
+  int type;          // 0 diffuse, 1 modified Phong, 2 dielectric
+  V3 kd, ks;
+  float n, ior, transparency;
+  float kda, ksa;    // channel averages (ModifiedPhongBSDF::init)
+};
+
+MGPU_HD Material material_from(const float *m) {
+  Material r;
+  r.type = (int)m[0];
+  r.kd = v3(m[1], m[2], m[3]);
+  r.ks = v3(m[4], m[5], m[6]);
+  r.n = m[7];
+  r.ior = m[8];
+  r.transparency = m[9];
+  r.kda = (r.kd.x + r.kd.y + r.kd.z) / 3.0f;
+  r.ksa = (r.ks.x + r.ks.y + r.ks.z) / 3.0f;
+  return r;
+}
+
+MGPU_HD bool is_specular(const Material &m) { return m.type == 2; }
+
+// Quad light = Milton `Plane` under a transform
+struct Light {
+  V3 center, ex, ez, normal;
+  float area;
+  V3 Le;
+};
+
+MGPU_HD Light light_from(const float *l) {
+  Light r;
+  r.center = v3(l[0], l[1], l[2]);
+  r.ex = v3(l[3], l[4], l[5]);
+  r.ez = v3(l[6], l[7], l[8]);
+  r.normal = normalize(v3(l[9], l[10], l[11]));
+  r.area = l[12];
+  r.Le = v3(l[13], l[14], l[15]);
+  return r;
+}
+
+// Pinhole camera (ThinLensCamera::getWorldRay with aperture 0, ThinLensCamera.cpp:131-135)
+struct Camera {
+  V3 eye, u, v, n;
+  float tan_w, tan_h;
+};
+
+MGPU_HD V3 camera_dir(const Camera &c, float x, float y) {
+  float nx = 2.0f * x - 1.0f, ny = 1.0f - 2.0f * y;
+  return normalize(c.u * (c.tan_w * nx) + c.v * (c.tan_h * ny) - c.n);
+}
+
+// Vector::getOrthonormalBasis (Vector.inl:527-538)
+MGPU_HD void onb(V3 n, V3 &U, V3 &W) {
+  V3 up = v3(0.0f, 1.0f, 0.0f);
+  if (fabsf(dot(up, n)) > 0.8f) up = v3(1.0f, 0.0f, 0.0f);
+  U = normalize(cross(up, n));
+  W = normalize(cross(n, U));
+}
+
+// Vector3::cosRandom + convertHemisphere (Vector.cpp:21-29, Vector3.inl:18-21):
+// theta = acos(sqrt(u1)), phi = 2 pi u2, local (sin t cos p, cos t, sin t sin p)
+MGPU_HD V3 cos_random(V3 n, float u1, float u2) {
+  float ct = sqrtf(u1), st = sqrtf(fmaxf(0.0f, 1.0f - u1));
+  float phi = 2.0f * kPi * u2;
+  float sp, cp;
+#if defined(__CUDA_ARCH__)
+  sincosf(phi, &sp, &cp);
+#else
+  sp = sinf(phi); cp = cosf(phi);
+#endif
+  V3 U, W;
+  onb(n, U, W);
+  return U * (st * cp) + n * ct + W * (st * sp);
+}
+
+MGPU_HD V3 reflect(V3 wi, V3 n) { return n * (-2.0f * dot(wi, n)) + wi; }
+
+// Vector::refractVector (Vector.inl:467-495); ok = false on total internal reflection
+MGPU_HD V3 refract(V3 wi, V3 normal, float in, float out, bool &ok) {
+  V3 w = -wi, nrm;
+  float eta;
+  if (dot(wi, normal) < 0.0f) { nrm = normal; eta = in / out; }
+  else { nrm = -normal; eta = out / in; }
+  float d = dot(w, nrm);
+  float det = 1.0f - eta * eta * (1.0f - d * d);
+  if (det < 0.0f) { ok = false; return v3(0.0f, 0.0f, 0.0f); }
+  ok = true;
+  return w * (-eta) + nrm * (eta * d - sqrtf(det));
+}
+
+// Fresnel::getFr (Fresnel.h:45-90), unpolarised dielectric reflectance
+MGPU_HD float fresnel_cos(float ci, float n1, float n2) {
+  float si = sqrtf(fmaxf(0.0f, 1.0f - ci * ci));
+  float snell = (n1 / n2) * si;
+  if (fabsf(snell) >= 1.0f) return 1.0f;
+  float ct = sqrtf(fmaxf(0.0f, 1.0f - snell * snell));
+  float n1ci = n1 * ci, n1ct = n1 * ct, n2ci = n2 * ci, n2ct = n2 * ct;
+  float rs = (n1ci - n2ct) / (n1ci + n2ct);
+  float rp = (n1ct - n2ci) / (n1ct + n2ci);
+  return (rs * rs + rp * rp) * 0.5f;
+}
+
+MGPU_HD float fresnel(V3 wi, V3 N, float n1, float n2) {
+  float c = dot(N, wi);
+  if (c < 0.0f) return fresnel_cos(-c, n1, n2);
+  return fresnel_cos(c, n2, n1);
+}
+
+// BSDF evaluate fs(wi -> wo) for the non-specular BSDFs (the dielectric is only ever
+// evaluated on its own sample, which bsdf_sample handles through lobe flags).
+//   Diffuse: DiffuseBSDF::evaluate (DiffuseBSDF.cpp:41-48), one-sided
+//   Phong:   ModifiedPhongBSDF::evaluate (ModifiedPhongBSDF.cpp:163-181), including the
+//            reference's 1/kda and 1/ksa lobe normalisation
+MGPU_HD V3 bsdf_eval(const Material &m, V3 ns, V3 wi, V3 wo) {
+  if (m.type == 0) {
+    if (dot(ns, wi) >= 0.0f || dot(ns, wo) <= 0.0f) return v3(0.0f, 0.0f, 0.0f);
+    return m.kd * (1.0f / kPi);
+  }
+  if (m.type == 1) {
+    if (dot(ns, wo) <= 0.0f) return v3(0.0f, 0.0f, 0.0f);
+    V3 r = reflect(wi, ns);
+    float a = fminf(fmaxf(dot(r, wo), 0.0f), 1.0f);
+    float fsd = m.kda > 0.0f ? 1.0f / (kPi * m.kda) : 0.0f;
+    float fss = m.ksa > 0.0f ? ((m.n + 2.0f) / (2.0f * kPi * m.ksa)) * powf(a, m.n) : 0.0f;
+    return m.kd * fsd + m.ks * fss;
+  }
+  return v3(0.0f, 0.0f, 0.0f);
+}
+
+enum Event { EV_NONE = 0, EV_DIFFUSE = 1, EV_SPECULAR = 2, EV_REFLECT = 3, EV_REFRACT = 4, EV_ZERO_PDF = -1 };
+
+// BSDF::sample + getPd + evaluate/pdf; returns the event and fs = f / pdf.
+//   Diffuse:    DiffuseBSDF.cpp:21-39
+//   Phong:      ModifiedPhongBSDF.cpp:83-158 (lobe by p0 = U - EPSILON against kda, kda + ksa)
+//   Dielectric: DielectricBSDF.cpp:56-157 with the path's ior index (fs = ks on reflection,
+//               ks * e_index on refraction, pdf 1)
+MGPU_HD int bsdf_sample(const Material &m, V3 ns, V3 wi, uint32_t ior_index, float u0, float u1, float u2, V3 &wo,
+                        V3 &fs) {
+  fs = v3(0.0f, 0.0f, 0.0f);
+  if (m.type == 0) {
+    if (dot(ns, wi) > 0.0f) return EV_NONE;
+    wo = cos_random(ns, u0, u1);
+    float c = dot(ns, wo);
+    if (!(c > 0.0f)) return EV_ZERO_PDF;
+    fs = bsdf_eval(m, ns, wi, wo) * kPi;
+    return EV_DIFFUSE;
+  }
+  if (m.type == 1) {
+    float p0 = u0 - kEps;
+    int ev;
+    if (p0 <= m.kda) {
+      ev = EV_DIFFUSE;
+      wo = cos_random(ns, u1, u2);
+    } else if (p0 <= m.kda + m.ksa) {
+      ev = EV_SPECULAR;
+      float ca = powf(u1, 1.0f / (m.n + 1.0f));
+      float sa = sqrtf(fmaxf(0.0f, 1.0f - ca * ca));
+      float phi = 2.0f * kPi * u2;
+      float sp, cp;
+#if defined(__CUDA_ARCH__)
+      sincosf(phi, &sp, &cp);
+#else
+      sp = sinf(phi); cp = cosf(phi);
+#endif
+      V3 R = reflect(wi, ns);
+      V3 r = R, uu, vv;
+      if (fabsf(dot(ns, r)) < 0.95f) {
+        uu = normalize(cross(r, ns));
+        vv = cross(uu, r);
+      } else {
+        r = normalize(r);
+        onb(r, vv, uu);
+      }
+      V3 cand = uu * (sa * cp) + r * ca + vv * (sa * sp);
+      wo = dot(ns, cand) > 0.0f ? cand : R;
+    } else {
+      return EV_NONE;
+    }
+    float cosA = dot(ns, wo);
+    if (!(cosA > 0.0f)) return EV_ZERO_PDF;
+    float pdf;
+    if (ev == EV_SPECULAR) {
+      V3 r = reflect(wi, ns);
+      float ca = fabsf(dot(r, wo));
+      pdf = fminf(1.0f, (m.n + 1.0f) / (2.0f * kPi) * powf(ca, m.n)) / cosA;
+    } else {
+      pdf = (fabsf(cosA) / kPi) / cosA;
+    }
+    if (!(pdf > 0.0f)) return EV_ZERO_PDF;
+    fs = bsdf_eval(m, ns, wi, wo) * (1.0f / pdf);
+    return ev;
+  }
+  // dielectric
+  V3 N = dot(ns, wi) > 0.0f ? -ns : ns;
+  bool ok;
+  V3 wt = refract(wi, ns, kAir, m.ior, ok);
+  if (ok) {
+    float fr = fresnel(wi, ns, kAir, m.ior);
+    float fst = m.transparency * (1.0f - fr);
+    if (u0 < fst) {
+      wo = wt;
+      fs = v3(ior_index == 0 ? m.ks.x : 0.0f, ior_index == 1 ? m.ks.y : 0.0f, ior_index == 2 ? m.ks.z : 0.0f);
+      return EV_REFRACT;
+    }
+  }
+  wo = reflect(wi, N);
+  fs = m.ks;
+  return EV_REFLECT;
+}
+
+// OrientedEmitter::getLe (OrientedEmitter.cpp:17-23) with radiance already power/(area pi)
+MGPU_HD V3 emitted(V3 Le, V3 n, V3 w) { return dot(n, w) > 0.0f ? Le : v3(0.0f, 0.0f, 0.0f); }
+
+// Origin offset against self-intersection: Waechter and Binder, "A Fast and Robust Method
+// for Avoiding Self-Intersection", Ray Tracing Gems ch. 6 (2019).  n points to the side the
+// new ray leaves from.
+MGPU_HD V3 offset_origin(V3 p, V3 n) {
+  const float origin = 1.0f / 32.0f, fscale = 1.0f / 65536.0f, iscale = 256.0f;
+  int ix = (int)(iscale * n.x), iy = (int)(iscale * n.y), iz = (int)(iscale * n.z);
+  float px = bits_f(f_bits(p.x) + (uint32_t)((p.x < 0.0f) ? -ix : ix));
+  float py = bits_f(f_bits(p.y) + (uint32_t)((p.y < 0.0f) ? -iy : iy));
+  float pz = bits_f(f_bits(p.z) + (uint32_t)((p.z < 0.0f) ? -iz : iz));
+  return v3(fabsf(p.x) < origin ? p.x + fscale * n.x : px, fabsf(p.y) < origin ? p.y + fscale * n.y : py,
+            fabsf(p.z) < origin ? p.z + fscale * n.z : pz);
+}
+
+// Path flags kept in the radiance record's w word
+constexpr uint32_t kFlagIorMask = 3u;       // ior index 0..2 (PathTracer.cpp:32)
+constexpr uint32_t kFlagSpecular = 4u;      // data["specular"] (PathTracer.cpp:45-46)
+constexpr uint32_t kFlagContinued0 = 8u;    // the depth-0 vertex spawned a continuation
+constexpr uint32_t kFlagTruncated = 16u;    // hit the hard depth cap
+
+// Milton's single-wavelength masking at depth 0 (PathTracer.cpp:107-114)
+MGPU_HD V3 apply_mask(V3 L, uint32_t flags) {
+  if ((flags & kFlagSpecular) && (flags & kFlagContinued0)) {
+    uint32_t k = flags & kFlagIorMask;
+    return v3(k == 0 ? 3.0f * L.x : 0.0f, k == 1 ? 3.0f * L.y : 0.0f, k == 2 ? 3.0f * L.z : 0.0f);
+  }
+  return L;
+}
+
+}  // namespace mgpu

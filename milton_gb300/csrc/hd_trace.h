@@ -1,0 +1,267 @@
+// hd_trace.h -- kd-tree traversal and watertight FP32 ray/triangle tests (host/device).
+//
+// Layout in device memory (built by kdbuild.cpp):
+//   pairs  uint4[npairs]   one 16-byte record = the two children of an interior node, fetched
+//                          with a single 128-bit load; pair 0 holds the root (slot 0) and an
+//                          unused slot.  Each 8-byte slot is {w0, w1}:
+//                            interior: w0 = child_pair << 2 | axis (0..2), w1 = split (float bits)
+//                            leaf:     w0 = count << 2 | 3, w1 = first ref (count > 1) or the
+//                                      triangle itself (count == 1)
+//   refs   uint32[nrefs]   leaf triangle lists, each stored in reverse of Milton's list order so
+//                          that a forward scan visits primitives in the order kdTreeAccel's
+//                          `for (i = n; i--;)` loop does (kdTreeAccel.cpp:973-996).
+//   tris   float4[3*ntri]  v0, v1, v2 (world space); v0.w carries the triangle flags.
+//
+// The traversal follows kdTreeAccel::getIntersection / intersects (kdTreeAccel.cpp:893-1094):
+// root slab clip, near/far ordering by the sign of (split - origin) and the direction, a stack
+// of (far node, tmax), early exit once the best hit lies inside the current cell.  Two things
+// differ on purpose: the best hit is kept across leaves (not reset per cell), and the cell
+// interval is widened by a relative epsilon instead of Milton's absolute 1e-7, both because
+// the arithmetic is FP32.
+#pragma once
+
+#include "hd_math.h"
+
+#if !defined(__CUDACC__)
+#include <math.h>
+#endif
+
+namespace mgpu {
+
+constexpr int kMaxStack = 64;      // >= the deepest tree the builder will emit
+constexpr uint32_t kLeafTag = 3u;
+
+struct F4 {
+  float x, y, z, w;
+};
+
+struct Pair {
+  uint32_t a0, a1, b0, b1;
+};
+
+struct SceneView {
+  const Pair *pairs;
+  const uint32_t *refs;
+  const F4 *tris;          // 3 per triangle
+  float bmin[3], bmax[3];  // root bounds
+  int64_t ntri;
+  uint64_t npairs, nrefs;
+};
+
+struct Ray {
+  V3 o;
+  float tmin;
+  V3 d;
+  float tmax;
+};
+
+struct Hit {
+  float t;
+  int32_t prim;
+  float b1, b2;  // barycentric weights of v1 and v2
+};
+
+struct TraceCounts {
+  uint32_t nodes, refs, tris, max_stack;
+};
+
+MGPU_HD float fabs_(float x) { return fabsf(x); }
+
+// Watertight ray/triangle intersection: Woop, Benthin, Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2(1), 2013.  Per-ray shear constants are precomputed in RayPre.
+struct RayPre {
+  int kx, ky, kz;
+  float sx, sy, sz;
+  V3 o;
+};
+
+MGPU_HD RayPre precompute(const Ray &r) {
+  RayPre p;
+  float ax = fabsf(r.d.x), ay = fabsf(r.d.y), az = fabsf(r.d.z);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz + 1; if (kx == 3) kx = 0;
+  int ky = kx + 1; if (ky == 3) ky = 0;
+  float dz = comp(r.d, kz);
+  if (dz < 0.0f) { int t = kx; kx = ky; ky = t; }
+  p.kx = kx; p.ky = ky; p.kz = kz;
+  p.sx = comp(r.d, kx) / dz;
+  p.sy = comp(r.d, ky) / dz;
+  p.sz = 1.0f / dz;
+  p.o = r.o;
+  return p;
+}
+
+// Tests one triangle.  On a hit with tmin < t < tbest returns true and fills t, b1, b2.
+// culled: accept only rays arriving on the side that (v1-v0) x (v2-v0) faces, like Milton's
+// back-face culled `Triangle` (det = e1 . (d x e2) > 0 in Triangle.cpp:245-248).
+MGPU_HD bool intersect_tri(const RayPre &p, V3 v0, V3 v1, V3 v2, bool culled, float tmin, float tbest, float &t_out,
+                           float &b1_out, float &b2_out) {
+  V3 A = v0 - p.o, B = v1 - p.o, C = v2 - p.o;
+  float Akz = comp(A, p.kz), Bkz = comp(B, p.kz), Ckz = comp(C, p.kz);
+  float Ax = comp(A, p.kx) - p.sx * Akz, Ay = comp(A, p.ky) - p.sy * Akz;
+  float Bx = comp(B, p.kx) - p.sx * Bkz, By = comp(B, p.ky) - p.sy * Bkz;
+  float Cx = comp(C, p.kx) - p.sx * Ckz, Cy = comp(C, p.ky) - p.sy * Ckz;
+  float U = Cx * By - Cy * Bx;
+  float Vv = Ax * Cy - Ay * Cx;
+  float W = Bx * Ay - By * Ax;
+  if (U == 0.0f || Vv == 0.0f || W == 0.0f) {
+    // edge case: redo the 2D cross products in double so that shared edges stay watertight
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    Vv = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  bool anyneg = (U < 0.0f || Vv < 0.0f || W < 0.0f);
+  bool anypos = (U > 0.0f || Vv > 0.0f || W > 0.0f);
+  if (anyneg && anypos) return false;
+  float det = U + Vv + W;
+  if (det == 0.0f) return false;
+  // orientation: with this permutation det > 0 <=> the ray arrives on the side that
+  // (v1-v0) x (v2-v0) faces, i.e. Milton's det = e1 . (d x e2) > 0
+  if (culled && det < 0.0f) return false;
+  float Az = p.sz * Akz, Bz = p.sz * Bkz, Cz = p.sz * Ckz;
+  float T = U * Az + Vv * Bz + W * Cz;
+  float rcp = 1.0f / det;
+  float t = T * rcp;
+  if (!(t > tmin && t < tbest)) return false;
+  t_out = t;
+  b1_out = Vv * rcp;
+  b2_out = W * rcp;
+  return true;
+}
+
+// Node fetch: device code reads through the read-only path; a shared-memory copy of the top
+// pairs can be supplied by the kernel (top != nullptr, ntop pairs).
+MGPU_HD Pair load_pair(const SceneView &s, const Pair *top, uint32_t ntop, uint32_t idx) {
+  if (top != nullptr && idx < ntop) return top[idx];
+#if defined(__CUDA_ARCH__)
+  uint4 q = __ldg(reinterpret_cast<const uint4 *>(s.pairs) + idx);
+  Pair r; r.a0 = q.x; r.a1 = q.y; r.b0 = q.z; r.b1 = q.w;
+  return r;
+#else
+  return s.pairs[idx];
+#endif
+}
+
+MGPU_HD F4 load_f4(const F4 *p, int64_t i) {
+#if defined(__CUDA_ARCH__)
+  float4 q = __ldg(reinterpret_cast<const float4 *>(p) + i);
+  F4 r; r.x = q.x; r.y = q.y; r.z = q.z; r.w = q.w;
+  return r;
+#else
+  return p[i];
+#endif
+}
+
+MGPU_HD uint32_t load_u32(const uint32_t *p, uint64_t i) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(p + i);
+#else
+  return p[i];
+#endif
+}
+
+// root slab clip, AABB.inl:25-56
+MGPU_HD bool clip_root(const SceneView &s, const Ray &r, V3 inv, float &t0, float &t1) {
+  float lo = -INFINITY, hi = INFINITY;
+  const float o[3] = {r.o.x, r.o.y, r.o.z};
+  const float iv[3] = {inv.x, inv.y, inv.z};
+  for (int k = 0; k < 3; ++k) {
+    float a = (s.bmin[k] - o[k]) * iv[k];
+    float b = (s.bmax[k] - o[k]) * iv[k];
+    float n = fminf(a, b), f = fmaxf(a, b);
+    if (a != a || b != b) {  // 0 * inf: origin on a slab plane with d parallel to it
+      n = -INFINITY; f = INFINITY;
+      if (o[k] < s.bmin[k] || o[k] > s.bmax[k]) return false;
+    }
+    lo = fmaxf(lo, n);
+    hi = fminf(hi, f);
+  }
+  t0 = lo; t1 = hi;
+  return lo <= hi;
+}
+
+constexpr float kCellEps = 1.0f / 262144.0f;  // relative widening of cell intervals (2^-18)
+
+// ANY = shadow query (returns on the first hit inside (tmin, tmax)).
+template <bool ANY, bool COUNT>
+MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *top, uint32_t ntop, TraceCounts *cnt) {
+  hit.t = INFINITY; hit.prim = -1; hit.b1 = 0.0f; hit.b2 = 0.0f;
+  if (s.ntri <= 0) return false;
+  V3 inv = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  float t0, t1;
+  if (!clip_root(s, r, inv, t0, t1)) return false;
+  float tmin = fmaxf(t0, r.tmin);
+  float tmax = fminf(t1, r.tmax);
+  if (tmin > tmax) return false;
+  RayPre pre = precompute(r);
+  float best = r.tmax;
+  int32_t best_prim = -1;
+  float bb1 = 0.0f, bb2 = 0.0f;
+
+  struct Entry { uint32_t w0, w1; float tmax; };
+  Entry stack[kMaxStack];
+  int sp = 0;
+  const float o[3] = {r.o.x, r.o.y, r.o.z};
+  const float dd[3] = {r.d.x, r.d.y, r.d.z};
+  const float iv[3] = {inv.x, inv.y, inv.z};
+
+  Pair root = load_pair(s, top, ntop, 0);
+  uint32_t w0 = root.a0, w1 = root.a1;
+  for (;;) {
+    while ((w0 & 3u) != kLeafTag) {
+      if (COUNT) cnt->nodes++;
+      int ax = (int)(w0 & 3u);
+      float split = bits_f(w1);
+      float diff = split - o[ax];
+      float dt = diff * iv[ax];
+      bool rev = diff <= 0.0f ? (dd[ax] <= 0.0f) : (dd[ax] < 0.0f);
+      Pair pr = load_pair(s, top, ntop, w0 >> 2);
+      uint32_t n0 = rev ? pr.b0 : pr.a0, n1 = rev ? pr.b1 : pr.a1;
+      uint32_t f0 = rev ? pr.a0 : pr.b0, f1 = rev ? pr.a1 : pr.b1;
+      float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
+      if (dt > tmax + slack || dt != dt) {
+        w0 = n0; w1 = n1;               // far child not reached inside this cell
+      } else if (dt < tmin - slack) {
+        w0 = f0; w1 = f1;               // near child lies behind the cell
+      } else {
+        if (sp < kMaxStack) {
+          stack[sp].w0 = f0; stack[sp].w1 = f1; stack[sp].tmax = tmax;
+          ++sp;
+          if (COUNT && (uint32_t)sp > cnt->max_stack) cnt->max_stack = (uint32_t)sp;
+        }
+        w0 = n0; w1 = n1;
+        tmax = fminf(tmax, dt);
+      }
+    }
+    if (COUNT) cnt->nodes++;
+    uint32_t count = w0 >> 2;
+    for (uint32_t i = 0; i < count; ++i) {
+      uint32_t tri = (count == 1) ? w1 : load_u32(s.refs, (uint64_t)w1 + i);
+      if (COUNT) { cnt->refs += (count == 1) ? 0u : 1u; cnt->tris++; }
+      F4 a = load_f4(s.tris, 3 * (int64_t)tri + 0);
+      F4 b = load_f4(s.tris, 3 * (int64_t)tri + 1);
+      F4 c = load_f4(s.tris, 3 * (int64_t)tri + 2);
+      bool culled = (f_bits(a.w) & 1u) != 0u;
+      float t, b1, b2;
+      if (intersect_tri(pre, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), culled, r.tmin, best, t, b1,
+                        b2)) {
+        best = t; best_prim = (int32_t)tri; bb1 = b1; bb2 = b2;
+        if (ANY) {
+          hit.t = t; hit.prim = best_prim; hit.b1 = b1; hit.b2 = b2;
+          return true;
+        }
+      }
+    }
+    if (!ANY && best_prim >= 0 && best <= tmax + kCellEps * fabsf(tmax)) break;  // early exit
+    if (sp == 0) break;
+    --sp;
+    tmin = tmax;
+    w0 = stack[sp].w0; w1 = stack[sp].w1; tmax = stack[sp].tmax;
+    if (!ANY && best_prim >= 0 && best < tmin) break;
+  }
+  if (best_prim < 0) return false;
+  hit.t = best; hit.prim = best_prim; hit.b1 = bb1; hit.b2 = bb2;
+  return true;
+}
+
+}  // namespace mgpu

@@ -1,0 +1,597 @@
+// render.cu -- wavefront path tracer: generate -> (extend -> shade -> shadow)* -> accumulate.
+//
+// One wave = a range of pixel slots (8x8 tiles, row-major tile order) x a range of sample
+// passes.  Per path the state is split in two:
+//   path_L[p]     float4  radiance accumulated so far (rgb) + path flags (w) -- path-indexed,
+//                          updated by shade (emission) and shadow (direct light), read once by
+//                          accumulate;
+//   ray queue     3 x float4 per live path (origin + path index, direction, throughput + depth
+//                          state), compacted every bounce by warp ballot + one atomicAdd per warp.
+// Shadow work is one task per non-specular hit (DirectIllumination::evaluate over all lights,
+// DirectIllumination.cpp:46-138): the shadow kernel samples every light, evaluates the BSDF and
+// traces the any-hit rays itself, so each path's radiance is written by exactly one thread per
+// kernel and the image does not depend on queue order.
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace mgpu {
+
+constexpr int kBlock = 128;
+constexpr int kHardCap = 1024;          // vertex cap when max_depth = 0 (Milton has none)
+constexpr int kCtrRay = 0;              // counters[kCtrRay + b]  live paths at bounce b
+constexpr int kCtrNee = kHardCap + 8;   // counters[kCtrNee + b]  shadow tasks at bounce b
+constexpr int kCtrTrunc = 2 * (kHardCap + 8);
+constexpr int kCtrShadowRays = kCtrTrunc + 1;
+constexpr int kNumCounters = kCtrTrunc + 8;
+constexpr float kShadowMargin = 1e-4f;  // shadow rays stop this fraction short of the light
+
+struct RenderArgs {
+  SceneView view;
+  uint32_t ntop;
+  const float4 *shade;
+  const float4 *mats;    // 4 per material
+  const float4 *lights;  // 4 per light
+  int32_t nlight;
+  Camera cam;
+  Rng rng;
+  int32_t W, H, spp, side, s2;
+  int32_t nds, nds_side;
+  int32_t max_depth, rr_start, efficient;
+  int32_t tiles_x;
+  int64_t slot0, nslots;
+  int32_t s0, ns;        // samples [s0, s0 + ns) of this wave
+  int32_t sample_begin, sample_count;
+  float4 *path_L;
+  float4 *qo[2], *qd[2], *qt[2];
+  float4 *qhit;
+  float4 *np_, *nn_, *nw_, *nt_, *ng_;  // shadow task queue
+  uint32_t *counters;
+  unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] truncated paths, [3] bounces
+  int32_t max_b;
+  float4 *film_sum, *film_c;
+  float4 *path_out;      // optional
+};
+
+__device__ __forceinline__ bool slot_pixel(const RenderArgs &a, int64_t slot, int &x, int &y) {
+  int64_t tile = slot >> 6;
+  int within = (int)(slot & 63);
+  x = (int)(tile % a.tiles_x) * 8 + (within & 7);
+  y = (int)(tile / a.tiles_x) * 8 + (within >> 3);
+  return x < a.W && y < a.H;
+}
+
+// global path id (pixel * spp + sample) for wave-local path p
+__device__ __forceinline__ uint64_t path_id(const RenderArgs &a, int64_t p, int &x, int &y, int &s) {
+  int64_t slot = a.slot0 + p / a.ns;
+  s = a.s0 + (int)(p % a.ns);
+  slot_pixel(a, slot, x, y);
+  return ((uint64_t)y * a.W + x) * (uint64_t)a.spp + (uint64_t)s;
+}
+
+// warp-aggregated queue append: returns the slot for this lane (valid only if want)
+__device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
+  unsigned active = __activemask();
+  unsigned mask = __ballot_sync(active, want);
+  if (mask == 0) return 0;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+  base = __shfl_sync(active, base, leader);
+  return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ Material load_mat(const RenderArgs &a, int i) {
+  float m[16];
+  float4 *mm = reinterpret_cast<float4 *>(m);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) mm[k] = __ldg(a.mats + 4 * i + k);
+  return material_from(m);
+}
+
+__device__ __forceinline__ Light load_light(const RenderArgs &a, int i) {
+  float l[16];
+  float4 *ll = reinterpret_cast<float4 *>(l);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) ll[k] = __ldg(a.lights + 4 * i + k);
+  return light_from(l);
+}
+
+__device__ __forceinline__ void load_top(const RenderArgs &a) {
+  extern __shared__ uint4 smem_top[];
+  for (uint32_t i = threadIdx.x; i < a.ntop; i += blockDim.x)
+    smem_top[i] = __ldg(reinterpret_cast<const uint4 *>(a.view.pairs) + i);
+  __syncthreads();
+}
+
+__device__ __forceinline__ const Pair *top_ptr(const RenderArgs &a) {
+  extern __shared__ uint4 smem_top[];
+  return a.ntop ? reinterpret_cast<const Pair *>(smem_top) : nullptr;
+}
+
+// ---------------------------------------------------------------------------------------
+// generate: camera rays for every path of the wave (RayTracer::sample, RayTracer.cpp:19-30;
+// SuperSampleGenerator strata, SuperSampleGenerator.cpp:60-90)
+__global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
+  const int64_t n = a.nslots * a.ns;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    int64_t p = base + threadIdx.x;
+    bool valid = p < n;
+    bool live = false;
+    float4 o4 = make_float4(0, 0, 0, 0), d4 = o4;
+    if (valid) {
+      int x, y, s;
+      uint64_t pid = path_id(a, p, x, y, s);
+      live = x < a.W && y < a.H;
+      uint32_t flags = 0;
+      if (live) {
+        uint64_t pix = (uint64_t)y * a.W + x;
+        int k = s % a.s2;
+        F4u j = uniforms(a.rng, pix * (uint64_t)a.s2 + (uint64_t)k, kDepthJitter, 0);
+        float px = ((float)x + ((float)(k % a.side) + j.a) / (float)a.side) / (float)a.W;
+        float py = ((float)y + ((float)(k / a.side) + j.b) / (float)a.side) / (float)a.H;
+        F4u ui = uniforms(a.rng, pid, kDepthPathInit, 0);
+        uint32_t ior = min((uint32_t)(ui.a * 3.0f), 2u);
+        flags = ior;
+        V3 d = camera_dir(a.cam, px, py);
+        o4 = make_float4(a.cam.eye.x, a.cam.eye.y, a.cam.eye.z, __int_as_float((int)p));
+        d4 = make_float4(d.x, d.y, d.z, 0.0f);
+      }
+      a.path_L[p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(flags));
+    }
+    uint32_t q = warp_append(&a.counters[kCtrRay + 0], live);
+    if (live) {
+      a.qo[0][q] = o4;
+      a.qd[0][q] = d4;
+      a.qt[0][q] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+    }
+  }
+}
+
+// extend: closest hit for the live queue of bounce b
+__global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
+  load_top(a);
+  const Pair *top = top_ptr(a);
+  const uint32_t n = a.counters[kCtrRay + b];
+  const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 o = qo[i], d = qd[i];
+    Ray r;
+    r.o = v3(o.x, o.y, o.z);
+    r.tmin = 0.0f;
+    r.d = v3(d.x, d.y, d.z);
+    r.tmax = INFINITY;
+    Hit h;
+    bool hit = traverse<false, false>(a.view, r, h, top, a.ntop, nullptr);
+    a.qhit[i] = make_float4(hit ? h.t : INFINITY, __int_as_float(hit ? h.prim : -1), h.b1, h.b2);
+  }
+}
+
+// shade: emission, shadow task, BSDF sample and Russian roulette (PathTracer.cpp:36-115)
+__global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
+  const uint32_t n = a.counters[kCtrRay + b];
+  const int cur = b & 1, nxt = (b + 1) & 1;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    uint32_t i = base + threadIdx.x;
+    bool valid = i < n;
+    bool want_next = false, want_nee = false;
+    float4 no_o, no_d, no_t;
+    float4 ne_p, ne_n, ne_w, ne_t, ne_g;
+    if (valid) {
+      float4 o4 = a.qo[cur][i], d4 = a.qd[cur][i], t4 = a.qt[cur][i], h4 = a.qhit[i];
+      int64_t p = (int64_t)__float_as_int(o4.w);
+      uint32_t state = __float_as_uint(t4.w);
+      int depth = (int)(state & 0xFFFFu);
+      bool ec = (state >> 16) & 1u;
+      V3 thr = v3(t4.x, t4.y, t4.z);
+      V3 d = v3(d4.x, d4.y, d4.z);
+      int prim = __float_as_int(h4.y);
+      float4 L4 = a.path_L[p];
+      uint32_t flags = __float_as_uint(L4.w);
+      V3 L = v3(L4.x, L4.y, L4.z);
+      if (prim >= 0) {
+        int x, y, s;
+        uint64_t pid = path_id(a, p, x, y, s);
+        float t = h4.x, b1 = h4.z, b2 = h4.w, b0 = 1.0f - b1 - b2;
+        float4 va = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim);
+        float4 vb = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim + 1);
+        float4 vc = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim + 2);
+        float4 s0 = __ldg(a.shade + 3 * (int64_t)prim), s1 = __ldg(a.shade + 3 * (int64_t)prim + 1),
+               s2 = __ldg(a.shade + 3 * (int64_t)prim + 2);
+        V3 v0 = v3(va.x, va.y, va.z), v1 = v3(vb.x, vb.y, vb.z), v2 = v3(vc.x, vc.y, vc.z);
+        V3 P = v0 * b0 + v1 * b1 + v2 * b2;
+        V3 ns = normalize(v3(s0.x, s0.y, s0.z) * b0 + v3(s1.x, s1.y, s1.z) * b1 + v3(s2.x, s2.y, s2.z) * b2);
+        V3 ng = normalize(cross(v1 - v0, v2 - v0));
+        int mi = __float_as_int(s0.w);
+        int li = __float_as_int(s1.w);
+        Material m = load_mat(a, mi);
+        bool spec = is_specular(m);
+        if (spec) flags |= kFlagSpecular;
+        if (li >= 0) {
+          Light lt = load_light(a, li);
+          V3 Le = emitted(lt.Le, ns, -d);
+          if (!a.efficient || depth == 0) L = L + mul(thr, Le);
+          else if (ec) L = L + mul(thr, Le) * (lt.area / (t * t));
+        }
+        if (a.efficient && !spec && a.nlight > (li >= 0 ? 1 : 0)) {
+          want_nee = true;
+          ne_p = make_float4(P.x, P.y, P.z, __int_as_float((int)p));
+          ne_n = make_float4(ns.x, ns.y, ns.z, __int_as_float(mi));
+          ne_w = make_float4(d.x, d.y, d.z, __int_as_float(li));
+          ne_t = make_float4(thr.x, thr.y, thr.z, __int_as_float(depth));
+          ne_g = make_float4(ng.x, ng.y, ng.z, 0.0f);
+        }
+        F4u u = uniforms(a.rng, pid, (uint32_t)depth, 0);
+        V3 wo, fs;
+        int ev = bsdf_sample(m, ns, d, flags & kFlagIorMask, u.a, u.b, u.c, wo, fs);
+        if (ev > 0) {
+          float pc = depth < a.rr_start ? (nonzero(fs) ? 1.0f : 0.0f) : fminf(0.95f, maxc(fs));
+          bool capped = (a.max_depth > 0 && depth + 1 >= a.max_depth);
+          if (!capped && u.d < pc) {
+            if (depth + 1 >= kHardCap) {
+              flags |= kFlagTruncated;
+              atomicAdd(&a.counters[kCtrTrunc], 1u);
+            } else {
+              want_next = true;
+              if (depth == 0) flags |= kFlagContinued0;
+              V3 nthr = mul(thr, fs) * (1.0f / pc);
+              bool nec = spec && dot(ns, wo) > kEps;
+              V3 org = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
+              no_o = make_float4(org.x, org.y, org.z, o4.w);
+              no_d = make_float4(wo.x, wo.y, wo.z, 0.0f);
+              no_t = make_float4(nthr.x, nthr.y, nthr.z, __uint_as_float((uint32_t)(depth + 1) | (nec ? 0x10000u : 0u)));
+            }
+          }
+        }
+        a.path_L[p] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
+      }
+    }
+    uint32_t q = warp_append(&a.counters[kCtrRay + b + 1], want_next);
+    if (want_next) {
+      a.qo[nxt][q] = no_o;
+      a.qd[nxt][q] = no_d;
+      a.qt[nxt][q] = no_t;
+    }
+    uint32_t e = warp_append(&a.counters[kCtrNee + b], want_nee);
+    if (want_nee) {
+      a.np_[e] = ne_p;
+      a.nn_[e] = ne_n;
+      a.nw_[e] = ne_w;
+      a.nt_[e] = ne_t;
+      a.ng_[e] = ne_g;
+    }
+  }
+}
+
+// shadow: DirectIllumination::evaluate for one hit (all lights x noDirectSamples)
+__global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
+  load_top(a);
+  const Pair *top = top_ptr(a);
+  const uint32_t n = a.counters[kCtrNee + b];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 p4 = a.np_[i], n4 = a.nn_[i], w4 = a.nw_[i], t4 = a.nt_[i], g4 = a.ng_[i];
+    int64_t p = (int64_t)__float_as_int(p4.w);
+    int x, y, s;
+    uint64_t pid = path_id(a, p, x, y, s);
+    V3 P = v3(p4.x, p4.y, p4.z), ns = v3(n4.x, n4.y, n4.z), wi = v3(w4.x, w4.y, w4.z), ng = v3(g4.x, g4.y, g4.z);
+    int self = __float_as_int(w4.w);
+    int depth = __float_as_int(t4.w);
+    Material m = load_mat(a, __float_as_int(n4.w));
+    V3 sum = v3(0.0f, 0.0f, 0.0f);
+    uint32_t traced = 0;
+    const int side = a.nds_side;
+    for (int li = a.nlight - 1; li >= 0; --li) {
+      if (li == self) continue;
+      Light lt = load_light(a, li);
+      V3 dsum = v3(0.0f, 0.0f, 0.0f);
+      for (int sy = 0; sy < side; ++sy)
+        for (int sx = 0; sx < side; ++sx) {
+          int mi = (li * side + sy) * side + sx;
+          F4u u = uniforms(a.rng, pid, (uint32_t)depth, 1u + (uint32_t)(mi >> 1));
+          float ux = ((float)sx + ((mi & 1) ? u.c : u.a)) / (float)side;
+          float uy = ((float)sy + ((mi & 1) ? u.d : u.b)) / (float)side;
+          V3 lp = lt.center + lt.ex * (ux - 0.5f) + lt.ez * (uy - 0.5f);
+          V3 wo = lp - P;
+          float t = length(wo);
+          wo = wo * (1.0f / t);
+          float cwo = fabsf(dot(ns, wo)), cwi = fabsf(dot(lt.normal, wo));
+          V3 fr = bsdf_eval(m, ns, wi, wo);
+          if (cwo > 0.0f && cwi > 0.0f && nonzero(fr)) {
+            V3 Le = emitted(lt.Le, lt.normal, -wo);
+            if (nonzero(Le)) {
+              Ray r;
+              r.o = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
+              r.d = wo;
+              r.tmin = 0.0f;
+              r.tmax = t * (1.0f - kShadowMargin);
+              Hit h;
+              ++traced;
+              if (!traverse<true, false>(a.view, r, h, top, a.ntop, nullptr))
+                dsum = dsum + mul(fr, Le) * (cwo * cwi / (t * t));
+            }
+          }
+        }
+      sum = sum + dsum * (lt.area / (float)a.nds);
+    }
+    if (traced) atomicAdd(&a.counters[kCtrShadowRays], traced);
+    if (nonzero(sum)) {
+      float4 L4 = a.path_L[p];
+      V3 thr = v3(t4.x, t4.y, t4.z);
+      a.path_L[p] = make_float4(L4.x + thr.x * sum.x, L4.y + thr.y * sum.y, L4.z + thr.z * sum.z, L4.w);
+    }
+  }
+}
+
+// accumulate: per pixel, Kahan-add the wave's samples into the compensated FP32 film
+// (ProgressiveFilterValue::addSample, ProgressiveFilterValue.h:33-36, box weight 1)
+__global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned long long ext = 0, bounces = 0;
+    for (int b = 0; b < a.max_b; ++b) {
+      uint32_t c = a.counters[kCtrRay + b];
+      ext += c;
+      bounces += c ? 1ull : 0ull;
+    }
+    a.stats[0] += ext;
+    a.stats[1] += a.counters[kCtrShadowRays];
+    a.stats[2] += a.counters[kCtrTrunc];
+    a.stats[3] += bounces;
+  }
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.nslots; q += stride) {
+    int x, y;
+    if (!slot_pixel(a, a.slot0 + q, x, y)) continue;
+    int64_t pix = (int64_t)y * a.W + x;
+    float4 S = a.film_sum[pix], C = a.film_c[pix];
+    for (int si = 0; si < a.ns; ++si) {
+      float4 L4 = a.path_L[q * a.ns + si];
+      V3 L = apply_mask(v3(L4.x, L4.y, L4.z), __float_as_uint(L4.w));
+      if (a.path_out) {
+        int s = a.s0 + si - a.sample_begin;
+        a.path_out[pix * a.sample_count + s] = make_float4(L.x, L.y, L.z, L4.w);
+      }
+      float yx = L.x - C.x, tx = S.x + yx; C.x = (tx - S.x) - yx; S.x = tx;
+      float yy = L.y - C.y, ty = S.y + yy; C.y = (ty - S.y) - yy; S.y = ty;
+      float yz = L.z - C.z, tz = S.z + yz; C.z = (tz - S.z) - yz; S.z = tz;
+    }
+    S.w += (float)a.ns;
+    a.film_sum[pix] = S;
+    a.film_c[pix] = C;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// host driver
+
+struct Workspace {
+  int device = -1;
+  int64_t cap = 0;  // paths
+  void *block = nullptr;
+  float4 *path_L = nullptr, *qo[2] = {}, *qd[2] = {}, *qt[2] = {}, *qhit = nullptr;
+  float4 *np_ = nullptr, *nn_ = nullptr, *nw_ = nullptr, *nt_ = nullptr, *ng_ = nullptr;
+  uint32_t *counters = nullptr;
+  unsigned long long *stats = nullptr;
+  uint32_t *h_counters = nullptr;  // pinned
+  ~Workspace() {
+    if (block) cudaFree(block);
+    if (h_counters) cudaFreeHost(h_counters);
+  }
+};
+
+static thread_local Workspace *t_ws = nullptr;
+static thread_local mgpu_render_stats t_stats{};
+static thread_local cudaStream_t t_stats_stream = nullptr;
+static thread_local bool t_stats_pending = false;
+
+static int ensure_workspace(int64_t paths) {
+  int dev = 0;
+  MGPU_CUDA(cudaGetDevice(&dev));
+  if (t_ws && t_ws->device == dev && t_ws->cap >= paths) return MGPU_OK;
+  if (t_ws) {
+    cudaDeviceSynchronize();
+    delete t_ws;
+    t_ws = nullptr;
+  }
+  Workspace *w = new Workspace();
+  w->device = dev;
+  w->cap = paths;
+  size_t per = (size_t)paths * sizeof(float4);
+  size_t total = per * 13 + kNumCounters * sizeof(uint32_t) + 4 * sizeof(unsigned long long) + 256;
+  cudaError_t e = cudaMalloc(&w->block, total);
+  if (e != cudaSuccess) {
+    delete w;
+    return cuda_fail(e, "render workspace cudaMalloc");
+  }
+  float4 *f = (float4 *)w->block;
+  w->path_L = f; f += paths;
+  for (int k = 0; k < 2; ++k) { w->qo[k] = f; f += paths; w->qd[k] = f; f += paths; w->qt[k] = f; f += paths; }
+  w->qhit = f; f += paths;
+  w->np_ = f; f += paths; w->nn_ = f; f += paths; w->nw_ = f; f += paths; w->nt_ = f; f += paths; w->ng_ = f; f += paths;
+  w->stats = (unsigned long long *)f;
+  w->counters = (uint32_t *)(w->stats + 4);
+  e = cudaMallocHost(&w->h_counters, 64);
+  if (e != cudaSuccess) {
+    delete w;
+    return cuda_fail(e, "render workspace cudaMallocHost");
+  }
+  t_ws = w;
+  return MGPU_OK;
+}
+
+static int grid_for(const void *kern, size_t smem) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem);
+  if (per_sm < 1) per_sm = 1;
+  return device_sm_count() * per_sm;
+}
+
+static Camera make_camera(const float *c) {
+  // ThinLensCamera::setOrientation (ThinLensCamera.cpp:241-259) and _computeMatrix (:204-210)
+  double eye[3] = {c[0], c[1], c[2]}, look[3] = {c[3], c[4], c[5]}, up[3] = {c[6], c[7], c[8]};
+  double n[3] = {-look[0], -look[1], -look[2]};
+  double u[3] = {up[1] * n[2] - up[2] * n[1], up[2] * n[0] - up[0] * n[2], up[0] * n[1] - up[1] * n[0]};
+  double ln = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), lu = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  for (int k = 0; k < 3; ++k) { n[k] /= ln; u[k] /= lu; }
+  double v[3] = {n[1] * u[2] - n[2] * u[1], n[2] * u[0] - n[0] * u[2], n[0] * u[1] - n[1] * u[0]};
+  double va = c[9] * (3.14159265358979323846 / 180.0);
+  double th = tan(va / 2), tw = c[10] * th;
+  Camera k;
+  k.eye = v3((float)eye[0], (float)eye[1], (float)eye[2]);
+  k.u = v3((float)u[0], (float)u[1], (float)u[2]);
+  k.v = v3((float)v[0], (float)v[1], (float)v[2]);
+  k.n = v3((float)n[0], (float)n[1], (float)n[2]);
+  k.tan_w = (float)tw;
+  k.tan_h = (float)th;
+  return k;
+}
+
+static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_film *film, float *d_path_out,
+                       void *stream) {
+  if (!sc || !rp || !film) return fail(MGPU_E_INVALID, "mgpu_render: null argument");
+  if (rp->width != film->width || rp->height != film->height)
+    return fail(MGPU_E_INVALID, "mgpu_render: film size differs from the render size");
+  if (rp->width <= 0 || rp->height <= 0 || rp->spp <= 0 || rp->sample_count < 0 || rp->sample_begin < 0 ||
+      rp->no_direct_samples <= 0 || rp->max_depth < 0 || rp->rr_start_depth < 0)
+    return fail(MGPU_E_INVALID, "mgpu_render: bad parameters");
+  if (rp->sample_count == 0) return MGPU_OK;
+  if ((int64_t)rp->sample_begin + rp->sample_count > (int64_t)1 << 30)
+    return fail(MGPU_E_INVALID, "mgpu_render: sample range too large");
+  cudaStream_t st = as_stream(stream);
+  RenderArgs a;
+  memset(&a, 0, sizeof(a));
+  a.view = sc->view;
+  a.ntop = sc->top_pairs;
+  a.shade = sc->d_shade;
+  a.mats = (const float4 *)sc->d_mats;
+  a.lights = (const float4 *)sc->d_lights;
+  a.nlight = sc->nlight;
+  a.cam = make_camera(rp->camera);
+  a.rng.k0 = (uint32_t)rp->seed;
+  a.rng.k1 = (uint32_t)(rp->seed >> 32);
+  a.rng.stream = rp->stream_id;
+  a.W = rp->width;
+  a.H = rp->height;
+  a.spp = rp->spp;
+  a.side = std::max(1, (int)sqrt((double)rp->spp));
+  a.s2 = a.side * a.side;
+  a.nds = rp->no_direct_samples;
+  a.nds_side = std::max(1, (int)sqrt((double)rp->no_direct_samples));
+  a.max_depth = rp->max_depth;
+  a.rr_start = rp->rr_start_depth;
+  a.efficient = rp->efficient_direct;
+  a.tiles_x = (a.W + 7) / 8;
+  a.sample_begin = rp->sample_begin;
+  a.sample_count = rp->sample_count;
+  a.film_sum = film->d_sum;
+  a.film_c = film->d_c;
+  a.path_out = (float4 *)d_path_out;
+  const int64_t tiles_y = (a.H + 7) / 8;
+  const int64_t total_slots = (int64_t)a.tiles_x * tiles_y * 64;
+  int64_t wave = rp->wave_paths > 0 ? rp->wave_paths : (int64_t)1 << 22;
+  // samples per wave: as many passes of the whole image as fit, else one pass over a slot range
+  int ns = (int)std::max<int64_t>(1, std::min<int64_t>(rp->sample_count, wave / total_slots));
+  int64_t slots_per_wave = std::min<int64_t>(total_slots, std::max<int64_t>(64, wave / ns) / 64 * 64);
+  int64_t cap = slots_per_wave * ns;
+  int rc = ensure_workspace(cap);
+  if (rc != MGPU_OK) return rc;
+  Workspace *w = t_ws;
+  a.path_L = w->path_L;
+  for (int k = 0; k < 2; ++k) { a.qo[k] = w->qo[k]; a.qd[k] = w->qd[k]; a.qt[k] = w->qt[k]; }
+  a.qhit = w->qhit;
+  a.np_ = w->np_; a.nn_ = w->nn_; a.nw_ = w->nw_; a.nt_ = w->nt_; a.ng_ = w->ng_;
+  a.counters = w->counters;
+  a.stats = w->stats;
+
+  size_t smem = (size_t)a.ntop * sizeof(uint4);
+  if (smem > 48 * 1024) {
+    MGPU_CUDA(cudaFuncSetAttribute(k_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MGPU_CUDA(cudaFuncSetAttribute(k_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  const int g_gen = grid_for((const void *)k_generate, 0);
+  const int g_ext = grid_for((const void *)k_extend, smem);
+  const int g_sha = grid_for((const void *)k_shade, 0);
+  const int g_shw = grid_for((const void *)k_shadow, smem);
+  const int g_acc = grid_for((const void *)k_accumulate, 0);
+
+  mgpu_render_stats stats{};
+  uint64_t launches = 0;
+  const int max_b = rp->max_depth > 0 ? std::min(rp->max_depth, kHardCap) : kHardCap;
+  a.max_b = max_b;
+  MGPU_CUDA(cudaMemsetAsync(w->stats, 0, 4 * sizeof(unsigned long long), st));
+  for (int s0 = rp->sample_begin; s0 < rp->sample_begin + rp->sample_count; s0 += ns) {
+    a.s0 = s0;
+    a.ns = std::min(ns, rp->sample_begin + rp->sample_count - s0);
+    for (int64_t slot0 = 0; slot0 < total_slots; slot0 += slots_per_wave) {
+      a.slot0 = slot0;
+      a.nslots = std::min(slots_per_wave, total_slots - slot0);
+      MGPU_CUDA(cudaMemsetAsync(w->counters, 0, kNumCounters * sizeof(uint32_t), st));
+      k_generate<<<g_gen, kBlock, 0, st>>>(a);
+      ++launches;
+      int b = 0;
+      while (b < max_b) {
+        // with a fixed depth cap every bounce is launched blind; without one, check the live
+        // count every 4 bounces and stop when the wave has drained
+        int chunk = rp->max_depth > 0 ? max_b : std::min(4, max_b - b);
+        for (int k = 0; k < chunk; ++k, ++b) {
+          k_extend<<<g_ext, kBlock, smem, st>>>(a, b);
+          k_shade<<<g_sha, kBlock, 0, st>>>(a, b);
+          k_shadow<<<g_shw, kBlock, smem, st>>>(a, b);
+          launches += 3;
+        }
+        if (rp->max_depth > 0) break;
+        MGPU_CUDA(cudaMemcpyAsync(w->h_counters, w->counters + kCtrRay + b, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        MGPU_CUDA(cudaStreamSynchronize(st));
+        if (w->h_counters[0] == 0) break;
+      }
+      k_accumulate<<<g_acc, kBlock, 0, st>>>(a);
+      ++launches;
+      MGPU_CUDA(cudaGetLastError());
+    }
+  }
+  g_launches.fetch_add(launches);
+  stats.paths = (uint64_t)a.W * a.H * (uint64_t)rp->sample_count;
+  stats.kernel_launches = launches;
+  t_stats = stats;
+  t_stats_stream = st;
+  t_stats_pending = true;
+  return MGPU_OK;
+}
+
+}  // namespace mgpu
+
+using namespace mgpu;
+
+extern "C" {
+
+int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream) {
+  return render_impl(scene, params, film, nullptr, stream);
+}
+
+int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,
+                      void *stream) {
+  if (!d_path_L) return fail(MGPU_E_INVALID, "mgpu_render_paths: null path buffer");
+  return render_impl(scene, params, film, d_path_L, stream);
+}
+
+int mgpu_render_stats_get(mgpu_render_stats *out) {
+  if (!out) return fail(MGPU_E_INVALID, "mgpu_render_stats_get: null argument");
+  if (t_stats_pending && t_ws) {
+    unsigned long long h[4];
+    MGPU_CUDA(cudaStreamSynchronize(t_stats_stream));
+    MGPU_CUDA(cudaMemcpy(h, t_ws->stats, sizeof(h), cudaMemcpyDeviceToHost));
+    t_stats.extension_rays = h[0];
+    t_stats.shadow_rays = h[1];
+    t_stats.truncated_paths = h[2];
+    t_stats.bounces = h[3];
+    t_stats_pending = false;
+  }
+  *out = t_stats;
+  return MGPU_OK;
+}
+
+}  // extern "C"

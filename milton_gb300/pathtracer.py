@@ -1,0 +1,304 @@
+"""Python host mirroring Milton's PathTracer / PointSampleRenderer interface over libmgpu.
+
+Milton drives a renderer through a PropertyMap of string keys (mlt/src/milton/utils/PropertyMap.h),
+``init()`` (Renderer.cpp:28-53) and a synchronous ``render()``; output is a per-pixel mean of
+radiance samples (RenderOutput.cpp:72-101).  ``PathTracer`` here takes the same keys
+(noSuperSamples, noDirectSamples, efficientDirect, kdMinPrimitives, kdMaxDepth,
+kdCostTraversal, kdEmptyBias) plus maxDepth / rrStartDepth (defaults: no cap and 2, Milton's
+behaviour, PathTracer.cpp:88-92), seed and wavePaths.
+
+All rendering runs in libmgpu.so on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from .scene import Scene
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.current_stream().cuda_stream
+        except Exception:  # torch absent: legacy default stream
+            return None
+        return None
+    if isinstance(stream, int):
+        return stream
+    return getattr(stream, "cuda_stream", None)
+
+
+def _desc(scene: Scene) -> N.SceneDesc:
+    d = N.SceneDesc()
+    d.ntri = scene.ntri
+    d.tri_v = N.ptr(scene.tri_v)
+    d.tri_n = N.ptr(scene.tri_n)
+    d.tri_mat = N.ptr(scene.tri_mat)
+    d.tri_light = N.ptr(scene.tri_light)
+    d.tri_flags = N.ptr(scene.tri_flags)
+    d.nmat = len(scene.materials)
+    d.materials = N.ptr(scene.materials)
+    d.nlight = len(scene.lights)
+    lights = scene.lights if len(scene.lights) else np.zeros((1, 16), np.float32)
+    d.lights = N.ptr(lights)
+    d._keep = (scene, lights)  # keep buffers alive while the struct is used
+    return d
+
+
+@dataclass
+class KdSettings:
+    """kdTreeAccel build parameters (kdTreeAccel.h:97-104 defaults)."""
+    min_prims: int = 3
+    max_depth: int = 24
+    cost_traversal: float = 1.0
+    empty_bias: float = 0.9
+    threads: int = 0
+
+    def to_c(self) -> N.KdParams:
+        return N.KdParams(self.min_prims, self.max_depth, self.cost_traversal, self.empty_bias, self.threads)
+
+
+class Accel:
+    """Host SAH kd-tree over a scene's triangle soup (mgpu_accel_*)."""
+
+    def __init__(self, scene: Scene, kd: KdSettings | None = None):
+        self._lib = N.load()
+        self.handle = C.c_void_p()
+        d = _desc(scene)
+        N.check(self._lib.mgpu_accel_build(C.byref(d), C.byref((kd or KdSettings()).to_c()), C.byref(self.handle)))
+        self.ntri = scene.ntri
+
+    def stats(self) -> dict:
+        s = N.KdStats()
+        N.check(self._lib.mgpu_accel_stats(self.handle, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in N.KdStats._fields_}
+
+    def serialize(self):
+        nn, npr = C.c_int64(), C.c_int64()
+        N.check(self._lib.mgpu_accel_serialize(self.handle, None, None, None, None, C.byref(nn), C.byref(npr)))
+        kind = np.zeros(nn.value, np.int32)
+        split = np.zeros(nn.value, np.float32)
+        count = np.zeros(nn.value, np.int32)
+        prims = np.zeros(max(npr.value, 1), np.int32)
+        N.check(self._lib.mgpu_accel_serialize(self.handle, N.ptr(kind), N.ptr(split), N.ptr(count), N.ptr(prims),
+                                               C.byref(nn), C.byref(npr)))
+        return kind, split, count, prims[:npr.value]
+
+    def close(self):
+        if self.handle:
+            self._lib.mgpu_accel_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceScene:
+    """Scene resident on the current CUDA device (mgpu_scene_create)."""
+
+    def __init__(self, scene: Scene, accel: Accel, stream=None):
+        self._lib = N.load()
+        self.handle = C.c_void_p()
+        d = _desc(scene)
+        N.check(self._lib.mgpu_scene_create(C.byref(d), accel.handle, _stream_handle(stream), C.byref(self.handle)))
+        self.scene = scene
+
+    @property
+    def nbytes(self) -> int:
+        v = C.c_uint64()
+        N.check(self._lib.mgpu_scene_bytes(self.handle, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.handle:
+            self._lib.mgpu_scene_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Film:
+    """Compensated FP32 film (per pixel: rgb sum + count, rgb Kahan compensation)."""
+
+    def __init__(self, width: int, height: int, stream=None):
+        self._lib = N.load()
+        self.width, self.height = width, height
+        self.handle = C.c_void_p()
+        N.check(self._lib.mgpu_film_create(width, height, _stream_handle(stream), C.byref(self.handle)))
+
+    def clear(self, stream=None):
+        N.check(self._lib.mgpu_film_clear(self.handle, _stream_handle(stream)))
+
+    def mean(self, stream=None) -> np.ndarray:
+        out = np.zeros((self.height, self.width, 3), np.float64)
+        N.check(self._lib.mgpu_film_read(self.handle, N.ptr(out), _stream_handle(stream)))
+        return out
+
+    def raw(self, stream=None) -> np.ndarray:
+        out = np.zeros((2, self.height, self.width, 4), np.float32)
+        N.check(self._lib.mgpu_film_read_raw(self.handle, N.ptr(out), _stream_handle(stream)))
+        return out
+
+    def close(self):
+        if self.handle:
+            self._lib.mgpu_film_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class RenderSettings:
+    width: int
+    height: int
+    spp: int
+    sample_begin: int = 0
+    sample_count: int | None = None
+    no_direct_samples: int = 1
+    max_depth: int = 0
+    rr_start_depth: int = 2
+    efficient_direct: int = 1
+    wave_paths: int = 0
+    seed: int = 0
+    stream_id: int = 0
+
+    def to_c(self, camera: np.ndarray) -> N.RenderParams:
+        p = N.RenderParams()
+        p.width, p.height, p.spp = self.width, self.height, self.spp
+        p.sample_begin = self.sample_begin
+        p.sample_count = self.spp - self.sample_begin if self.sample_count is None else self.sample_count
+        p.no_direct_samples = self.no_direct_samples
+        p.max_depth, p.rr_start_depth = self.max_depth, self.rr_start_depth
+        p.efficient_direct, p.wave_paths = self.efficient_direct, self.wave_paths
+        p.seed, p.stream_id = self.seed, self.stream_id
+        for i in range(11):
+            p.camera[i] = float(camera[i])
+        return p
+
+
+def render(dscene: DeviceScene, settings: RenderSettings, film: Film, camera: np.ndarray | None = None,
+           stream=None, path_out=None) -> None:
+    """mgpu_render: add sample passes to the film (stream-ordered)."""
+    lib = N.load()
+    p = settings.to_c(dscene.scene.camera if camera is None else camera)
+    if path_out is None:
+        N.check(lib.mgpu_render(dscene.handle, C.byref(p), film.handle, _stream_handle(stream)))
+    else:
+        N.check(lib.mgpu_render_paths(dscene.handle, C.byref(p), film.handle, path_out.data_ptr(),
+                                      _stream_handle(stream)))
+
+
+def render_stats() -> dict:
+    s = N.RenderStats()
+    N.check(N.load().mgpu_render_stats_get(C.byref(s)))
+    return {f: getattr(s, f) for f, _ in N.RenderStats._fields_}
+
+
+def launch_count() -> int:
+    return int(N.load().mgpu_launch_count())
+
+
+def trace_closest(dscene: DeviceScene, rays, stream=None, counts=None):
+    """rays: CUDA float32 tensor (n, 8) -> hits (n, 4): t, prim (int bits), b1, b2."""
+    import torch
+    n = rays.shape[0]
+    hits = torch.empty((n, 4), dtype=torch.float32, device=rays.device)
+    lib = N.load()
+    if counts is None:
+        N.check(lib.mgpu_trace_closest(dscene.handle, rays.data_ptr(), hits.data_ptr(), n, _stream_handle(stream)))
+    else:
+        N.check(lib.mgpu_trace_closest_counted(dscene.handle, rays.data_ptr(), hits.data_ptr(), counts.data_ptr(), n,
+                                               _stream_handle(stream)))
+    return hits
+
+
+def trace_any(dscene: DeviceScene, rays, stream=None):
+    import torch
+    n = rays.shape[0]
+    occ = torch.empty((n,), dtype=torch.uint8, device=rays.device)
+    N.check(N.load().mgpu_trace_any(dscene.handle, rays.data_ptr(), occ.data_ptr(), n, _stream_handle(stream)))
+    return occ
+
+
+@dataclass
+class PathTracer:
+    """Milton ``PathTracer`` with its PropertyMap keys; ``init`` builds the kd-tree and makes
+    the scene resident, ``render`` runs every super-sample pass on the GPU."""
+    props: dict = field(default_factory=dict)
+    scene: Scene | None = None
+    width: int = 0
+    height: int = 0
+
+    def __post_init__(self):
+        self._accel = None
+        self._dscene = None
+        self._film = None
+
+    # PropertyMap::getValue(key, default)
+    def get(self, key, default):
+        return self.props.get(key, default)
+
+    def set_scene(self, scene: Scene):
+        self.scene = scene
+
+    def set_output(self, width: int, height: int):
+        self.width, self.height = width, height
+
+    def kd_settings(self) -> KdSettings:
+        return KdSettings(int(self.get("kdMinPrimitives", 3)), int(self.get("kdMaxDepth", 24)),
+                          float(self.get("kdCostTraversal", 1.0)), float(self.get("kdEmptyBias", 0.9)),
+                          int(self.get("kdNoThreads", 0)))
+
+    def settings(self) -> RenderSettings:
+        return RenderSettings(
+            width=self.width, height=self.height, spp=int(self.get("noSuperSamples", 4)),
+            no_direct_samples=int(self.get("noDirectSamples", 1)), max_depth=int(self.get("maxDepth", 0)),
+            rr_start_depth=int(self.get("rrStartDepth", 2)), efficient_direct=int(bool(self.get("efficientDirect", True))),
+            wave_paths=int(self.get("wavePaths", 0)), seed=int(self.get("seed", 0)))
+
+    def init(self):
+        if self.scene is None:
+            raise ValueError("PathTracer.init: no scene set")
+        if self.width <= 0 or self.height <= 0:
+            raise ValueError("PathTracer.init: no output set")
+        self._accel = Accel(self.scene, self.kd_settings())
+        self._dscene = DeviceScene(self.scene, self._accel)
+        self._film = Film(self.width, self.height)
+
+    def render(self, stream=None):
+        if self._dscene is None:
+            raise RuntimeError("PathTracer.render: init() has not been called")
+        self._film.clear(stream)
+        render(self._dscene, self.settings(), self._film, stream=stream)
+
+    def output(self) -> np.ndarray:
+        return self._film.mean()
+
+    @property
+    def accel(self) -> Accel:
+        return self._accel
+
+    @property
+    def device_scene(self) -> DeviceScene:
+        return self._dscene
+
+    @property
+    def film(self) -> Film:
+        return self._film

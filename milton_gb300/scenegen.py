@@ -1,0 +1,225 @@
+"""Seeded synthetic scenes for the benchmark configurations (no external assets).
+
+* ``plain``  closed box of 5 axis-aligned quads (10 triangles, open toward the camera), two boxes
+             rotated about y at seeded angles (24 triangles), one 0.25-area quad light of
+             radiance 15, Lambertian albedos U[0.2, 0.8] per RGB, pinhole camera with a 40 degree
+             vertical field of view; rendered at 256x256, 16 spp, max depth 5, RR from depth 3.
+* ``mid``    400 seeded UV spheres (50 x 26 segments = 2,500 triangles each, smooth normals) with
+             log-uniform radii in [0.05, 1.0], resting without overlap on a 20 x 20 ground quad;
+             materials 60% Lambertian / 30% modified Phong (n ~ U[10, 200], kd + ks <= 1) / 10%
+             dielectric (IOR 1.5); 4 quad lights; 1024x1024, 64 spp, depth 8.
+* ``batch``  many independent scenes of uneven size built from the same recipes.
+
+Every generator is a pure function of its seed (numpy PCG64).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .scene import SceneBuilder, Scene, camera, dielectric, diffuse, phong
+
+
+# ------------------------------------------------------------------------------------------
+# primitives
+
+def quad_tris(p0, p1, p2, p3) -> np.ndarray:
+    """Two triangles of the quad p0 p1 p2 p3 (counter-clockwise seen from the front)."""
+    return np.array([[p0, p1, p2], [p0, p2, p3]], np.float32)
+
+
+def box_tris(center, size, angle_y: float) -> tuple[np.ndarray, np.ndarray]:
+    """12 triangles of a box resting on y = center[1], rotated by angle_y about +y; outward
+    flat normals (each face has its own vertices, as a mesh with per-face normals)."""
+    cx, cy, cz = center
+    sx, sy, sz = (s / 2 for s in size)
+    c, s = np.cos(angle_y), np.sin(angle_y)
+
+    def P(x, y, z):
+        return np.array([cx + c * x + s * z, cy + y, cz - s * x + c * z], np.float64)
+
+    y0, y1 = 0.0, 2 * sy
+    faces = [
+        (P(-sx, y0, sz), P(sx, y0, sz), P(sx, y1, sz), P(-sx, y1, sz)),     # +z
+        (P(sx, y0, -sz), P(-sx, y0, -sz), P(-sx, y1, -sz), P(sx, y1, -sz)),  # -z
+        (P(sx, y0, sz), P(sx, y0, -sz), P(sx, y1, -sz), P(sx, y1, sz)),     # +x
+        (P(-sx, y0, -sz), P(-sx, y0, sz), P(-sx, y1, sz), P(-sx, y1, -sz)),  # -x
+        (P(-sx, y1, sz), P(sx, y1, sz), P(sx, y1, -sz), P(-sx, y1, -sz)),   # +y
+        (P(-sx, y0, -sz), P(sx, y0, -sz), P(sx, y0, sz), P(-sx, y0, sz)),   # -y
+    ]
+    tris = np.concatenate([quad_tris(*f) for f in faces]).astype(np.float32)
+    fn = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0]).astype(np.float64)
+    fn /= np.linalg.norm(fn, axis=1, keepdims=True)
+    return tris, np.repeat(fn[:, None, :], 3, axis=1).astype(np.float32)
+
+
+def uv_sphere(center, radius, nu: int = 50, nv: int = 26) -> tuple[np.ndarray, np.ndarray]:
+    """UV sphere: nu segments, nv rings -> 2 * nu * (nv - 2) + 2 * nu triangles, radial normals
+    (what Mesh::computeNormals' vertex averaging converges to, Mesh.cpp:335-377)."""
+    c = np.asarray(center, np.float64)
+    th = np.linspace(0.0, np.pi, nv + 1)
+    ph = np.linspace(0.0, 2 * np.pi, nu + 1)
+    T, PH = np.meshgrid(th, ph, indexing="ij")
+    dirs = np.stack([np.sin(T) * np.cos(PH), np.cos(T), np.sin(T) * np.sin(PH)], -1)
+    dirs[:, -1] = dirs[:, 0]
+    pts = c + radius * dirs
+    tris, nrms = [], []
+    for i in range(nv):
+        for j in range(nu):
+            a, b = pts[i, j], pts[i, j + 1]
+            cc, d = pts[i + 1, j + 1], pts[i + 1, j]
+            na, nb, nc, nd = dirs[i, j], dirs[i, j + 1], dirs[i + 1, j + 1], dirs[i + 1, j]
+            if i != 0:           # skip the degenerate triangle at the north pole
+                tris.append((a, d, b)); nrms.append((na, nd, nb))
+            if i != nv - 1:      # and at the south pole
+                tris.append((b, d, cc)); nrms.append((nb, nd, nc))
+    return np.asarray(tris, np.float32), np.asarray(nrms, np.float32)
+
+
+def _uv_sphere_fast(center, radius, nu: int = 50, nv: int = 26):
+    """Vectorised uv_sphere (same triangles, same order)."""
+    c = np.asarray(center, np.float64)
+    th = np.linspace(0.0, np.pi, nv + 1)
+    ph = np.linspace(0.0, 2 * np.pi, nu + 1)
+    T, PH = np.meshgrid(th, ph, indexing="ij")
+    dirs = np.stack([np.sin(T) * np.cos(PH), np.cos(T), np.sin(T) * np.sin(PH)], -1)
+    dirs[:, -1] = dirs[:, 0]
+    pts = c + radius * dirs
+    i, j = np.meshgrid(np.arange(nv), np.arange(nu), indexing="ij")
+    a, b, cc, d = (i, j), (i, j + 1), (i + 1, j + 1), (i + 1, j)
+    t1 = np.stack([pts[a], pts[d], pts[b]], -2)
+    n1 = np.stack([dirs[a], dirs[d], dirs[b]], -2)
+    t2 = np.stack([pts[b], pts[d], pts[cc]], -2)
+    n2 = np.stack([dirs[b], dirs[d], dirs[cc]], -2)
+    keep1 = (i != 0)
+    keep2 = (i != nv - 1)
+    # interleave per cell as uv_sphere does: [t1 (if kept), t2 (if kept)]
+    T2 = np.stack([t1, t2], 2)           # (nv, nu, 2, 3, 3)
+    N2 = np.stack([n1, n2], 2)
+    K2 = np.stack([keep1, keep2], 2)     # (nv, nu, 2)
+    return T2[K2].astype(np.float32), N2[K2].astype(np.float32)
+
+
+# ------------------------------------------------------------------------------------------
+# configurations
+
+PLAIN = dict(width=256, height=256, spp=16, max_depth=5, rr_start=3, nds=1)
+MID = dict(width=1024, height=1024, spp=64, max_depth=8, rr_start=3, nds=1)
+
+
+def plain(seed: int = 0) -> Scene:
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    alb = lambda: rng.uniform(0.2, 0.8, 3)  # noqa: E731
+    # closed box x in [-1, 1], y in [0, 2], z in [-1, 1], open toward +z; normals face inward
+    walls = {
+        "floor": ((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)),
+        "ceiling": ((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)),
+        "back": ((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)),
+        "left": ((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)),
+        "right": ((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)),
+    }
+    for name, pts in walls.items():
+        m = b.material(diffuse(alb()))
+        b.add(name, quad_tris(*[np.asarray(p, np.float32) for p in pts]), None, m)
+    for name, center, size in (("tallBox", (-0.35, 0.0, -0.3), (0.6, 1.2, 0.6)),
+                               ("shortBox", (0.4, 0.0, 0.3), (0.6, 0.6, 0.6))):
+        ang = rng.uniform(-np.pi / 4, np.pi / 4)
+        tris, nrm = box_tris(center, size, ang)
+        b.add(name, tris, nrm, b.material(diffuse(alb())))
+    lm = b.material(diffuse(0.0))
+    # 0.5 x 0.5 quad just below the ceiling, emitting downward (normal = ez x ex = -y)
+    b.add_quad_light("light", (0.0, 1.999, 0.0), (0.5, 0.0, 0.0), (0.0, 0.0, -0.5), 15.0, lm)
+    cam = camera(eye=(0.0, 1.0, 3.75), look=(0.0, 0.0, -1.0), up=(0, 1, 0), height_angle=40.0, aspect=1.0)
+    return b.build(cam, name="plain")
+
+
+def _place_spheres(rng, n, rmin, rmax, half_extent, max_tries=200000):
+    radii = np.exp(rng.uniform(np.log(rmin), np.log(rmax), n))
+    radii = np.sort(radii)[::-1]
+    centers = []
+    placed_r = []
+    for r in radii:
+        for _ in range(max_tries):
+            x = rng.uniform(-half_extent + r, half_extent - r)
+            z = rng.uniform(-half_extent + r, half_extent - r)
+            ok = True
+            for (cx, cz), pr in zip(centers, placed_r):
+                if (x - cx) ** 2 + (z - cz) ** 2 < (r + pr + 1e-3) ** 2:
+                    ok = False
+                    break
+            if ok:
+                centers.append((x, z))
+                placed_r.append(r)
+                break
+        else:
+            raise RuntimeError("could not place spheres without overlap")
+    return [(x, r, z) for (x, z), r in zip(centers, placed_r)], placed_r
+
+
+def mid(seed: int = 0, n_spheres: int = 400, nu: int = 50, nv: int = 26, n_lights: int = 4,
+        ground: float = 20.0) -> Scene:
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    h = ground / 2
+    gm = b.material(diffuse(rng.uniform(0.3, 0.7, 3)))
+    b.add("ground", quad_tris(np.array((-h, 0, h), np.float32), np.array((h, 0, h), np.float32),
+                              np.array((h, 0, -h), np.float32), np.array((-h, 0, -h), np.float32)), None, gm)
+    centers, radii = _place_spheres(rng, n_spheres, 0.05, 1.0, h)
+    for k, (c, r) in enumerate(zip(centers, radii)):
+        u = rng.uniform()
+        if u < 0.6:
+            m = diffuse(rng.uniform(0.2, 0.8, 3))
+        elif u < 0.9:
+            kd = rng.uniform(0.05, 0.5, 3)
+            ks = rng.uniform(0.1, 0.45, 3)
+            m = phong(kd, ks, rng.uniform(10.0, 200.0))
+        else:
+            m = dielectric(1.5)
+        tris, nrm = _uv_sphere_fast(c, r, nu, nv)
+        b.add(f"sphere{k}", tris, nrm, b.material(m))
+    lm = b.material(diffuse(0.0))
+    # lights: 2 x 2 quads at height 8 over the four quadrants, facing down, radiance 10
+    for i in range(n_lights):
+        ang = 2 * np.pi * (i + 0.5) / n_lights
+        cx, cz = 5.0 * np.cos(ang), 5.0 * np.sin(ang)
+        b.add_quad_light(f"light{i}", (cx, 8.0, cz), (2.0, 0.0, 0.0), (0.0, 0.0, -2.0), 10.0, lm)
+    cam = camera(eye=(0.0, 7.0, 17.0), focus=(0.0, 0.0, 0.0), up=(0, 1, 0), height_angle=40.0, aspect=1.0)
+    return b.build(cam, name="mid")
+
+
+def random_scene(seed: int, target_tris: int) -> Scene:
+    """Spheres and boxes on a ground quad with one to four quad lights, about target_tris
+    triangles (batched / serving workloads)."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    gm = b.material(diffuse(rng.uniform(0.3, 0.7, 3)))
+    h = 10.0
+    b.add("ground", quad_tris(np.array((-h, 0, h), np.float32), np.array((h, 0, h), np.float32),
+                              np.array((h, 0, -h), np.float32), np.array((-h, 0, -h), np.float32)), None, gm)
+    per_sphere = 2500
+    n_sph = max(1, target_tris // per_sphere)
+    nu = 50 if target_tris >= per_sphere else max(4, int(np.sqrt(target_tris / 2)))
+    nv = 26 if target_tris >= per_sphere else max(3, nu // 2)
+    centers, radii = _place_spheres(rng, min(n_sph, 1500), 0.05, 1.0, h)
+    for k, (c, r) in enumerate(zip(centers, radii)):
+        u = rng.uniform()
+        if u < 0.6:
+            m = diffuse(rng.uniform(0.2, 0.8, 3))
+        elif u < 0.9:
+            m = phong(rng.uniform(0.05, 0.5, 3), rng.uniform(0.1, 0.45, 3), rng.uniform(10.0, 200.0))
+        else:
+            m = dielectric(1.5)
+        tris, nrm = _uv_sphere_fast(c, r, nu, nv)
+        b.add(f"sphere{k}", tris, nrm, b.material(m))
+    for k in range(int(rng.integers(0, 4))):
+        tris, nrm = box_tris((rng.uniform(-8, 8), 0.0, rng.uniform(-8, 8)), rng.uniform(0.3, 1.5, 3),
+                             rng.uniform(-np.pi, np.pi))
+        b.add(f"box{k}", tris, nrm, b.material(diffuse(rng.uniform(0.2, 0.8, 3))))
+    lm = b.material(diffuse(0.0))
+    nl = int(rng.integers(1, 5))
+    for i in range(nl):
+        ang = 2 * np.pi * (i + 0.5) / nl
+        b.add_quad_light(f"light{i}", (5.0 * np.cos(ang), 8.0, 5.0 * np.sin(ang)), (2.0, 0.0, 0.0),
+                         (0.0, 0.0, -2.0), 10.0, lm)
+    cam = camera(eye=(0.0, 6.0, 15.0), focus=(0.0, 0.0, 0.0), height_angle=40.0, aspect=1.0)
+    return b.build(cam, name=f"random{seed}")

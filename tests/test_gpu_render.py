@@ -1,0 +1,117 @@
+"""Wavefront renderer parity against the FP64 PathTracer oracle, called through the C ABI.
+
+* per path: the GPU and the oracle draw the same Philox numbers, so most paths follow the same
+  vertices; a path may diverge where FP32 and FP64 take different discrete decisions (Russian
+  roulette or lobe thresholds, hits within FP32 precision of an edge);
+* per pixel: independent estimates (different seeds) agree in a z-test on per-pixel means;
+* film: deterministic, independent of wave size and of how sample passes are split.
+"""
+import numpy as np
+import pytest
+
+from milton_gb300 import pathtracer as pt
+from milton_gb300 import scenegen
+from gpu_util import gpu_render_paths
+
+pytestmark = pytest.mark.gpu
+
+PATH_RTOL = 2e-3   # per-path radiance tolerance (relative, FP32 vs FP64)
+PATH_ATOL = 1e-4
+
+
+def _path_agreement(a, b):
+    ok = np.all(np.abs(a - b) <= PATH_ATOL + PATH_RTOL * np.maximum(np.abs(a), np.abs(b)), axis=-1)
+    return ok.mean()
+
+
+@pytest.mark.parametrize("mode", ["config", "reference"])
+def test_plain_per_path(cuda, oracle, mode):
+    s = scenegen.plain(0)
+    kw = dict(max_depth=5, rr_start=3) if mode == "config" else dict(max_depth=0, rr_start=2)
+    W = H = 64
+    spp = 16
+    st = pt.RenderSettings(W, H, spp, max_depth=kw["max_depth"], rr_start_depth=kw["rr_start"], seed=3)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st)
+    tree = oracle.Tree(s.tri_v)
+    mean_o, paths_o, ost = oracle.render(s, tree, W, H, spp, seed=3, per_path=True, **kw)
+    agree = _path_agreement(paths_g, paths_o)
+    rmse = np.sqrt(((mean_g - mean_o) ** 2).mean())
+    print(f"plain {mode}: path agreement {agree:.5f}, image rmse {rmse:.3e}, mean {mean_g.mean():.5f}/{mean_o.mean():.5f}")
+    assert agree >= 0.98
+    assert rmse <= 0.02 * mean_o.mean()
+    assert np.allclose(mean_g, paths_g.mean(axis=2), rtol=1e-5, atol=1e-6)
+
+
+def test_materials_per_path(cuda, oracle):
+    # spheres with Lambertian, modified Phong and dielectric BSDFs, several lights
+    s = scenegen.random_scene(11, 30000)
+    W = H = 48
+    st = pt.RenderSettings(W, H, 8, max_depth=8, rr_start_depth=3, seed=5)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st)
+    tree = oracle.Tree(s.tri_v)
+    mean_o, paths_o, _ = oracle.render(s, tree, W, H, 8, max_depth=8, rr_start=3, seed=5, per_path=True)
+    agree = _path_agreement(paths_g, paths_o)
+    print(f"materials: path agreement {agree:.5f}")
+    assert agree >= 0.95
+
+
+def test_plain_independent_estimates_z_test(cuda, oracle):
+    s = scenegen.plain(0)
+    W = H = 32
+    spp = 256
+    st = pt.RenderSettings(W, H, spp, max_depth=5, rr_start_depth=3, seed=101)
+    _, pg, _ = gpu_render_paths(cuda, s, st)
+    tree = oracle.Tree(s.tri_v)
+    _, po, _ = oracle.render(s, tree, W, H, spp, max_depth=5, rr_start=3, seed=202, per_path=True)
+    mg, mo = pg.mean(2), po.mean(2)
+    se = np.sqrt(pg.var(2, ddof=1) / spp + po.var(2, ddof=1) / spp)
+    z = np.where(se > 0, (mg - mo) / np.maximum(se, 1e-12), 0.0)
+    frac = (np.abs(z) > 4).mean()
+    print(f"z-test: |z|>4 fraction {frac:.4f}, mean |z| {np.abs(z).mean():.3f}")
+    assert frac <= 0.01
+    assert abs(np.abs(z).mean() - 0.8) < 0.25  # E|z| = sqrt(2/pi) for a standard normal
+
+
+def test_film_determinism_and_pass_splits(cuda):
+    s = scenegen.plain(0)
+    acc = pt.Accel(s)
+    ds = pt.DeviceScene(s, acc)
+    W = H = 40  # not a multiple of the 8x8 tile
+    base = pt.RenderSettings(W, H, 16, max_depth=5, rr_start_depth=3, seed=9)
+    f1 = pt.Film(W, H)
+    pt.render(ds, base, f1)
+    f2 = pt.Film(W, H)
+    pt.render(ds, base, f2)
+    raw1, raw2 = f1.raw(), f2.raw()
+    assert np.array_equal(raw1, raw2)
+    # the same passes in two calls, and with tiny waves
+    f3 = pt.Film(W, H)
+    pt.render(ds, pt.RenderSettings(W, H, 16, sample_begin=0, sample_count=7, max_depth=5, rr_start_depth=3, seed=9), f3)
+    pt.render(ds, pt.RenderSettings(W, H, 16, sample_begin=7, sample_count=9, max_depth=5, rr_start_depth=3, seed=9), f3)
+    assert np.array_equal(raw1, f3.raw())
+    f4 = pt.Film(W, H)
+    pt.render(ds, pt.RenderSettings(W, H, 16, max_depth=5, rr_start_depth=3, seed=9, wave_paths=4096), f4)
+    assert np.array_equal(raw1, f4.raw())
+    assert np.all(raw1[0, ..., 3] == 16)  # sample count per pixel
+    stats = pt.render_stats()
+    assert stats["paths"] == W * H * 16 and stats["extension_rays"] >= W * H * 16
+
+
+def test_renderer_plugin_object(cuda):
+    from milton_gb300.plugin import load_dynamic_renderer
+    from milton_gb300._native import LIB_PATH
+    s = scenegen.plain(0)
+    r = load_dynamic_renderer(str(LIB_PATH))
+    r.set_scene(s)
+    r.set_output(32, 32)
+    for k, v in dict(noSuperSamples=4, maxDepth=5, rrStartDepth=3, seed=9).items():
+        r[k] = v
+    r.init()
+    r.render()
+    out = r.output()
+    acc = pt.Accel(s)
+    ds = pt.DeviceScene(s, acc)
+    f = pt.Film(32, 32)
+    pt.render(ds, pt.RenderSettings(32, 32, 4, max_depth=5, rr_start_depth=3, seed=9), f)
+    assert np.array_equal(out, f.mean())
+    r.close()

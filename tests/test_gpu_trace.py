@@ -1,0 +1,99 @@
+"""Closest-hit and any-hit parity of the sm_103a kernels against the FP64 oracle, called
+through the C ABI.  Primitive ids must match except at reported ties (the two nearest hits
+within 1e-6 relative t, or a hit on an edge shared by two triangles)."""
+import numpy as np
+import pytest
+
+from milton_gb300 import pathtracer as pt
+from milton_gb300 import scenegen
+from gpu_util import gpu_any, gpu_trace
+from raygen import camera_rays, classify, sphere_rays
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def plain_dev(cuda):
+    s = scenegen.plain(0)
+    flags = s.tri_flags.copy()
+    flags[::3] = 1  # a third of the triangles back-face culled (Milton `Triangle`)
+    s.tri_flags = flags
+    acc = pt.Accel(s)
+    return s, acc, pt.DeviceScene(s, acc)
+
+
+def test_closest_hit_plain_2x2e20(cuda, oracle, plain_dev):
+    s, _, ds = plain_dev
+    rays = np.concatenate([camera_rays(s.camera, 1 << 20, 0), sphere_rays((-1, 0, -1), (1, 2, 1), 1 << 20, 1)])
+    h, _ = gpu_trace(cuda, ds, rays)
+    t, p, t2, _ = oracle.trace_closest(None, s.tri_v, s.tri_flags, rays)
+    r = classify(p, t, t2, h[:, 1].view(np.int32), h[:, 0])
+    print("plain closest:", {k: v for k, v in r.items() if k != "bad_idx"})
+    assert r["mismatches"] == 0
+    assert r["ties"] <= 0.002 * r["n"]
+    hit = p >= 0
+    assert np.all(np.abs(h[hit, 0] - t[hit]) <= 1e-5 * np.maximum(t[hit], 1.0) + 2e-6)
+
+
+def test_any_hit_plain(cuda, oracle, plain_dev):
+    s, _, ds = plain_dev
+    rays = np.concatenate([camera_rays(s.camera, 1 << 18, 2), sphere_rays((-1, 0, -1), (1, 2, 1), 1 << 18, 3)])
+    t, p, _, _ = oracle.trace_closest(None, s.tri_v, s.tri_flags, rays)
+    hit = np.isfinite(t)
+    # FP32 window margin: 1e-4 relative plus 1e-5 absolute (coordinates are O(1) here)
+    margin = 1e-4 * np.where(hit, t, 0.0) + 1e-5
+    short = rays.copy()
+    short[:, 7] = np.where(hit, t - margin, 10.0)
+    long_ = rays.copy()
+    long_[:, 7] = np.where(hit, t + margin, 10.0)
+    occ_s = gpu_any(cuda, ds, short)
+    occ_l = gpu_any(cuda, ds, long_)
+    assert occ_s.sum() == 0
+    assert occ_l[hit].mean() >= 0.9999 and occ_l[~hit].sum() == 0
+    # same answer as the oracle's any-hit where the window is not within 1e-4 of a surface
+    mid = rays.copy()
+    mid[:, 7] = np.where(hit, t * 0.5, 10.0)
+    assert gpu_any(cuda, ds, mid).sum() == oracle.trace_any(None, s.tri_v, s.tri_flags, mid).sum() == 0
+
+
+def test_closest_hit_spheres_against_oracle_kd(cuda, oracle):
+    s = scenegen.random_scene(8, 120000)
+    acc = pt.Accel(s)
+    ds = pt.DeviceScene(s, acc)
+    lo, hi = s.tri_v.reshape(-1, 3).min(0), s.tri_v.reshape(-1, 3).max(0)
+    rays = np.concatenate([camera_rays(s.camera, 1 << 16, 5), sphere_rays(lo, hi, 1 << 16, 6)])
+    h, cnt = gpu_trace(cuda, ds, rays, counts=True)
+    tree = oracle.Tree(s.tri_v)
+    t, p, _, ocnt = oracle.trace_closest(tree, s.tri_v, s.tri_flags, rays, with_counts=True)
+    pg = h[:, 1].view(np.int32)
+    bad = np.nonzero(pg != p)[0]
+    if bad.size:
+        tb, pb, t2b, _ = oracle.trace_closest(None, s.tri_v, s.tri_flags, rays[bad])
+        r = classify(pb, tb, t2b, pg[bad], h[bad, 0])
+        assert r["mismatches"] == 0, r
+    assert bad.size <= 0.002 * len(rays)
+    # counted launch: same hits, and traversal work within a few percent of the oracle's
+    h2, _ = gpu_trace(cuda, ds, rays)
+    assert np.array_equal(h, h2)
+    gn, gt = cnt[:, 0].sum(), cnt[:, 2].sum()
+    assert abs(gn / ocnt[0] - 1) < 0.05 and abs(gt / ocnt[2] - 1) < 0.05, (gn, ocnt[0], gt, ocnt[2])
+
+
+def test_edge_cases(cuda, oracle, plain_dev):
+    s, _, ds = plain_dev
+    r = np.zeros((6, 8), np.float32)
+    r[:, 7] = np.inf
+    r[0, :3] = (5, 5, 5); r[0, 4:7] = (1, 0, 0)             # misses the scene box
+    r[1, :3] = (0.1, 1.0, 0.2); r[1, 4:7] = (0, -1, 0)      # axis-aligned, straight down
+    r[2, :3] = (-1, 1.0, 0.0); r[2, 4:7] = (1, 0, 0)        # origin on the root box boundary
+    r[3, :3] = (0, 1, 0); r[3, 4:7] = (0, 0, -1); r[3, 7] = 0.5  # tmax before any surface
+    r[4, :3] = (0, 1, 0); r[4, 4:7] = (0, 1, 0); r[4, 3] = 2.0   # tmin past every surface
+    r[5, :3] = (0.3, 0.7, 0.1); r[5, 4:7] = (0, 0, 1)
+    h, _ = gpu_trace(cuda, ds, r)
+    pg = h[:, 1].view(np.int32)
+    assert pg[0] == -1 and np.isinf(h[0, 0])
+    assert pg[3] == -1 and pg[4] == -1
+    t, p, _, _ = oracle.trace_closest(None, s.tri_v, s.tri_flags, r[[1, 2, 5]])
+    assert list(pg[[1, 2, 5]]) == list(p)
+    # empty batch is a no-op
+    assert pt.trace_closest(ds, cuda.zeros((0, 8), dtype=cuda.float32, device="cuda")).shape == (0, 4)

@@ -1,0 +1,111 @@
+"""The FP32 arithmetic the kernels run (milton_gb300/csrc/hd_*.h, compiled for the host by the
+test harness in tests/native) against the FP64 oracle -- runs without a GPU."""
+import numpy as np
+import pytest
+
+from milton_gb300 import scenegen
+from milton_gb300.scene import dielectric, diffuse, phong
+from raygen import camera_rays, classify, sphere_rays
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def hc_trace(lib, v, flags, rays, top=1, max_depth=24):
+    n = rays.shape[0]
+    hits = np.zeros((n, 4), np.float32)
+    occ = np.zeros(n, np.uint8)
+    cnt = np.zeros((n, 4), np.uint32)
+    v = np.ascontiguousarray(v, np.float32)
+    fl = None if flags is None else np.ascontiguousarray(flags, np.uint32)
+    rays = np.ascontiguousarray(rays, np.float32)
+    assert lib.hc_trace(_p(v), _p(fl), v.reshape(-1, 9).shape[0], _p(rays), n, _p(hits), _p(occ), _p(cnt),
+                        max_depth, top) == 0
+    return hits, occ, cnt
+
+
+@pytest.mark.parametrize("top", [0, 1])
+def test_fp32_traversal_plain(oracle, hostcheck, top):
+    s = scenegen.plain(0)
+    flags = s.tri_flags.copy()
+    flags[::3] = 1
+    rays = np.concatenate([camera_rays(s.camera, 30000, 0), sphere_rays((-1, 0, -1), (1, 2, 1), 30000, 1)])
+    t, p, t2, _ = oracle.trace_closest(None, s.tri_v, flags, rays)
+    h, occ, cnt = hc_trace(hostcheck, s.tri_v, flags, rays, top=top)
+    r = classify(p, t, t2, h[:, 1].view(np.int32), h[:, 0])
+    assert r["mismatches"] == 0, r
+    assert r["ties"] <= 0.005 * r["n"]
+    # any-hit with tmax just short of the closest hit sees nothing; beyond it sees the hit
+    r2 = rays.copy()
+    hit = np.isfinite(t)
+    r2[:, 7] = np.where(hit, t * (1 - 1e-4), 10.0)
+    _, occ_short, _ = hc_trace(hostcheck, s.tri_v, flags, r2, top=top)
+    assert occ_short.sum() <= 2
+    r2[:, 7] = np.where(hit, t * (1 + 1e-4), 10.0)
+    _, occ_long, _ = hc_trace(hostcheck, s.tri_v, flags, r2, top=top)
+    assert np.array_equal(occ_long.astype(bool)[hit], np.ones(hit.sum(), bool)) or \
+        (occ_long.astype(bool)[hit].mean() > 0.999)
+
+
+def test_fp32_traversal_spheres(oracle, hostcheck):
+    s = scenegen.random_scene(8, 40000)
+    lo, hi = s.tri_v.reshape(-1, 3).min(0), s.tri_v.reshape(-1, 3).max(0)
+    rays = np.concatenate([camera_rays(s.camera, 20000, 5), sphere_rays(lo, hi, 20000, 6)])
+    tree = oracle.Tree(s.tri_v)
+    t, p, _, _ = oracle.trace_closest(tree, s.tri_v, s.tri_flags, rays)
+    h, _, cnt = hc_trace(hostcheck, s.tri_v, s.tri_flags, rays)
+    pg = h[:, 1].view(np.int32)
+    bad = np.nonzero(pg != p)[0]
+    # every disagreement must be a tie in the brute-force oracle
+    if bad.size:
+        tb, pb, t2b, _ = oracle.trace_closest(None, s.tri_v, s.tri_flags, rays[bad])
+        r = classify(pb, tb, t2b, pg[bad], h[bad, 0])
+        assert r["mismatches"] == 0, r
+    assert bad.size <= 0.01 * len(rays)
+    assert cnt[:, 3].max() <= 24
+
+
+def test_uniforms_match_oracle(oracle, hostcheck):
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        seed, stream, path = int(rng.integers(1 << 62)), int(rng.integers(1 << 31)), int(rng.integers(1 << 60))
+        depth, block = int(rng.integers(0, 0x10000)), int(rng.integers(0, 0x10000))
+        u32 = np.zeros(4, np.float32)
+        hostcheck.hc_uniforms(seed, stream, path, depth, block, u32.ctypes.data)
+        assert np.array_equal(u32.astype(np.float64), oracle.uniforms(seed, stream, path, depth, block))
+
+
+@pytest.mark.parametrize("mat", [diffuse([0.6, 0.5, 0.4]), phong([0.3, 0.2, 0.25], [0.5, 0.6, 0.4], 80.0),
+                                 phong([0.05, 0.05, 0.05], [0.9, 0.9, 0.9], 200.0), dielectric(1.5)])
+def test_fp32_bsdf_matches_fp64(oracle, hostcheck, mat):
+    rng = np.random.default_rng(2)
+    agree = 0
+    N = 3000
+    for k in range(N):
+        ns = rng.normal(size=3); ns /= np.linalg.norm(ns)
+        wi = rng.normal(size=3); wi /= np.linalg.norm(wi)
+        if rng.random() < 0.8:
+            wi = wi - 2 * max(0.0, wi @ ns) * ns  # mostly front-side hits
+            wi /= np.linalg.norm(wi)
+        u = rng.random(3)
+        ns32, wi32, u32 = ns.astype(np.float32), wi.astype(np.float32), u.astype(np.float32)
+        ev64, wo64, fs64 = oracle.bsdf_sample(mat, ns32, wi32, k % 3, u32)
+        wo = np.zeros(3, np.float32)
+        fs = np.zeros(3, np.float32)
+        ev32 = hostcheck.hc_bsdf_sample(mat.ctypes.data, ns32.ctypes.data, wi32.ctypes.data, k % 3, u32.ctypes.data,
+                                        wo.ctypes.data, fs.ctypes.data)
+        if ev32 == ev64 and np.allclose(wo, wo64, atol=2e-4) and np.allclose(fs, fs64, rtol=2e-3, atol=1e-4):
+            agree += 1
+    # lobe decisions can flip only on FP32/FP64 rounding near a threshold
+    assert agree >= 0.995 * N, agree
+
+
+def test_offset_moves_off_the_surface(hostcheck):
+    rng = np.random.default_rng(1)
+    for _ in range(1000):
+        p = (rng.normal(size=3) * 10 ** rng.uniform(-3, 3)).astype(np.float32)
+        n = rng.normal(size=3).astype(np.float32); n /= np.linalg.norm(n)
+        out = np.zeros(3, np.float32)
+        hostcheck.hc_offset(p.ctypes.data, n.ctypes.data, out.ctypes.data)
+        assert float((out.astype(np.float64) - p) @ n) > 0
