@@ -159,6 +159,16 @@ int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_
 int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,
                       void *stream);
 int mgpu_render_stats_get(mgpu_render_stats *out); /* stats of the last render on this thread (synchronises) */
+/* Render with traversal counters: counts8 = extension {nodes, leaf refs, triangles, rays},
+ * shadow {nodes, leaf refs, triangles, rays} summed over the render (synchronises).
+ * Measurement helper for the memory roofline; slower than mgpu_render.                   */
+int mgpu_render_counted(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, uint64_t *counts8,
+                        void *stream);
+/* Per-kernel timing: when enabled, every render launch on this thread is bracketed by CUDA
+ * events on its stream.  mgpu_profile_read (synchronises) returns milliseconds and launch
+ * counts per kernel: generate, extend, shade, shadow, accumulate.  Enabling resets. */
+int mgpu_profile_enable(int enable);
+int mgpu_profile_read(double *ms5, uint64_t *launches5);
 
 /* Kernel launches issued by this library since load (for launch accounting). */
 uint64_t mgpu_launch_count(void);

@@ -74,6 +74,9 @@ SIGNATURES = [
     ("mgpu_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_render_paths", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_render_stats_get", C.c_int, [C.POINTER(RenderStats)]),
+    ("mgpu_render_counted", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mgpu_profile_enable", C.c_int, [C.c_int]),
+    ("mgpu_profile_read", C.c_int, [C.c_void_p, C.c_void_p]),
     ("mgpu_launch_count", C.c_uint64, []),
     ("plugin_type", C.c_int, []),
     ("plugin_new", C.c_void_p, []),

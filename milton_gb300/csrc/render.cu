@@ -50,6 +50,7 @@ struct RenderArgs {
   float4 *np_, *nn_, *nw_, *nt_, *ng_;  // shadow task queue
   uint32_t *counters;
   unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] truncated paths, [3] bounces
+  unsigned long long *tcount; // counted mode: ext nodes, refs, tris, rays; shadow nodes, refs, tris, rays
   int32_t max_b;
   float4 *film_sum, *film_c;
   float4 *path_out;      // optional
@@ -153,11 +154,14 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
 }
 
 // extend: closest hit for the live queue of bounce b
+template <bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
   load_top(a);
   const Pair *top = top_ptr(a);
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
+  TraceCounts c = {0, 0, 0, 0};
+  uint32_t rays = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 o = qo[i], d = qd[i];
     Ray r;
@@ -166,8 +170,15 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
     r.d = v3(d.x, d.y, d.z);
     r.tmax = INFINITY;
     Hit h;
-    bool hit = traverse<false, false>(a.view, r, h, top, a.ntop, nullptr);
+    bool hit = traverse<false, COUNT>(a.view, r, h, top, a.ntop, &c);
     a.qhit[i] = make_float4(hit ? h.t : INFINITY, __int_as_float(hit ? h.prim : -1), h.b1, h.b2);
+    ++rays;
+  }
+  if (COUNT && rays) {
+    atomicAdd(&a.tcount[0], (unsigned long long)c.nodes);
+    atomicAdd(&a.tcount[1], (unsigned long long)c.refs);
+    atomicAdd(&a.tcount[2], (unsigned long long)c.tris);
+    atomicAdd(&a.tcount[3], (unsigned long long)rays);
   }
 }
 
@@ -269,8 +280,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
 }
 
 // shadow: DirectIllumination::evaluate for one hit (all lights x noDirectSamples)
+template <bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
   load_top(a);
+  TraceCounts c = {0, 0, 0, 0};
+  uint32_t rays_total = 0;
   const Pair *top = top_ptr(a);
   const uint32_t n = a.counters[kCtrNee + b];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -311,7 +325,7 @@ __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
               r.tmax = t * (1.0f - kShadowMargin);
               Hit h;
               ++traced;
-              if (!traverse<true, false>(a.view, r, h, top, a.ntop, nullptr))
+              if (!traverse<true, COUNT>(a.view, r, h, top, a.ntop, &c))
                 dsum = dsum + mul(fr, Le) * (cwo * cwi / (t * t));
             }
           }
@@ -319,11 +333,18 @@ __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
       sum = sum + dsum * (lt.area / (float)a.nds);
     }
     if (traced) atomicAdd(&a.counters[kCtrShadowRays], traced);
+    rays_total += traced;
     if (nonzero(sum)) {
       float4 L4 = a.path_L[p];
       V3 thr = v3(t4.x, t4.y, t4.z);
       a.path_L[p] = make_float4(L4.x + thr.x * sum.x, L4.y + thr.y * sum.y, L4.z + thr.z * sum.z, L4.w);
     }
+  }
+  if (COUNT && rays_total) {
+    atomicAdd(&a.tcount[4], (unsigned long long)c.nodes);
+    atomicAdd(&a.tcount[5], (unsigned long long)c.refs);
+    atomicAdd(&a.tcount[6], (unsigned long long)c.tris);
+    atomicAdd(&a.tcount[7], (unsigned long long)rays_total);
   }
 }
 
@@ -375,7 +396,8 @@ struct Workspace {
   float4 *path_L = nullptr, *qo[2] = {}, *qd[2] = {}, *qt[2] = {}, *qhit = nullptr;
   float4 *np_ = nullptr, *nn_ = nullptr, *nw_ = nullptr, *nt_ = nullptr, *ng_ = nullptr;
   uint32_t *counters = nullptr;
-  unsigned long long *stats = nullptr;
+  unsigned long long *stats = nullptr;   // 4
+  unsigned long long *tcount = nullptr;  // 8
   uint32_t *h_counters = nullptr;  // pinned
   ~Workspace() {
     if (block) cudaFree(block);
@@ -387,6 +409,53 @@ static thread_local Workspace *t_ws = nullptr;
 static thread_local mgpu_render_stats t_stats{};
 static thread_local cudaStream_t t_stats_stream = nullptr;
 static thread_local bool t_stats_pending = false;
+
+// Per-kernel timing with CUDA events recorded on the launching stream around every launch.
+enum { kProfGenerate = 0, kProfExtend, kProfShade, kProfShadow, kProfAccumulate, kProfClasses };
+struct Profiler {
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  std::vector<std::pair<int, size_t>> marks;  // (class, index of begin event); end = begin + 1
+  cudaStream_t stream = nullptr;
+  double ms[kProfClasses] = {0, 0, 0, 0, 0};
+  uint64_t launches[kProfClasses] = {0, 0, 0, 0, 0};
+  cudaEvent_t next() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  int begin(int cls, cudaStream_t st) {
+    if (!enabled) return -1;
+    stream = st;
+    size_t i = used;
+    cudaEventRecord(next(), st);
+    next();
+    marks.push_back({cls, i});
+    return (int)marks.size() - 1;
+  }
+  void end(int mark, cudaStream_t st) {
+    if (mark < 0) return;
+    cudaEventRecord(pool[marks[(size_t)mark].second + 1], st);
+  }
+  int flush() {
+    if (marks.empty()) return MGPU_OK;
+    MGPU_CUDA(cudaStreamSynchronize(stream));
+    for (auto &m : marks) {
+      float t = 0;
+      MGPU_CUDA(cudaEventElapsedTime(&t, pool[m.second], pool[m.second + 1]));
+      ms[m.first] += t;
+      launches[m.first] += 1;
+    }
+    marks.clear();
+    used = 0;
+    return MGPU_OK;
+  }
+};
+static thread_local Profiler t_prof;
 
 static int ensure_workspace(int64_t paths) {
   int dev = 0;
@@ -401,7 +470,7 @@ static int ensure_workspace(int64_t paths) {
   w->device = dev;
   w->cap = paths;
   size_t per = (size_t)paths * sizeof(float4);
-  size_t total = per * 13 + kNumCounters * sizeof(uint32_t) + 4 * sizeof(unsigned long long) + 256;
+  size_t total = per * 13 + 12 * sizeof(unsigned long long) + kNumCounters * sizeof(uint32_t) + 256;
   cudaError_t e = cudaMalloc(&w->block, total);
   if (e != cudaSuccess) {
     delete w;
@@ -413,7 +482,8 @@ static int ensure_workspace(int64_t paths) {
   w->qhit = f; f += paths;
   w->np_ = f; f += paths; w->nn_ = f; f += paths; w->nw_ = f; f += paths; w->nt_ = f; f += paths; w->ng_ = f; f += paths;
   w->stats = (unsigned long long *)f;
-  w->counters = (uint32_t *)(w->stats + 4);
+  w->tcount = w->stats + 4;
+  w->counters = (uint32_t *)(w->tcount + 8);
   e = cudaMallocHost(&w->h_counters, 64);
   if (e != cudaSuccess) {
     delete w;
@@ -450,6 +520,7 @@ static Camera make_camera(const float *c) {
   return k;
 }
 
+template <bool COUNT>
 static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_film *film, float *d_path_out,
                        void *stream) {
   if (!sc || !rp || !film) return fail(MGPU_E_INVALID, "mgpu_render: null argument");
@@ -506,23 +577,27 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   a.np_ = w->np_; a.nn_ = w->nn_; a.nw_ = w->nw_; a.nt_ = w->nt_; a.ng_ = w->ng_;
   a.counters = w->counters;
   a.stats = w->stats;
+  a.tcount = w->tcount;
 
+  auto kext = k_extend<COUNT>;
+  auto kshw = k_shadow<COUNT>;
   size_t smem = (size_t)a.ntop * sizeof(uint4);
   if (smem > 48 * 1024) {
-    MGPU_CUDA(cudaFuncSetAttribute(k_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MGPU_CUDA(cudaFuncSetAttribute(k_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MGPU_CUDA(cudaFuncSetAttribute(kext, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MGPU_CUDA(cudaFuncSetAttribute(kshw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
   const int g_gen = grid_for((const void *)k_generate, 0);
-  const int g_ext = grid_for((const void *)k_extend, smem);
+  const int g_ext = grid_for((const void *)kext, smem);
   const int g_sha = grid_for((const void *)k_shade, 0);
-  const int g_shw = grid_for((const void *)k_shadow, smem);
+  const int g_shw = grid_for((const void *)kshw, smem);
   const int g_acc = grid_for((const void *)k_accumulate, 0);
 
   mgpu_render_stats stats{};
   uint64_t launches = 0;
   const int max_b = rp->max_depth > 0 ? std::min(rp->max_depth, kHardCap) : kHardCap;
   a.max_b = max_b;
-  MGPU_CUDA(cudaMemsetAsync(w->stats, 0, 4 * sizeof(unsigned long long), st));
+  MGPU_CUDA(cudaMemsetAsync(w->stats, 0, 12 * sizeof(unsigned long long), st));
+  Profiler &pf = t_prof;
   for (int s0 = rp->sample_begin; s0 < rp->sample_begin + rp->sample_count; s0 += ns) {
     a.s0 = s0;
     a.ns = std::min(ns, rp->sample_begin + rp->sample_count - s0);
@@ -530,7 +605,9 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
       a.slot0 = slot0;
       a.nslots = std::min(slots_per_wave, total_slots - slot0);
       MGPU_CUDA(cudaMemsetAsync(w->counters, 0, kNumCounters * sizeof(uint32_t), st));
+      int m = pf.begin(kProfGenerate, st);
       k_generate<<<g_gen, kBlock, 0, st>>>(a);
+      pf.end(m, st);
       ++launches;
       int b = 0;
       while (b < max_b) {
@@ -538,9 +615,15 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
         // count every 4 bounces and stop when the wave has drained
         int chunk = rp->max_depth > 0 ? max_b : std::min(4, max_b - b);
         for (int k = 0; k < chunk; ++k, ++b) {
-          k_extend<<<g_ext, kBlock, smem, st>>>(a, b);
+          m = pf.begin(kProfExtend, st);
+          kext<<<g_ext, kBlock, smem, st>>>(a, b);
+          pf.end(m, st);
+          m = pf.begin(kProfShade, st);
           k_shade<<<g_sha, kBlock, 0, st>>>(a, b);
-          k_shadow<<<g_shw, kBlock, smem, st>>>(a, b);
+          pf.end(m, st);
+          m = pf.begin(kProfShadow, st);
+          kshw<<<g_shw, kBlock, smem, st>>>(a, b);
+          pf.end(m, st);
           launches += 3;
         }
         if (rp->max_depth > 0) break;
@@ -548,7 +631,9 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
         MGPU_CUDA(cudaStreamSynchronize(st));
         if (w->h_counters[0] == 0) break;
       }
+      m = pf.begin(kProfAccumulate, st);
       k_accumulate<<<g_acc, kBlock, 0, st>>>(a);
+      pf.end(m, st);
       ++launches;
       MGPU_CUDA(cudaGetLastError());
     }
@@ -569,13 +654,23 @@ using namespace mgpu;
 extern "C" {
 
 int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream) {
-  return render_impl(scene, params, film, nullptr, stream);
+  return render_impl<false>(scene, params, film, nullptr, stream);
 }
 
 int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,
                       void *stream) {
   if (!d_path_L) return fail(MGPU_E_INVALID, "mgpu_render_paths: null path buffer");
-  return render_impl(scene, params, film, d_path_L, stream);
+  return render_impl<false>(scene, params, film, d_path_L, stream);
+}
+
+int mgpu_render_counted(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film,
+                        uint64_t *counts8, void *stream) {
+  if (!counts8) return fail(MGPU_E_INVALID, "mgpu_render_counted: null output");
+  int rc = render_impl<true>(scene, params, film, nullptr, stream);
+  if (rc != MGPU_OK) return rc;
+  MGPU_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  MGPU_CUDA(cudaMemcpy(counts8, t_ws->tcount, 8 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  return MGPU_OK;
 }
 
 int mgpu_render_stats_get(mgpu_render_stats *out) {
@@ -591,6 +686,24 @@ int mgpu_render_stats_get(mgpu_render_stats *out) {
     t_stats_pending = false;
   }
   *out = t_stats;
+  return MGPU_OK;
+}
+
+int mgpu_profile_enable(int enable) {
+  Profiler &p = t_prof;
+  int rc = p.flush();
+  if (rc != MGPU_OK) return rc;
+  p.enabled = enable != 0;
+  for (int k = 0; k < kProfClasses; ++k) { p.ms[k] = 0; p.launches[k] = 0; }
+  return MGPU_OK;
+}
+
+int mgpu_profile_read(double *ms5, uint64_t *launches5) {
+  if (!ms5 || !launches5) return fail(MGPU_E_INVALID, "mgpu_profile_read: null argument");
+  Profiler &p = t_prof;
+  int rc = p.flush();
+  if (rc != MGPU_OK) return rc;
+  for (int k = 0; k < kProfClasses; ++k) { ms5[k] = p.ms[k]; launches5[k] = p.launches[k]; }
   return MGPU_OK;
 }
 

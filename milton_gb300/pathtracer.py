@@ -205,6 +205,30 @@ def render(dscene: DeviceScene, settings: RenderSettings, film: Film, camera: np
                                       _stream_handle(stream)))
 
 
+def render_counted(dscene: DeviceScene, settings: RenderSettings, film: Film, stream=None) -> dict:
+    """Render with traversal counters (slower; measurement only)."""
+    lib = N.load()
+    p = settings.to_c(dscene.scene.camera)
+    out = np.zeros(8, np.uint64)
+    N.check(lib.mgpu_render_counted(dscene.handle, C.byref(p), film.handle, N.ptr(out), _stream_handle(stream)))
+    keys = ("ext_nodes", "ext_refs", "ext_tris", "ext_rays", "sh_nodes", "sh_refs", "sh_tris", "sh_rays")
+    return {k: int(v) for k, v in zip(keys, out)}
+
+
+KERNELS = ("generate", "extend", "shade", "shadow", "accumulate")
+
+
+def profile_enable(enable: bool = True) -> None:
+    N.check(N.load().mgpu_profile_enable(1 if enable else 0))
+
+
+def profile_read() -> dict:
+    ms = np.zeros(5, np.float64)
+    n = np.zeros(5, np.uint64)
+    N.check(N.load().mgpu_profile_read(N.ptr(ms), N.ptr(n)))
+    return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(KERNELS)}
+
+
 def render_stats() -> dict:
     s = N.RenderStats()
     N.check(N.load().mgpu_render_stats_get(C.byref(s)))
