@@ -130,6 +130,9 @@ int mgpu_accel_destroy(mgpu_accel *accel);
 int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void *stream, mgpu_scene **out);
 int mgpu_scene_destroy(mgpu_scene *scene);
 int mgpu_scene_bytes(const mgpu_scene *scene, uint64_t *out);
+/* Tuning: how many of the breadth-first top 16-byte pairs the traversal kernels stage in
+ * shared memory per block (0 = none; clamped to what the builder laid out breadth-first). */
+int mgpu_scene_set_top_pairs(mgpu_scene *scene, uint32_t n);
 
 /* Ray queries on device buffers (Scene::getIntersection / Scene::intersects).
  *   rays: n * 8 floats  (origin xyz, tmin, direction xyz, tmax)

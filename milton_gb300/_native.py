@@ -62,6 +62,7 @@ SIGNATURES = [
     ("mgpu_scene_create", C.c_int, [C.POINTER(SceneDesc), C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("mgpu_scene_destroy", C.c_int, [C.c_void_p]),
     ("mgpu_scene_bytes", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    ("mgpu_scene_set_top_pairs", C.c_int, [C.c_void_p, C.c_uint32]),
     ("mgpu_trace_closest", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("mgpu_trace_any", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("mgpu_trace_closest_counted", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,

@@ -205,6 +205,7 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   s->nmat = desc->nmat;
   s->nlight = desc->nlight;
   s->top_pairs = tr.top_pairs;
+  s->top_pairs_max = tr.top_pairs;
   s->d_err = (uint32_t *)(base + off_err);
   s->bytes = total;
   *out = s;
@@ -220,6 +221,14 @@ int mgpu_scene_destroy(mgpu_scene *s) {
   if (cur != s->device) cudaSetDevice(cur);
   delete s;
   if (e != cudaSuccess) return cuda_fail(e, "mgpu_scene_destroy: cudaFree");
+  return MGPU_OK;
+}
+
+int mgpu_scene_set_top_pairs(mgpu_scene *s, uint32_t n) {
+  if (!s) return fail(MGPU_E_INVALID, "mgpu_scene_set_top_pairs: null scene");
+  if (n > s->top_pairs_max) n = s->top_pairs_max;
+  if ((size_t)n * 16 > 96 * 1024) return fail(MGPU_E_INVALID, "mgpu_scene_set_top_pairs: more than 96 KiB of shared memory");
+  s->top_pairs = n;
   return MGPU_OK;
 }
 

@@ -48,7 +48,8 @@ struct mgpu_scene {
   float *d_mats = nullptr;
   float *d_lights = nullptr;
   int32_t nmat = 0, nlight = 0;
-  uint32_t top_pairs = 0;
+  uint32_t top_pairs = 0;       // pairs staged in shared memory by the traversal kernels
+  uint32_t top_pairs_max = 0;   // breadth-first pairs available for staging
   void *d_block = nullptr;      // one allocation holding everything above
   uint64_t bytes = 0;
   uint32_t *d_err = nullptr;    // device error word

@@ -245,6 +245,7 @@ constexpr uint32_t kFlagIorMask = 3u;       // ior index 0..2 (PathTracer.cpp:32
 constexpr uint32_t kFlagSpecular = 4u;      // data["specular"] (PathTracer.cpp:45-46)
 constexpr uint32_t kFlagContinued0 = 8u;    // the depth-0 vertex spawned a continuation
 constexpr uint32_t kFlagTruncated = 16u;    // hit the hard depth cap
+constexpr uint32_t kFlagNeePending = 32u;   // light-sample slots hold unfolded direct light
 
 // Milton's single-wavelength masking at depth 0 (PathTracer.cpp:107-114)
 MGPU_HD V3 apply_mask(V3 L, uint32_t flags) {

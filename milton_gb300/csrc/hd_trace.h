@@ -216,14 +216,31 @@ MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *to
       float dt = diff * iv[ax];
       bool rev = diff <= 0.0f ? (dd[ax] <= 0.0f) : (dd[ax] < 0.0f);
       Pair pr = load_pair(s, top, ntop, w0 >> 2);
+      if (dd[ax] == 0.0f) {
+        // ray parallel to the split plane: only the side holding the origin (both if the ray
+        // lies in the plane).  Milton's traversal evaluates 0 * inf here and, for a +0
+        // direction component, descends into the wrong child.
+        if (diff > 0.0f) { w0 = pr.a0; w1 = pr.a1; }
+        else if (diff < 0.0f) { w0 = pr.b0; w1 = pr.b1; }
+        else {
+          if (sp < kMaxStack) {
+            stack[sp].w0 = pr.b0; stack[sp].w1 = pr.b1; stack[sp].tmax = tmax;
+            ++sp;
+            if (COUNT && (uint32_t)sp > cnt->max_stack) cnt->max_stack = (uint32_t)sp;
+          }
+          w0 = pr.a0; w1 = pr.a1;
+        }
+        continue;
+      }
       uint32_t n0 = rev ? pr.b0 : pr.a0, n1 = rev ? pr.b1 : pr.a1;
       uint32_t f0 = rev ? pr.a0 : pr.b0, f1 = rev ? pr.a1 : pr.b1;
       float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
-      if (dt > tmax + slack || dt != dt) {
+      if (dt > tmax + slack) {
         w0 = n0; w1 = n1;               // far child not reached inside this cell
       } else if (dt < tmin - slack) {
         w0 = f0; w1 = f1;               // near child lies behind the cell
       } else {
+        // the ray crosses the plane inside the cell: near child first, far child on the stack
         if (sp < kMaxStack) {
           stack[sp].w0 = f0; stack[sp].w1 = f1; stack[sp].tmax = tmax;
           ++sp;

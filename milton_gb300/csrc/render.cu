@@ -7,10 +7,13 @@
 //                          accumulate;
 //   ray queue     3 x float4 per live path (origin + path index, direction, throughput + depth
 //                          state), compacted every bounce by warp ballot + one atomicAdd per warp.
-// Shadow work is one task per non-specular hit (DirectIllumination::evaluate over all lights,
-// DirectIllumination.cpp:46-138): the shadow kernel samples every light, evaluates the BSDF and
-// traces the any-hit rays itself, so each path's radiance is written by exactly one thread per
-// kernel and the image does not depend on queue order.
+// Direct light (DirectIllumination::evaluate over all lights x noDirectSamples,
+// DirectIllumination.cpp:46-138) is split in two: shade samples every light, evaluates the BSDF,
+// writes each sample's contribution into the path's slot for that sample and queues one shadow
+// ray per non-zero contribution; the shadow kernel is a plain any-hit query that zeroes the slot
+// of an occluded sample.  The next kernel to see the path (shade at the next bounce, or
+// accumulate) folds its slots into the radiance in slot order, so every sum runs in a fixed
+// order and the image does not depend on queue order.
 #include <string.h>
 
 #include <vector>
@@ -22,7 +25,7 @@ namespace mgpu {
 constexpr int kBlock = 128;
 constexpr int kHardCap = 1024;          // vertex cap when max_depth = 0 (Milton has none)
 constexpr int kCtrRay = 0;              // counters[kCtrRay + b]  live paths at bounce b
-constexpr int kCtrNee = kHardCap + 8;   // counters[kCtrNee + b]  shadow tasks at bounce b
+constexpr int kCtrNee = kHardCap + 8;   // counters[kCtrNee + b]  shadow rays at bounce b
 constexpr int kCtrTrunc = 2 * (kHardCap + 8);
 constexpr int kCtrShadowRays = kCtrTrunc + 1;
 constexpr int kNumCounters = kCtrTrunc + 8;
@@ -47,7 +50,9 @@ struct RenderArgs {
   float4 *path_L;
   float4 *qo[2], *qd[2], *qt[2];
   float4 *qhit;
-  float4 *np_, *nn_, *nw_, *nt_, *ng_;  // shadow task queue
+  float4 *so, *sd;       // shadow ray queue: origin + slot index, direction + tmax
+  float4 *slots;         // nl_slots per path: direct-light contribution per light sample
+  int32_t nl_slots;      // nlight * nds_side^2
   uint32_t *counters;
   unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] truncated paths, [3] bounces
   unsigned long long *tcount; // counted mode: ext nodes, refs, tris, rays; shadow nodes, refs, tris, rays
@@ -182,32 +187,52 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
   }
 }
 
-// shade: emission, shadow task, BSDF sample and Russian roulette (PathTracer.cpp:36-115)
+// shade: pending direct light, emission, light sampling, BSDF sample and Russian roulette
+// (PathTracer.cpp:36-115, DirectIllumination.cpp:46-138)
+__device__ __forceinline__ V3 fold_slots(const RenderArgs &a, int64_t p, V3 L) {
+  const float4 *sl = a.slots + p * a.nl_slots;
+  for (int k = 0; k < a.nl_slots; ++k) {
+    float4 c = sl[k];
+    L = L + v3(c.x, c.y, c.z);
+  }
+  return L;
+}
+
 __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const int cur = b & 1, nxt = (b + 1) & 1;
   const uint32_t stride = gridDim.x * blockDim.x;
+  const int s2n = a.nds_side * a.nds_side;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
     uint32_t i = base + threadIdx.x;
     bool valid = i < n;
-    bool want_next = false, want_nee = false;
+    bool want_next = false, do_nee = false;
     float4 no_o, no_d, no_t;
-    float4 ne_p, ne_n, ne_w, ne_t, ne_g;
+    int64_t p = 0;
+    uint64_t pid = 0;
+    int depth = 0, self = -1;
+    V3 P = v3(0, 0, 0), ns = P, ng = P, d = P, thr = P;
+    Material m;
+    m.type = 0;
     if (valid) {
       float4 o4 = a.qo[cur][i], d4 = a.qd[cur][i], t4 = a.qt[cur][i], h4 = a.qhit[i];
-      int64_t p = (int64_t)__float_as_int(o4.w);
+      p = (int64_t)__float_as_int(o4.w);
       uint32_t state = __float_as_uint(t4.w);
-      int depth = (int)(state & 0xFFFFu);
+      depth = (int)(state & 0xFFFFu);
       bool ec = (state >> 16) & 1u;
-      V3 thr = v3(t4.x, t4.y, t4.z);
-      V3 d = v3(d4.x, d4.y, d4.z);
+      thr = v3(t4.x, t4.y, t4.z);
+      d = v3(d4.x, d4.y, d4.z);
       int prim = __float_as_int(h4.y);
       float4 L4 = a.path_L[p];
       uint32_t flags = __float_as_uint(L4.w);
       V3 L = v3(L4.x, L4.y, L4.z);
+      if (flags & kFlagNeePending) {
+        L = fold_slots(a, p, L);
+        flags &= ~kFlagNeePending;
+      }
       if (prim >= 0) {
         int x, y, s;
-        uint64_t pid = path_id(a, p, x, y, s);
+        pid = path_id(a, p, x, y, s);
         float t = h4.x, b1 = h4.z, b2 = h4.w, b0 = 1.0f - b1 - b2;
         float4 va = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim);
         float4 vb = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim + 1);
@@ -215,27 +240,23 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
         float4 s0 = __ldg(a.shade + 3 * (int64_t)prim), s1 = __ldg(a.shade + 3 * (int64_t)prim + 1),
                s2 = __ldg(a.shade + 3 * (int64_t)prim + 2);
         V3 v0 = v3(va.x, va.y, va.z), v1 = v3(vb.x, vb.y, vb.z), v2 = v3(vc.x, vc.y, vc.z);
-        V3 P = v0 * b0 + v1 * b1 + v2 * b2;
-        V3 ns = normalize(v3(s0.x, s0.y, s0.z) * b0 + v3(s1.x, s1.y, s1.z) * b1 + v3(s2.x, s2.y, s2.z) * b2);
-        V3 ng = normalize(cross(v1 - v0, v2 - v0));
+        P = v0 * b0 + v1 * b1 + v2 * b2;
+        ns = normalize(v3(s0.x, s0.y, s0.z) * b0 + v3(s1.x, s1.y, s1.z) * b1 + v3(s2.x, s2.y, s2.z) * b2);
+        ng = normalize(cross(v1 - v0, v2 - v0));
         int mi = __float_as_int(s0.w);
-        int li = __float_as_int(s1.w);
-        Material m = load_mat(a, mi);
+        self = __float_as_int(s1.w);
+        m = load_mat(a, mi);
         bool spec = is_specular(m);
         if (spec) flags |= kFlagSpecular;
-        if (li >= 0) {
-          Light lt = load_light(a, li);
+        if (self >= 0) {
+          Light lt = load_light(a, self);
           V3 Le = emitted(lt.Le, ns, -d);
           if (!a.efficient || depth == 0) L = L + mul(thr, Le);
           else if (ec) L = L + mul(thr, Le) * (lt.area / (t * t));
         }
-        if (a.efficient && !spec && a.nlight > (li >= 0 ? 1 : 0)) {
-          want_nee = true;
-          ne_p = make_float4(P.x, P.y, P.z, __int_as_float((int)p));
-          ne_n = make_float4(ns.x, ns.y, ns.z, __int_as_float(mi));
-          ne_w = make_float4(d.x, d.y, d.z, __int_as_float(li));
-          ne_t = make_float4(thr.x, thr.y, thr.z, __int_as_float(depth));
-          ne_g = make_float4(ng.x, ng.y, ng.z, 0.0f);
+        if (a.efficient && !spec && a.nlight > 0) {
+          do_nee = true;
+          flags |= kFlagNeePending;
         }
         F4u u = uniforms(a.rng, pid, (uint32_t)depth, 0);
         V3 wo, fs;
@@ -259,8 +280,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
             }
           }
         }
-        a.path_L[p] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
       }
+      a.path_L[p] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
     }
     uint32_t q = warp_append(&a.counters[kCtrRay + b + 1], want_next);
     if (want_next) {
@@ -268,83 +289,74 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
       a.qd[nxt][q] = no_d;
       a.qt[nxt][q] = no_t;
     }
-    uint32_t e = warp_append(&a.counters[kCtrNee + b], want_nee);
-    if (want_nee) {
-      a.np_[e] = ne_p;
-      a.nn_[e] = ne_n;
-      a.nw_[e] = ne_w;
-      a.nt_[e] = ne_t;
-      a.ng_[e] = ne_g;
-    }
-  }
-}
-
-// shadow: DirectIllumination::evaluate for one hit (all lights x noDirectSamples)
-template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
-  load_top(a);
-  TraceCounts c = {0, 0, 0, 0};
-  uint32_t rays_total = 0;
-  const Pair *top = top_ptr(a);
-  const uint32_t n = a.counters[kCtrNee + b];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 p4 = a.np_[i], n4 = a.nn_[i], w4 = a.nw_[i], t4 = a.nt_[i], g4 = a.ng_[i];
-    int64_t p = (int64_t)__float_as_int(p4.w);
-    int x, y, s;
-    uint64_t pid = path_id(a, p, x, y, s);
-    V3 P = v3(p4.x, p4.y, p4.z), ns = v3(n4.x, n4.y, n4.z), wi = v3(w4.x, w4.y, w4.z), ng = v3(g4.x, g4.y, g4.z);
-    int self = __float_as_int(w4.w);
-    int depth = __float_as_int(t4.w);
-    Material m = load_mat(a, __float_as_int(n4.w));
-    V3 sum = v3(0.0f, 0.0f, 0.0f);
-    uint32_t traced = 0;
-    const int side = a.nds_side;
-    for (int li = a.nlight - 1; li >= 0; --li) {
-      if (li == self) continue;
-      Light lt = load_light(a, li);
-      V3 dsum = v3(0.0f, 0.0f, 0.0f);
-      for (int sy = 0; sy < side; ++sy)
-        for (int sx = 0; sx < side; ++sx) {
-          int mi = (li * side + sy) * side + sx;
-          F4u u = uniforms(a.rng, pid, (uint32_t)depth, 1u + (uint32_t)(mi >> 1));
-          float ux = ((float)sx + ((mi & 1) ? u.c : u.a)) / (float)side;
-          float uy = ((float)sy + ((mi & 1) ? u.d : u.b)) / (float)side;
+    // light samples: every lane of the warp runs the same k loop (uniform trip count), so the
+    // warp-aggregated append stays converged
+    const float inv_nds = 1.0f / (float)a.nds;
+    for (int k = 0; k < a.nl_slots; ++k) {
+      bool want = false;
+      float4 so4, sd4;
+      if (do_nee) {
+        int li = k / s2n, within = k - li * s2n;
+        int sy = within / a.nds_side, sx = within - sy * a.nds_side;
+        V3 c = v3(0.0f, 0.0f, 0.0f);
+        if (li != self) {
+          Light lt = load_light(a, li);
+          F4u u = uniforms(a.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
+          float ux = ((float)sx + ((k & 1) ? u.c : u.a)) / (float)a.nds_side;
+          float uy = ((float)sy + ((k & 1) ? u.d : u.b)) / (float)a.nds_side;
           V3 lp = lt.center + lt.ex * (ux - 0.5f) + lt.ez * (uy - 0.5f);
           V3 wo = lp - P;
           float t = length(wo);
           wo = wo * (1.0f / t);
           float cwo = fabsf(dot(ns, wo)), cwi = fabsf(dot(lt.normal, wo));
-          V3 fr = bsdf_eval(m, ns, wi, wo);
+          V3 fr = bsdf_eval(m, ns, d, wo);
           if (cwo > 0.0f && cwi > 0.0f && nonzero(fr)) {
             V3 Le = emitted(lt.Le, lt.normal, -wo);
-            if (nonzero(Le)) {
-              Ray r;
-              r.o = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
-              r.d = wo;
-              r.tmin = 0.0f;
-              r.tmax = t * (1.0f - kShadowMargin);
-              Hit h;
-              ++traced;
-              if (!traverse<true, COUNT>(a.view, r, h, top, a.ntop, &c))
-                dsum = dsum + mul(fr, Le) * (cwo * cwi / (t * t));
+            c = mul(thr, mul(fr, Le)) * (cwo * cwi / (t * t) * lt.area * inv_nds);
+            if (nonzero(c)) {
+              want = true;
+              V3 org = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
+              so4 = make_float4(org.x, org.y, org.z, __uint_as_float((uint32_t)(p * a.nl_slots + k)));
+              sd4 = make_float4(wo.x, wo.y, wo.z, t * (1.0f - kShadowMargin));
             }
           }
         }
-      sum = sum + dsum * (lt.area / (float)a.nds);
-    }
-    if (traced) atomicAdd(&a.counters[kCtrShadowRays], traced);
-    rays_total += traced;
-    if (nonzero(sum)) {
-      float4 L4 = a.path_L[p];
-      V3 thr = v3(t4.x, t4.y, t4.z);
-      a.path_L[p] = make_float4(L4.x + thr.x * sum.x, L4.y + thr.y * sum.y, L4.z + thr.z * sum.z, L4.w);
+        a.slots[p * a.nl_slots + k] = make_float4(c.x, c.y, c.z, 0.0f);
+      }
+      uint32_t e = warp_append(&a.counters[kCtrNee + b], want);
+      if (want) {
+        a.so[e] = so4;
+        a.sd[e] = sd4;
+      }
     }
   }
-  if (COUNT && rays_total) {
+}
+
+// shadow: any-hit query per queued light sample; an occluded sample's slot is zeroed
+template <bool COUNT>
+__global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
+  load_top(a);
+  TraceCounts c = {0, 0, 0, 0};
+  uint32_t rays = 0;
+  const Pair *top = top_ptr(a);
+  const uint32_t n = a.counters[kCtrNee + b];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 o = a.so[i], d = a.sd[i];
+    Ray r;
+    r.o = v3(o.x, o.y, o.z);
+    r.tmin = 0.0f;
+    r.d = v3(d.x, d.y, d.z);
+    r.tmax = d.w;
+    Hit h;
+    if (traverse<true, COUNT>(a.view, r, h, top, a.ntop, &c))
+      a.slots[__float_as_uint(o.w)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    ++rays;
+  }
+  if (COUNT && rays) {
     atomicAdd(&a.tcount[4], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[5], (unsigned long long)c.refs);
     atomicAdd(&a.tcount[6], (unsigned long long)c.tris);
-    atomicAdd(&a.tcount[7], (unsigned long long)rays_total);
+    atomicAdd(&a.tcount[7], (unsigned long long)rays);
   }
 }
 
@@ -358,8 +370,10 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
       ext += c;
       bounces += c ? 1ull : 0ull;
     }
+    unsigned long long sh = 0;
+    for (int b = 0; b < a.max_b; ++b) sh += a.counters[kCtrNee + b];
     a.stats[0] += ext;
-    a.stats[1] += a.counters[kCtrShadowRays];
+    a.stats[1] += sh;
     a.stats[2] += a.counters[kCtrTrunc];
     a.stats[3] += bounces;
   }
@@ -370,8 +384,11 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
     int64_t pix = (int64_t)y * a.W + x;
     float4 S = a.film_sum[pix], C = a.film_c[pix];
     for (int si = 0; si < a.ns; ++si) {
-      float4 L4 = a.path_L[q * a.ns + si];
-      V3 L = apply_mask(v3(L4.x, L4.y, L4.z), __float_as_uint(L4.w));
+      const int64_t p = q * a.ns + si;
+      float4 L4 = a.path_L[p];
+      V3 L = v3(L4.x, L4.y, L4.z);
+      if (__float_as_uint(L4.w) & kFlagNeePending) L = fold_slots(a, p, L);
+      L = apply_mask(L, __float_as_uint(L4.w));
       if (a.path_out) {
         int s = a.s0 + si - a.sample_begin;
         a.path_out[pix * a.sample_count + s] = make_float4(L.x, L.y, L.z, L4.w);
@@ -394,7 +411,8 @@ struct Workspace {
   int64_t cap = 0;  // paths
   void *block = nullptr;
   float4 *path_L = nullptr, *qo[2] = {}, *qd[2] = {}, *qt[2] = {}, *qhit = nullptr;
-  float4 *np_ = nullptr, *nn_ = nullptr, *nw_ = nullptr, *nt_ = nullptr, *ng_ = nullptr;
+  float4 *so = nullptr, *sd = nullptr, *slots = nullptr;
+  int64_t slot_cap = 0;  // light-sample slots
   uint32_t *counters = nullptr;
   unsigned long long *stats = nullptr;   // 4
   unsigned long long *tcount = nullptr;  // 8
@@ -457,10 +475,10 @@ struct Profiler {
 };
 static thread_local Profiler t_prof;
 
-static int ensure_workspace(int64_t paths) {
+static int ensure_workspace(int64_t paths, int64_t slots) {
   int dev = 0;
   MGPU_CUDA(cudaGetDevice(&dev));
-  if (t_ws && t_ws->device == dev && t_ws->cap >= paths) return MGPU_OK;
+  if (t_ws && t_ws->device == dev && t_ws->cap >= paths && t_ws->slot_cap >= slots) return MGPU_OK;
   if (t_ws) {
     cudaDeviceSynchronize();
     delete t_ws;
@@ -469,8 +487,10 @@ static int ensure_workspace(int64_t paths) {
   Workspace *w = new Workspace();
   w->device = dev;
   w->cap = paths;
+  w->slot_cap = slots;
   size_t per = (size_t)paths * sizeof(float4);
-  size_t total = per * 13 + 12 * sizeof(unsigned long long) + kNumCounters * sizeof(uint32_t) + 256;
+  size_t total = per * 8 + (size_t)slots * 3 * sizeof(float4) + 12 * sizeof(unsigned long long) +
+                 kNumCounters * sizeof(uint32_t) + 256;
   cudaError_t e = cudaMalloc(&w->block, total);
   if (e != cudaSuccess) {
     delete w;
@@ -480,7 +500,7 @@ static int ensure_workspace(int64_t paths) {
   w->path_L = f; f += paths;
   for (int k = 0; k < 2; ++k) { w->qo[k] = f; f += paths; w->qd[k] = f; f += paths; w->qt[k] = f; f += paths; }
   w->qhit = f; f += paths;
-  w->np_ = f; f += paths; w->nn_ = f; f += paths; w->nw_ = f; f += paths; w->nt_ = f; f += paths; w->ng_ = f; f += paths;
+  w->so = f; f += slots; w->sd = f; f += slots; w->slots = f; f += slots;
   w->stats = (unsigned long long *)f;
   w->tcount = w->stats + 4;
   w->counters = (uint32_t *)(w->tcount + 8);
@@ -568,13 +588,15 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   int ns = (int)std::max<int64_t>(1, std::min<int64_t>(rp->sample_count, wave / total_slots));
   int64_t slots_per_wave = std::min<int64_t>(total_slots, std::max<int64_t>(64, wave / ns) / 64 * 64);
   int64_t cap = slots_per_wave * ns;
-  int rc = ensure_workspace(cap);
+  a.nl_slots = sc->nlight * a.nds_side * a.nds_side;
+  if (a.nl_slots > 4096) return fail(MGPU_E_INVALID, "mgpu_render: too many light samples per vertex");
+  int rc = ensure_workspace(cap, std::max<int64_t>(1, cap * a.nl_slots));
   if (rc != MGPU_OK) return rc;
   Workspace *w = t_ws;
   a.path_L = w->path_L;
   for (int k = 0; k < 2; ++k) { a.qo[k] = w->qo[k]; a.qd[k] = w->qd[k]; a.qt[k] = w->qt[k]; }
   a.qhit = w->qhit;
-  a.np_ = w->np_; a.nn_ = w->nn_; a.nw_ = w->nw_; a.nt_ = w->nt_; a.ng_ = w->ng_;
+  a.so = w->so; a.sd = w->sd; a.slots = w->slots;
   a.counters = w->counters;
   a.stats = w->stats;
   a.tcount = w->tcount;

@@ -112,6 +112,9 @@ class DeviceScene:
         N.check(self._lib.mgpu_scene_create(C.byref(d), accel.handle, _stream_handle(stream), C.byref(self.handle)))
         self.scene = scene
 
+    def set_top_pairs(self, n: int) -> None:
+        N.check(self._lib.mgpu_scene_set_top_pairs(self.handle, n))
+
     @property
     def nbytes(self) -> int:
         v = C.c_uint64()
