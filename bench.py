@@ -313,6 +313,24 @@ def run_ours(args):
     return 0
 
 
+def run_profile_case(args):
+    """Small case for ncu captures: the mid scene (~143 MB resident, larger than the 129 MB
+    L2) at 512 x 512 x 4 spp = 1,048,576 paths per frame, two frames."""
+    import torch
+
+    from milton_gb300 import pathtracer as pt
+    from milton_gb300 import scenegen
+    s = scenegen.mid(SEED)
+    ds = pt.DeviceScene(s, pt.Accel(s))
+    film = pt.Film(512, 512)
+    st = pt.RenderSettings(512, 512, 4, max_depth=MAX_DEPTH, rr_start_depth=RR_START, seed=SEED)
+    for _ in range(2):
+        pt.render(ds, st, film)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "mid 512x512x4spp x2", **pt.render_stats()}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -320,7 +338,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true", help="small two-frame case for ncu captures")
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -204,7 +204,9 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   s->d_lights = (float *)(base + off_lights);
   s->nmat = desc->nmat;
   s->nlight = desc->nlight;
-  s->top_pairs = tr.top_pairs;
+  // staging the top of the tree in shared memory costs more occupancy than it saves on GB300
+  // (the L1 keeps those pairs anyway); mgpu_scene_set_top_pairs turns it on
+  s->top_pairs = 0;
   s->top_pairs_max = tr.top_pairs;
   s->d_err = (uint32_t *)(base + off_err);
   s->bytes = total;

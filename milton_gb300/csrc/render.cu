@@ -583,7 +583,7 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   a.path_out = (float4 *)d_path_out;
   const int64_t tiles_y = (a.H + 7) / 8;
   const int64_t total_slots = (int64_t)a.tiles_x * tiles_y * 64;
-  int64_t wave = rp->wave_paths > 0 ? rp->wave_paths : (int64_t)1 << 22;
+  int64_t wave = rp->wave_paths > 0 ? rp->wave_paths : (int64_t)1 << 24;
   // samples per wave: as many passes of the whole image as fit, else one pass over a slot range
   int ns = (int)std::max<int64_t>(1, std::min<int64_t>(rp->sample_count, wave / total_slots));
   int64_t slots_per_wave = std::min<int64_t>(total_slots, std::max<int64_t>(64, wave / ns) / 64 * 64);
