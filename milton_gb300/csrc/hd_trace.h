@@ -182,103 +182,185 @@ MGPU_HD bool clip_root(const SceneView &s, const Ray &r, V3 inv, float &t0, floa
 
 constexpr float kCellEps = 1.0f / 262144.0f;  // relative widening of cell intervals (2^-18)
 
+// Resumable traversal state: one call of trav_step descends to the next leaf, tests it and
+// either finishes or pops the next cell.  Persistent kernels interleave steps of many rays per
+// warp (a lane whose ray finishes fetches another), the plain traverse() runs it to the end.
+struct TravEntry {
+  uint32_t w0, w1;
+  float tmax;
+};
+
+struct TravState {
+  RayPre pre;
+  V3 inv;
+  float tmin, tmax;   // current cell interval
+  float ray_tmin;
+  float best;         // closest accepted t so far (starts at the ray's tmax)
+  int32_t best_prim;
+  float bb1, bb2;
+  uint32_t w0, w1;    // current node slot
+  int sp;
+  TravEntry stack[kMaxStack];
+};
+
+// returns false when the ray misses the scene (no step needed)
+MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32_t ntop, TravState &st) {
+  st.best = r.tmax;
+  st.best_prim = -1;
+  st.bb1 = st.bb2 = 0.0f;
+  if (s.ntri <= 0) return false;
+  st.inv = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  float t0, t1;
+  if (!clip_root(s, r, st.inv, t0, t1)) return false;
+  st.tmin = fmaxf(t0, r.tmin);
+  st.tmax = fminf(t1, r.tmax);
+  if (st.tmin > st.tmax) return false;
+  st.ray_tmin = r.tmin;
+  st.pre = precompute(r);
+  st.sp = 0;
+  Pair root = load_pair(s, top, ntop, 0);
+  st.w0 = root.a0;
+  st.w1 = root.a1;
+  return true;
+}
+
+// One leaf: descend, test, then finish (true) or move to the next cell (false).
+template <bool ANY, bool COUNT>
+MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint32_t ntop, TraceCounts *cnt) {
+  const float o[3] = {st.pre.o.x, st.pre.o.y, st.pre.o.z};
+  const float iv[3] = {st.inv.x, st.inv.y, st.inv.z};
+  uint32_t w0 = st.w0, w1 = st.w1;
+  float tmin = st.tmin, tmax = st.tmax;
+  while ((w0 & 3u) != kLeafTag) {
+    if (COUNT) cnt->nodes++;
+    int ax = (int)(w0 & 3u);
+    float split = bits_f(w1);
+    float diff = split - o[ax];
+    float dinv = iv[ax];
+    Pair pr = load_pair(s, top, ntop, w0 >> 2);
+    if (isinf(dinv)) {
+      // ray parallel to the split plane: only the side holding the origin (both if the ray
+      // lies in the plane).  Milton's traversal evaluates 0 * inf here and, for a +0
+      // direction component, descends into the wrong child.
+      if (diff > 0.0f) { w0 = pr.a0; w1 = pr.a1; }
+      else if (diff < 0.0f) { w0 = pr.b0; w1 = pr.b1; }
+      else {
+        if (st.sp < kMaxStack) {
+          st.stack[st.sp].w0 = pr.b0; st.stack[st.sp].w1 = pr.b1; st.stack[st.sp].tmax = tmax;
+          ++st.sp;
+          if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
+        }
+        w0 = pr.a0; w1 = pr.a1;
+      }
+      continue;
+    }
+    float dt = diff * dinv;
+    // near child = the side of the origin (Milton's ordering by the signs of diff and d)
+    bool rev = diff <= 0.0f ? (dinv <= 0.0f) : (dinv < 0.0f);
+    uint32_t n0 = rev ? pr.b0 : pr.a0, n1 = rev ? pr.b1 : pr.a1;
+    uint32_t f0 = rev ? pr.a0 : pr.b0, f1 = rev ? pr.a1 : pr.b1;
+    float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
+    if (dt > tmax + slack) {
+      w0 = n0; w1 = n1;               // far child not reached inside this cell
+    } else if (dt < tmin - slack) {
+      w0 = f0; w1 = f1;               // near child lies behind the cell
+    } else {
+      // the ray crosses the plane inside the cell: near child first, far child on the stack
+      if (st.sp < kMaxStack) {
+        st.stack[st.sp].w0 = f0; st.stack[st.sp].w1 = f1; st.stack[st.sp].tmax = tmax;
+        ++st.sp;
+        if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
+      }
+      w0 = n0; w1 = n1;
+      tmax = fminf(tmax, dt);
+    }
+  }
+  if (COUNT) cnt->nodes++;
+  const uint32_t count = w0 >> 2;
+  for (uint32_t i = 0; i < count; ++i) {
+    uint32_t tri = (count == 1) ? w1 : load_u32(s.refs, (uint64_t)w1 + i);
+    if (COUNT) { cnt->refs += (count == 1) ? 0u : 1u; cnt->tris++; }
+    F4 a = load_f4(s.tris, 3 * (int64_t)tri + 0);
+    F4 b = load_f4(s.tris, 3 * (int64_t)tri + 1);
+    F4 c = load_f4(s.tris, 3 * (int64_t)tri + 2);
+    bool culled = (f_bits(a.w) & 1u) != 0u;
+    float t, b1, b2;
+    if (intersect_tri(st.pre, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), culled, st.ray_tmin, st.best, t,
+                      b1, b2)) {
+      st.best = t; st.best_prim = (int32_t)tri; st.bb1 = b1; st.bb2 = b2;
+      if (ANY) return true;
+    }
+  }
+  // early exit: the best hit lies inside this cell, later cells are farther
+  if (!ANY && st.best_prim >= 0 && st.best <= tmax + kCellEps * fabsf(tmax)) return true;
+  for (;;) {
+    if (st.sp == 0) return true;
+    --st.sp;
+    st.tmin = tmax;
+    st.w0 = st.stack[st.sp].w0; st.w1 = st.stack[st.sp].w1; st.tmax = st.stack[st.sp].tmax;
+    if (!ANY && st.best_prim >= 0 && st.best < st.tmin) return true;
+    return false;
+  }
+}
+
 // ANY = shadow query (returns on the first hit inside (tmin, tmax)).
 template <bool ANY, bool COUNT>
 MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *top, uint32_t ntop, TraceCounts *cnt) {
+  TravState st;
   hit.t = INFINITY; hit.prim = -1; hit.b1 = 0.0f; hit.b2 = 0.0f;
-  if (s.ntri <= 0) return false;
-  V3 inv = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
-  float t0, t1;
-  if (!clip_root(s, r, inv, t0, t1)) return false;
-  float tmin = fmaxf(t0, r.tmin);
-  float tmax = fminf(t1, r.tmax);
-  if (tmin > tmax) return false;
-  RayPre pre = precompute(r);
-  float best = r.tmax;
-  int32_t best_prim = -1;
-  float bb1 = 0.0f, bb2 = 0.0f;
-
-  struct Entry { uint32_t w0, w1; float tmax; };
-  Entry stack[kMaxStack];
-  int sp = 0;
-  const float o[3] = {r.o.x, r.o.y, r.o.z};
-  const float dd[3] = {r.d.x, r.d.y, r.d.z};
-  const float iv[3] = {inv.x, inv.y, inv.z};
-
-  Pair root = load_pair(s, top, ntop, 0);
-  uint32_t w0 = root.a0, w1 = root.a1;
-  for (;;) {
-    while ((w0 & 3u) != kLeafTag) {
-      if (COUNT) cnt->nodes++;
-      int ax = (int)(w0 & 3u);
-      float split = bits_f(w1);
-      float diff = split - o[ax];
-      float dt = diff * iv[ax];
-      bool rev = diff <= 0.0f ? (dd[ax] <= 0.0f) : (dd[ax] < 0.0f);
-      Pair pr = load_pair(s, top, ntop, w0 >> 2);
-      if (dd[ax] == 0.0f) {
-        // ray parallel to the split plane: only the side holding the origin (both if the ray
-        // lies in the plane).  Milton's traversal evaluates 0 * inf here and, for a +0
-        // direction component, descends into the wrong child.
-        if (diff > 0.0f) { w0 = pr.a0; w1 = pr.a1; }
-        else if (diff < 0.0f) { w0 = pr.b0; w1 = pr.b1; }
-        else {
-          if (sp < kMaxStack) {
-            stack[sp].w0 = pr.b0; stack[sp].w1 = pr.b1; stack[sp].tmax = tmax;
-            ++sp;
-            if (COUNT && (uint32_t)sp > cnt->max_stack) cnt->max_stack = (uint32_t)sp;
-          }
-          w0 = pr.a0; w1 = pr.a1;
-        }
-        continue;
-      }
-      uint32_t n0 = rev ? pr.b0 : pr.a0, n1 = rev ? pr.b1 : pr.a1;
-      uint32_t f0 = rev ? pr.a0 : pr.b0, f1 = rev ? pr.a1 : pr.b1;
-      float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
-      if (dt > tmax + slack) {
-        w0 = n0; w1 = n1;               // far child not reached inside this cell
-      } else if (dt < tmin - slack) {
-        w0 = f0; w1 = f1;               // near child lies behind the cell
-      } else {
-        // the ray crosses the plane inside the cell: near child first, far child on the stack
-        if (sp < kMaxStack) {
-          stack[sp].w0 = f0; stack[sp].w1 = f1; stack[sp].tmax = tmax;
-          ++sp;
-          if (COUNT && (uint32_t)sp > cnt->max_stack) cnt->max_stack = (uint32_t)sp;
-        }
-        w0 = n0; w1 = n1;
-        tmax = fminf(tmax, dt);
-      }
-    }
-    if (COUNT) cnt->nodes++;
-    uint32_t count = w0 >> 2;
-    for (uint32_t i = 0; i < count; ++i) {
-      uint32_t tri = (count == 1) ? w1 : load_u32(s.refs, (uint64_t)w1 + i);
-      if (COUNT) { cnt->refs += (count == 1) ? 0u : 1u; cnt->tris++; }
-      F4 a = load_f4(s.tris, 3 * (int64_t)tri + 0);
-      F4 b = load_f4(s.tris, 3 * (int64_t)tri + 1);
-      F4 c = load_f4(s.tris, 3 * (int64_t)tri + 2);
-      bool culled = (f_bits(a.w) & 1u) != 0u;
-      float t, b1, b2;
-      if (intersect_tri(pre, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), culled, r.tmin, best, t, b1,
-                        b2)) {
-        best = t; best_prim = (int32_t)tri; bb1 = b1; bb2 = b2;
-        if (ANY) {
-          hit.t = t; hit.prim = best_prim; hit.b1 = b1; hit.b2 = b2;
-          return true;
-        }
-      }
-    }
-    if (!ANY && best_prim >= 0 && best <= tmax + kCellEps * fabsf(tmax)) break;  // early exit
-    if (sp == 0) break;
-    --sp;
-    tmin = tmax;
-    w0 = stack[sp].w0; w1 = stack[sp].w1; tmax = stack[sp].tmax;
-    if (!ANY && best_prim >= 0 && best < tmin) break;
+  if (!trav_init(s, r, top, ntop, st)) return false;
+  while (!trav_step<ANY, COUNT>(s, st, top, ntop, cnt)) {
   }
-  if (best_prim < 0) return false;
-  hit.t = best; hit.prim = best_prim; hit.b1 = bb1; hit.b2 = bb2;
+  if (st.best_prim < 0) return false;
+  hit.t = st.best; hit.prim = st.best_prim; hit.b1 = st.bb1; hit.b2 = st.bb2;
   return true;
 }
+
+#if defined(__CUDACC__)
+// Persistent warp-level traversal (Aila and Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", HPG 2009): every lane owns one ray; after each leaf step, lanes whose
+// ray finished take new rays from a global counter with one warp-aggregated atomicAdd, so a
+// warp never idles behind its slowest ray.  All 32 lanes of every warp must call this.
+//   load(i, ray)            fills the i-th ray of the batch
+//   store(i, found, state)  consumes the i-th result
+template <bool ANY, bool COUNT, class Load, class Store>
+__device__ __forceinline__ void persistent_trace(const SceneView &s, const Pair *top, uint32_t ntop, uint32_t n,
+                                                 uint32_t *fetch, Load load, Store store, TraceCounts *cnt,
+                                                 uint32_t &rays_done) {
+  const unsigned kFull = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  TravState st;
+  uint32_t idx = 0;
+  bool have = false, exhausted = false;
+  for (;;) {
+    bool need = !have && !exhausted;
+    unsigned m = __ballot_sync(kFull, need);
+    if (m) {
+      int leader = __ffs(m) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(m));
+      base = __shfl_sync(kFull, base, leader);
+      if (need) {
+        uint32_t my = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        if (my < n) {
+          idx = my;
+          Ray r;
+          load(idx, r);
+          ++rays_done;
+          if (trav_init(s, r, top, ntop, st)) have = true;
+          else store(idx, false, st);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__all_sync(kFull, exhausted && !have)) break;
+    if (have && trav_step<ANY, COUNT>(s, st, top, ntop, cnt)) {
+      store(idx, st.best_prim >= 0, st);
+      have = false;
+    }
+  }
+}
+#endif
 
 }  // namespace mgpu

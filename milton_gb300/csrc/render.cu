@@ -26,8 +26,9 @@ constexpr int kBlock = 128;
 constexpr int kHardCap = 1024;          // vertex cap when max_depth = 0 (Milton has none)
 constexpr int kCtrRay = 0;              // counters[kCtrRay + b]  live paths at bounce b
 constexpr int kCtrNee = kHardCap + 8;   // counters[kCtrNee + b]  shadow rays at bounce b
-constexpr int kCtrTrunc = 2 * (kHardCap + 8);
-constexpr int kCtrShadowRays = kCtrTrunc + 1;
+constexpr int kCtrFetchExt = 2 * (kHardCap + 8);   // work counters of the persistent extend kernel
+constexpr int kCtrFetchSh = 3 * (kHardCap + 8);    // ... and of the persistent shadow kernel
+constexpr int kCtrTrunc = 4 * (kHardCap + 8);
 constexpr int kNumCounters = kCtrTrunc + 8;
 constexpr float kShadowMargin = 1e-4f;  // shadow rays stop this fraction short of the light
 
@@ -165,20 +166,21 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
   const Pair *top = top_ptr(a);
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
+  float4 *qhit = a.qhit;
   TraceCounts c = {0, 0, 0, 0};
   uint32_t rays = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  auto load = [&](uint32_t i, Ray &r) {
     float4 o = qo[i], d = qd[i];
-    Ray r;
     r.o = v3(o.x, o.y, o.z);
     r.tmin = 0.0f;
     r.d = v3(d.x, d.y, d.z);
     r.tmax = INFINITY;
-    Hit h;
-    bool hit = traverse<false, COUNT>(a.view, r, h, top, a.ntop, &c);
-    a.qhit[i] = make_float4(hit ? h.t : INFINITY, __int_as_float(hit ? h.prim : -1), h.b1, h.b2);
-    ++rays;
-  }
+  };
+  auto store = [&](uint32_t i, bool hit, const TravState &st) {
+    qhit[i] = make_float4(hit ? st.best : INFINITY, __int_as_float(hit ? st.best_prim : -1), hit ? st.bb1 : 0.0f,
+                          hit ? st.bb2 : 0.0f);
+  };
+  persistent_trace<false, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[0], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[1], (unsigned long long)c.refs);
@@ -336,22 +338,23 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
   load_top(a);
-  TraceCounts c = {0, 0, 0, 0};
-  uint32_t rays = 0;
   const Pair *top = top_ptr(a);
   const uint32_t n = a.counters[kCtrNee + b];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 o = a.so[i], d = a.sd[i];
-    Ray r;
+  const float4 *so = a.so, *sd = a.sd;
+  float4 *slots = a.slots;
+  TraceCounts c = {0, 0, 0, 0};
+  uint32_t rays = 0;
+  auto load = [&](uint32_t i, Ray &r) {
+    float4 o = so[i], d = sd[i];
     r.o = v3(o.x, o.y, o.z);
     r.tmin = 0.0f;
     r.d = v3(d.x, d.y, d.z);
     r.tmax = d.w;
-    Hit h;
-    if (traverse<true, COUNT>(a.view, r, h, top, a.ntop, &c))
-      a.slots[__float_as_uint(o.w)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    ++rays;
-  }
+  };
+  auto store = [&](uint32_t i, bool hit, const TravState &) {
+    if (hit) slots[__float_as_uint(so[i].w)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  };
+  persistent_trace<true, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[4], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[5], (unsigned long long)c.refs);

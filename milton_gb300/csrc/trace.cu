@@ -13,30 +13,32 @@ constexpr int kTraceBlock = 128;
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(kTraceBlock) k_trace(SceneView s, uint32_t ntop, const float4 *__restrict__ rays,
                                                       float4 *__restrict__ hits, uint8_t *__restrict__ occ,
-                                                      uint4 *__restrict__ counts, int64_t n) {
+                                                      uint4 *__restrict__ counts, uint32_t n, uint32_t *fetch) {
   extern __shared__ uint4 smem_top[];
   for (uint32_t i = threadIdx.x; i < ntop; i += blockDim.x)
     smem_top[i] = __ldg(reinterpret_cast<const uint4 *>(s.pairs) + i);
   __syncthreads();
-  const Pair *top = reinterpret_cast<const Pair *>(smem_top);
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
-    Ray r;
+  const Pair *top = ntop ? reinterpret_cast<const Pair *>(smem_top) : nullptr;
+  TraceCounts c = {0, 0, 0, 0};
+  uint32_t done = 0;
+  auto load = [&](uint32_t i, Ray &r) {
+    float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
     r.o = v3(a.x, a.y, a.z);
     r.tmin = a.w;
     r.d = v3(b.x, b.y, b.z);
     r.tmax = b.w;
-    Hit h;
-    TraceCounts c = {0, 0, 0, 0};
-    bool hit = traverse<ANY, COUNT>(s, r, h, ntop ? top : nullptr, ntop, &c);
+    if (COUNT) c = TraceCounts{0, 0, 0, 0};
+  };
+  auto store = [&](uint32_t i, bool hit, const TravState &st) {
     if (ANY) {
       occ[i] = hit ? 1 : 0;
     } else {
-      hits[i] = make_float4(hit ? h.t : INFINITY, __int_as_float(hit ? h.prim : -1), h.b1, h.b2);
+      hits[i] = make_float4(hit ? st.best : INFINITY, __int_as_float(hit ? st.best_prim : -1), hit ? st.bb1 : 0.0f,
+                            hit ? st.bb2 : 0.0f);
     }
     if (COUNT) counts[i] = make_uint4(c.nodes, c.refs, c.tris, c.max_stack);
-  }
+  };
+  persistent_trace<ANY, COUNT>(s, top, ntop, n, fetch, load, store, &c, done);
 }
 
 template <bool ANY, bool COUNT>
@@ -45,6 +47,7 @@ static int launch_trace(const mgpu_scene *s, const float *rays, float *hits, uin
   if (!s) return fail(MGPU_E_INVALID, "trace: null scene");
   if (n < 0) return fail(MGPU_E_INVALID, "trace: negative ray count");
   if (n == 0) return MGPU_OK;
+  if (n > (int64_t)0xFFFFFFFF) return fail(MGPU_E_INVALID, "trace: more than 2^32 - 1 rays in one call");
   if (!rays || (ANY ? !occ : !hits) || (COUNT && !counts)) return fail(MGPU_E_INVALID, "trace: null buffer");
   if (((uintptr_t)rays & 15) || (!ANY && ((uintptr_t)hits & 15)) || (COUNT && ((uintptr_t)counts & 15)))
     return fail(MGPU_E_INVALID, "trace: ray/hit/count buffers must be 16-byte aligned");
@@ -57,8 +60,9 @@ static int launch_trace(const mgpu_scene *s, const float *rays, float *hits, uin
   if (per_sm < 1) per_sm = 1;
   int64_t want = (n + kTraceBlock - 1) / kTraceBlock;
   int64_t grid = std::min<int64_t>(want, (int64_t)device_sm_count() * per_sm);
+  MGPU_CUDA(cudaMemsetAsync(s->d_err + 1, 0, sizeof(uint32_t), as_stream(stream)));
   kern<<<(unsigned)grid, kTraceBlock, smem, as_stream(stream)>>>(s->view, ntop, (const float4 *)rays, (float4 *)hits,
-                                                                  occ, (uint4 *)counts, n);
+                                                                  occ, (uint4 *)counts, (uint32_t)n, s->d_err + 1);
   g_launches.fetch_add(1);
   MGPU_CUDA(cudaGetLastError());
   return MGPU_OK;
