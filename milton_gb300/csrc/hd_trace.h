@@ -183,25 +183,52 @@ MGPU_HD bool clip_root(const SceneView &s, const Ray &r, V3 inv, float &t0, floa
 constexpr float kCellEps = 1.0f / 262144.0f;  // relative widening of cell intervals (2^-18)
 
 // Resumable traversal state: one call of trav_step descends to the next leaf, tests it and
-// either finishes or pops the next cell.  Persistent kernels interleave steps of many rays per
-// warp (a lane whose ray finishes fetches another), the plain traverse() runs it to the end.
-struct TravEntry {
-  uint32_t w0, w1;
-  float tmax;
-};
+// either finishes or moves on to the next cell.  The far-child stack is a short stack of
+// kShortStack entries held in registers (static indices only); when it overflows the oldest
+// entry is dropped, and when it runs empty before the ray has left the scene the descent
+// restarts from the root with the interval [end of the last cell, exit]
+// (kd-restart / short-stack traversal, Foley and Sugerman 2005, Horn et al. 2007).
+constexpr int kShortStack = 6;
+constexpr uint32_t kMaxLeafSteps = 1u << 20;  // guard: a ray that takes more leaf steps is abandoned
 
 struct TravState {
   RayPre pre;
   V3 inv;
   float tmin, tmax;   // current cell interval
+  float texit;        // where the ray leaves the root box (clipped to its tmax)
   float ray_tmin;
   float best;         // closest accepted t so far (starts at the ray's tmax)
   int32_t best_prim;
   float bb1, bb2;
   uint32_t w0, w1;    // current node slot
-  int sp;
-  TravEntry stack[kMaxStack];
+  uint32_t steps;
+  bool restart;       // descending from the root after the short stack ran empty
+  int sp;             // live entries in the short stack
+  uint32_t s0[kShortStack], s1[kShortStack];
+  float st[kShortStack];
 };
+
+MGPU_HD void stack_push(TravState &t, uint32_t w0, uint32_t w1, float tmax) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int i = kShortStack - 1; i > 0; --i) {
+    t.s0[i] = t.s0[i - 1]; t.s1[i] = t.s1[i - 1]; t.st[i] = t.st[i - 1];
+  }
+  t.s0[0] = w0; t.s1[0] = w1; t.st[0] = tmax;
+  if (t.sp < kShortStack) ++t.sp;
+}
+
+MGPU_HD void stack_pop(TravState &t, uint32_t &w0, uint32_t &w1, float &tmax) {
+  w0 = t.s0[0]; w1 = t.s1[0]; tmax = t.st[0];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int i = 0; i < kShortStack - 1; ++i) {
+    t.s0[i] = t.s0[i + 1]; t.s1[i] = t.s1[i + 1]; t.st[i] = t.st[i + 1];
+  }
+  --t.sp;
+}
 
 // returns false when the ray misses the scene (no step needed)
 MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32_t ntop, TravState &st) {
@@ -215,9 +242,12 @@ MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32
   st.tmin = fmaxf(t0, r.tmin);
   st.tmax = fminf(t1, r.tmax);
   if (st.tmin > st.tmax) return false;
+  st.texit = st.tmax;
   st.ray_tmin = r.tmin;
   st.pre = precompute(r);
   st.sp = 0;
+  st.steps = 0;
+  st.restart = false;
   Pair root = load_pair(s, top, ntop, 0);
   st.w0 = root.a0;
   st.w1 = root.a1;
@@ -231,6 +261,7 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint3
   const float iv[3] = {st.inv.x, st.inv.y, st.inv.z};
   uint32_t w0 = st.w0, w1 = st.w1;
   float tmin = st.tmin, tmax = st.tmax;
+  const bool restart = st.restart;
   while ((w0 & 3u) != kLeafTag) {
     if (COUNT) cnt->nodes++;
     int ax = (int)(w0 & 3u);
@@ -245,11 +276,8 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint3
       if (diff > 0.0f) { w0 = pr.a0; w1 = pr.a1; }
       else if (diff < 0.0f) { w0 = pr.b0; w1 = pr.b1; }
       else {
-        if (st.sp < kMaxStack) {
-          st.stack[st.sp].w0 = pr.b0; st.stack[st.sp].w1 = pr.b1; st.stack[st.sp].tmax = tmax;
-          ++st.sp;
-          if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
-        }
+        stack_push(st, pr.b0, pr.b1, tmax);
+        if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
         w0 = pr.a0; w1 = pr.a1;
       }
       continue;
@@ -260,22 +288,23 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint3
     uint32_t n0 = rev ? pr.b0 : pr.a0, n1 = rev ? pr.b1 : pr.a1;
     uint32_t f0 = rev ? pr.a0 : pr.b0, f1 = rev ? pr.a1 : pr.b1;
     float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
+    // after a restart the cells ending at tmin are finished: no widening on that side, so
+    // the descent cannot return to them
+    bool near_behind = restart ? (dt <= tmin) : (dt < tmin - slack);
     if (dt > tmax + slack) {
       w0 = n0; w1 = n1;               // far child not reached inside this cell
-    } else if (dt < tmin - slack) {
+    } else if (near_behind) {
       w0 = f0; w1 = f1;               // near child lies behind the cell
     } else {
       // the ray crosses the plane inside the cell: near child first, far child on the stack
-      if (st.sp < kMaxStack) {
-        st.stack[st.sp].w0 = f0; st.stack[st.sp].w1 = f1; st.stack[st.sp].tmax = tmax;
-        ++st.sp;
-        if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
-      }
+      stack_push(st, f0, f1, tmax);
+      if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
       w0 = n0; w1 = n1;
       tmax = fminf(tmax, dt);
     }
   }
   if (COUNT) cnt->nodes++;
+  st.restart = false;
   const uint32_t count = w0 >> 2;
   for (uint32_t i = 0; i < count; ++i) {
     uint32_t tri = (count == 1) ? w1 : load_u32(s.refs, (uint64_t)w1 + i);
@@ -293,14 +322,20 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint3
   }
   // early exit: the best hit lies inside this cell, later cells are farther
   if (!ANY && st.best_prim >= 0 && st.best <= tmax + kCellEps * fabsf(tmax)) return true;
-  for (;;) {
-    if (st.sp == 0) return true;
-    --st.sp;
-    st.tmin = tmax;
-    st.w0 = st.stack[st.sp].w0; st.w1 = st.stack[st.sp].w1; st.tmax = st.stack[st.sp].tmax;
-    if (!ANY && st.best_prim >= 0 && st.best < st.tmin) return true;
-    return false;
+  if (++st.steps >= kMaxLeafSteps) return true;
+  st.tmin = tmax;
+  if (st.sp > 0) {
+    stack_pop(st, st.w0, st.w1, st.tmax);
+  } else {
+    // short stack empty: done if the ray has left the scene, else restart from the root
+    if (!(tmax < st.texit)) return true;
+    Pair root = load_pair(s, top, ntop, 0);
+    st.w0 = root.a0; st.w1 = root.a1;
+    st.tmax = st.texit;
+    st.restart = true;
   }
+  if (!ANY && st.best_prim >= 0 && st.best < st.tmin) return true;
+  return false;
 }
 
 // ANY = shadow query (returns on the first hit inside (tmin, tmax)).
