@@ -169,9 +169,16 @@ int mgpu_render_counted(const mgpu_scene *scene, const mgpu_render_params *param
                         void *stream);
 /* Per-kernel timing: when enabled, every render launch on this thread is bracketed by CUDA
  * events on its stream.  mgpu_profile_read (synchronises) returns milliseconds and launch
- * counts per kernel: generate, extend, shade, shadow, accumulate.  Enabling resets. */
+ * counts per kernel class: generate, extend, shade, shadow, accumulate, queue binning.
+ * Enabling resets. */
 int mgpu_profile_enable(int enable);
-int mgpu_profile_read(double *ms5, uint64_t *launches5);
+int mgpu_profile_read(double *ms6, uint64_t *launches6);
+/* Process-wide tuning knobs (results do not depend on them):
+ *   "persistent"     0/1  persistent warp-level traversal with per-lane ray refill (default 0)
+ *   "bin_shadow"     0/1  counting-sort shadow rays by (light, origin cell) (default 1)
+ *   "bin_extension"  0/1  counting-sort extension rays by (direction octant, origin cell) (default 1) */
+int mgpu_tune_set(const char *key, int64_t value);
+int mgpu_tune_get(const char *key, int64_t *value);
 
 /* Kernel launches issued by this library since load (for launch accounting). */
 uint64_t mgpu_launch_count(void);

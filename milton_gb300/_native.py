@@ -78,6 +78,8 @@ SIGNATURES = [
     ("mgpu_render_counted", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_profile_enable", C.c_int, [C.c_int]),
     ("mgpu_profile_read", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("mgpu_tune_set", C.c_int, [C.c_char_p, C.c_int64]),
+    ("mgpu_tune_get", C.c_int, [C.c_char_p, C.POINTER(C.c_int64)]),
     ("mgpu_launch_count", C.c_uint64, []),
     ("plugin_type", C.c_int, []),
     ("plugin_new", C.c_void_p, []),

@@ -183,52 +183,27 @@ MGPU_HD bool clip_root(const SceneView &s, const Ray &r, V3 inv, float &t0, floa
 constexpr float kCellEps = 1.0f / 262144.0f;  // relative widening of cell intervals (2^-18)
 
 // Resumable traversal state: one call of trav_step descends to the next leaf, tests it and
-// either finishes or moves on to the next cell.  The far-child stack is a short stack of
-// kShortStack entries held in registers (static indices only); when it overflows the oldest
-// entry is dropped, and when it runs empty before the ray has left the scene the descent
-// restarts from the root with the interval [end of the last cell, exit]
-// (kd-restart / short-stack traversal, Foley and Sugerman 2005, Horn et al. 2007).
-constexpr int kShortStack = 6;
+// either finishes or pops the next cell.  The scalar state stays in registers; the far-child
+// stack is a separate array (local memory, kMaxStack >= the deepest tree the builder emits).
 constexpr uint32_t kMaxLeafSteps = 1u << 20;  // guard: a ray that takes more leaf steps is abandoned
+
+struct TravEntry {
+  uint32_t w0, w1;
+  float tmax;
+};
 
 struct TravState {
   RayPre pre;
   V3 inv;
   float tmin, tmax;   // current cell interval
-  float texit;        // where the ray leaves the root box (clipped to its tmax)
   float ray_tmin;
   float best;         // closest accepted t so far (starts at the ray's tmax)
   int32_t best_prim;
   float bb1, bb2;
   uint32_t w0, w1;    // current node slot
   uint32_t steps;
-  bool restart;       // descending from the root after the short stack ran empty
-  int sp;             // live entries in the short stack
-  uint32_t s0[kShortStack], s1[kShortStack];
-  float st[kShortStack];
+  int sp;
 };
-
-MGPU_HD void stack_push(TravState &t, uint32_t w0, uint32_t w1, float tmax) {
-#if defined(__CUDA_ARCH__)
-#pragma unroll
-#endif
-  for (int i = kShortStack - 1; i > 0; --i) {
-    t.s0[i] = t.s0[i - 1]; t.s1[i] = t.s1[i - 1]; t.st[i] = t.st[i - 1];
-  }
-  t.s0[0] = w0; t.s1[0] = w1; t.st[0] = tmax;
-  if (t.sp < kShortStack) ++t.sp;
-}
-
-MGPU_HD void stack_pop(TravState &t, uint32_t &w0, uint32_t &w1, float &tmax) {
-  w0 = t.s0[0]; w1 = t.s1[0]; tmax = t.st[0];
-#if defined(__CUDA_ARCH__)
-#pragma unroll
-#endif
-  for (int i = 0; i < kShortStack - 1; ++i) {
-    t.s0[i] = t.s0[i + 1]; t.s1[i] = t.s1[i + 1]; t.st[i] = t.st[i + 1];
-  }
-  --t.sp;
-}
 
 // returns false when the ray misses the scene (no step needed)
 MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32_t ntop, TravState &st) {
@@ -242,12 +217,10 @@ MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32
   st.tmin = fmaxf(t0, r.tmin);
   st.tmax = fminf(t1, r.tmax);
   if (st.tmin > st.tmax) return false;
-  st.texit = st.tmax;
   st.ray_tmin = r.tmin;
   st.pre = precompute(r);
   st.sp = 0;
   st.steps = 0;
-  st.restart = false;
   Pair root = load_pair(s, top, ntop, 0);
   st.w0 = root.a0;
   st.w1 = root.a1;
@@ -256,12 +229,12 @@ MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32
 
 // One leaf: descend, test, then finish (true) or move to the next cell (false).
 template <bool ANY, bool COUNT>
-MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint32_t ntop, TraceCounts *cnt) {
+MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, const Pair *top, uint32_t ntop,
+                       TraceCounts *cnt) {
   const float o[3] = {st.pre.o.x, st.pre.o.y, st.pre.o.z};
   const float iv[3] = {st.inv.x, st.inv.y, st.inv.z};
   uint32_t w0 = st.w0, w1 = st.w1;
   float tmin = st.tmin, tmax = st.tmax;
-  const bool restart = st.restart;
   while ((w0 & 3u) != kLeafTag) {
     if (COUNT) cnt->nodes++;
     int ax = (int)(w0 & 3u);
@@ -269,42 +242,43 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint3
     float diff = split - o[ax];
     float dinv = iv[ax];
     Pair pr = load_pair(s, top, ntop, w0 >> 2);
+    uint32_t n0, n1;
+    bool both;
+    float dt = diff * dinv;
     if (isinf(dinv)) {
       // ray parallel to the split plane: only the side holding the origin (both if the ray
       // lies in the plane).  Milton's traversal evaluates 0 * inf here and, for a +0
       // direction component, descends into the wrong child.
-      if (diff > 0.0f) { w0 = pr.a0; w1 = pr.a1; }
-      else if (diff < 0.0f) { w0 = pr.b0; w1 = pr.b1; }
-      else {
-        stack_push(st, pr.b0, pr.b1, tmax);
-        if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
-        w0 = pr.a0; w1 = pr.a1;
-      }
-      continue;
-    }
-    float dt = diff * dinv;
-    // near child = the side of the origin (Milton's ordering by the signs of diff and d)
-    bool rev = diff <= 0.0f ? (dinv <= 0.0f) : (dinv < 0.0f);
-    uint32_t n0 = rev ? pr.b0 : pr.a0, n1 = rev ? pr.b1 : pr.a1;
-    uint32_t f0 = rev ? pr.a0 : pr.b0, f1 = rev ? pr.a1 : pr.b1;
-    float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
-    // after a restart the cells ending at tmin are finished: no widening on that side, so
-    // the descent cannot return to them
-    bool near_behind = restart ? (dt <= tmin) : (dt < tmin - slack);
-    if (dt > tmax + slack) {
-      w0 = n0; w1 = n1;               // far child not reached inside this cell
-    } else if (near_behind) {
-      w0 = f0; w1 = f1;               // near child lies behind the cell
+      both = diff == 0.0f;
+      bool right = diff < 0.0f;
+      n0 = right ? pr.b0 : pr.a0; n1 = right ? pr.b1 : pr.a1;
+      dt = tmax;
     } else {
-      // the ray crosses the plane inside the cell: near child first, far child on the stack
-      stack_push(st, f0, f1, tmax);
-      if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
-      w0 = n0; w1 = n1;
+      // near child = the side of the origin (Milton's ordering by the signs of diff and d)
+      bool rev = diff <= 0.0f ? (dinv <= 0.0f) : (dinv < 0.0f);
+      float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
+      if (dt > tmax + slack) {          // far child not reached inside this cell
+        n0 = rev ? pr.b0 : pr.a0; n1 = rev ? pr.b1 : pr.a1; both = false;
+      } else if (dt < tmin - slack) {   // near child lies behind the cell
+        n0 = rev ? pr.a0 : pr.b0; n1 = rev ? pr.a1 : pr.b1; both = false;
+      } else {
+        n0 = rev ? pr.b0 : pr.a0; n1 = rev ? pr.b1 : pr.a1; both = true;
+      }
+    }
+    if (both) {
+      // near child first, far child on the stack
+      if (st.sp < kMaxStack) {
+        uint32_t f0 = (n0 == pr.a0 && n1 == pr.a1) ? pr.b0 : pr.a0;
+        uint32_t f1 = (n0 == pr.a0 && n1 == pr.a1) ? pr.b1 : pr.a1;
+        stack[st.sp].w0 = f0; stack[st.sp].w1 = f1; stack[st.sp].tmax = tmax;
+        ++st.sp;
+        if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
+      }
       tmax = fminf(tmax, dt);
     }
+    w0 = n0; w1 = n1;
   }
   if (COUNT) cnt->nodes++;
-  st.restart = false;
   const uint32_t count = w0 >> 2;
   for (uint32_t i = 0; i < count; ++i) {
     uint32_t tri = (count == 1) ? w1 : load_u32(s.refs, (uint64_t)w1 + i);
@@ -322,18 +296,10 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint3
   }
   // early exit: the best hit lies inside this cell, later cells are farther
   if (!ANY && st.best_prim >= 0 && st.best <= tmax + kCellEps * fabsf(tmax)) return true;
-  if (++st.steps >= kMaxLeafSteps) return true;
+  if (st.sp == 0 || ++st.steps >= kMaxLeafSteps) return true;
+  --st.sp;
   st.tmin = tmax;
-  if (st.sp > 0) {
-    stack_pop(st, st.w0, st.w1, st.tmax);
-  } else {
-    // short stack empty: done if the ray has left the scene, else restart from the root
-    if (!(tmax < st.texit)) return true;
-    Pair root = load_pair(s, top, ntop, 0);
-    st.w0 = root.a0; st.w1 = root.a1;
-    st.tmax = st.texit;
-    st.restart = true;
-  }
+  st.w0 = stack[st.sp].w0; st.w1 = stack[st.sp].w1; st.tmax = stack[st.sp].tmax;
   if (!ANY && st.best_prim >= 0 && st.best < st.tmin) return true;
   return false;
 }
@@ -342,9 +308,10 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, const Pair *top, uint3
 template <bool ANY, bool COUNT>
 MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *top, uint32_t ntop, TraceCounts *cnt) {
   TravState st;
+  TravEntry stack[kMaxStack];
   hit.t = INFINITY; hit.prim = -1; hit.b1 = 0.0f; hit.b2 = 0.0f;
   if (!trav_init(s, r, top, ntop, st)) return false;
-  while (!trav_step<ANY, COUNT>(s, st, top, ntop, cnt)) {
+  while (!trav_step<ANY, COUNT>(s, st, stack, top, ntop, cnt)) {
   }
   if (st.best_prim < 0) return false;
   hit.t = st.best; hit.prim = st.best_prim; hit.b1 = st.bb1; hit.b2 = st.bb2;
@@ -352,6 +319,26 @@ MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *to
 }
 
 #if defined(__CUDACC__)
+// Grid-stride traversal: every thread traces rays i, i + stride, ... to completion.
+template <bool ANY, bool COUNT, class Load, class Store>
+__device__ __forceinline__ void grid_trace(const SceneView &s, const Pair *top, uint32_t ntop, uint32_t n, Load load,
+                                           Store store, TraceCounts *cnt, uint32_t &rays_done) {
+  TravState st;
+  TravEntry stack[kMaxStack];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    Ray r;
+    load(i, r);
+    ++rays_done;
+    if (!trav_init(s, r, top, ntop, st)) {
+      store(i, false, st);
+      continue;
+    }
+    while (!trav_step<ANY, COUNT>(s, st, stack, top, ntop, cnt)) {
+    }
+    store(i, st.best_prim >= 0, st);
+  }
+}
+
 // Persistent warp-level traversal (Aila and Laine, "Understanding the Efficiency of Ray
 // Traversal on GPUs", HPG 2009): every lane owns one ray; after each leaf step, lanes whose
 // ray finished take new rays from a global counter with one warp-aggregated atomicAdd, so a
@@ -365,6 +352,7 @@ __device__ __forceinline__ void persistent_trace(const SceneView &s, const Pair 
   const unsigned kFull = 0xFFFFFFFFu;
   const int lane = threadIdx.x & 31;
   TravState st;
+  TravEntry stack[kMaxStack];
   uint32_t idx = 0;
   bool have = false, exhausted = false;
   for (;;) {
@@ -390,7 +378,7 @@ __device__ __forceinline__ void persistent_trace(const SceneView &s, const Pair 
       }
     }
     if (__all_sync(kFull, exhausted && !have)) break;
-    if (have && trav_step<ANY, COUNT>(s, st, top, ntop, cnt)) {
+    if (have && trav_step<ANY, COUNT>(s, st, stack, top, ntop, cnt)) {
       store(idx, st.best_prim >= 0, st);
       have = false;
     }

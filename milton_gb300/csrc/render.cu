@@ -52,6 +52,11 @@ struct RenderArgs {
   float4 *qo[2], *qd[2], *qt[2];
   float4 *qhit;
   float4 *so, *sd;       // shadow ray queue: origin + slot index, direction + tmax
+  float4 *qo_u, *qd_u, *qt_u;  // unsorted next-ray queue (binning on)
+  float4 *so_u, *sd_u;         // unsorted shadow queue (binning on)
+  uint32_t *qkey, *skey;       // bin keys of the unsorted queues
+  int32_t bin_ext, bin_sh;     // counting-sort the queues by (direction octant | light, origin cell)
+  int32_t sh_cell_bits;        // Morton bits of the origin cell in the shadow key
   float4 *slots;         // nl_slots per path: direct-light contribution per light sample
   int32_t nl_slots;      // nlight * nds_side^2
   uint32_t *counters;
@@ -119,6 +124,40 @@ __device__ __forceinline__ const Pair *top_ptr(const RenderArgs &a) {
   return a.ntop ? reinterpret_cast<const Pair *>(smem_top) : nullptr;
 }
 
+// Binning keys (kBins = 4096).  Ray coherence: rays of one warp should start close together
+// and head the same way, so that they visit the same nodes.  Keys combine the direction
+// octant (extension rays) or the light index (shadow rays) with the Morton code of the
+// origin's cell in a 16x16x16 grid over the scene bounds.
+constexpr int kBins = 4096;
+
+__device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> every third bit
+  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+
+__device__ __forceinline__ uint32_t morton12(const RenderArgs &a, V3 p) {
+  const float *lo = a.view.bmin, *hi = a.view.bmax;
+  uint32_t c[3];
+  const float pp[3] = {p.x, p.y, p.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float ext = hi[k] - lo[k];
+    float f = ext > 0.0f ? (pp[k] - lo[k]) / ext : 0.0f;
+    int q = (int)(f * 16.0f);
+    c[k] = (uint32_t)min(max(q, 0), 15);
+  }
+  return (spread4(c[0]) << 2) | (spread4(c[1]) << 1) | spread4(c[2]);
+}
+
+__device__ __forceinline__ uint32_t ext_key(const RenderArgs &a, V3 o, V3 d) {
+  uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+  return (oct << 9) | (morton12(a, o) >> 3);
+}
+
+__device__ __forceinline__ uint32_t sh_key(const RenderArgs &a, int light, V3 o) {
+  uint32_t cell = morton12(a, o) >> (12 - a.sh_cell_bits);
+  return (((uint32_t)light << a.sh_cell_bits) | cell) & (kBins - 1);
+}
+
 // ---------------------------------------------------------------------------------------
 // generate: camera rays for every path of the wave (RayTracer::sample, RayTracer.cpp:19-30;
 // SuperSampleGenerator strata, SuperSampleGenerator.cpp:60-90)
@@ -160,7 +199,7 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
 }
 
 // extend: closest hit for the live queue of bounce b
-template <bool COUNT>
+template <bool COUNT, bool PERSIST>
 __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
   load_top(a);
   const Pair *top = top_ptr(a);
@@ -180,7 +219,10 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
     qhit[i] = make_float4(hit ? st.best : INFINITY, __int_as_float(hit ? st.best_prim : -1), hit ? st.bb1 : 0.0f,
                           hit ? st.bb2 : 0.0f);
   };
-  persistent_trace<false, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
+  if (PERSIST)
+    persistent_trace<false, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
+  else
+    grid_trace<false, COUNT>(a.view, top, a.ntop, n, load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[0], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[1], (unsigned long long)c.refs);
@@ -287,9 +329,16 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
     }
     uint32_t q = warp_append(&a.counters[kCtrRay + b + 1], want_next);
     if (want_next) {
-      a.qo[nxt][q] = no_o;
-      a.qd[nxt][q] = no_d;
-      a.qt[nxt][q] = no_t;
+      if (a.bin_ext) {
+        a.qo_u[q] = no_o;
+        a.qd_u[q] = no_d;
+        a.qt_u[q] = no_t;
+        a.qkey[q] = ext_key(a, v3(no_o.x, no_o.y, no_o.z), v3(no_d.x, no_d.y, no_d.z));
+      } else {
+        a.qo[nxt][q] = no_o;
+        a.qd[nxt][q] = no_d;
+        a.qt[nxt][q] = no_t;
+      }
     }
     // light samples: every lane of the warp runs the same k loop (uniform trip count), so the
     // warp-aggregated append stays converged
@@ -327,15 +376,21 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
       }
       uint32_t e = warp_append(&a.counters[kCtrNee + b], want);
       if (want) {
-        a.so[e] = so4;
-        a.sd[e] = sd4;
+        if (a.bin_sh) {
+          a.so_u[e] = so4;
+          a.sd_u[e] = sd4;
+          a.skey[e] = sh_key(a, k / s2n, P);
+        } else {
+          a.so[e] = so4;
+          a.sd[e] = sd4;
+        }
       }
     }
   }
 }
 
 // shadow: any-hit query per queued light sample; an occluded sample's slot is zeroed
-template <bool COUNT>
+template <bool COUNT, bool PERSIST>
 __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
   load_top(a);
   const Pair *top = top_ptr(a);
@@ -354,12 +409,91 @@ __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
   auto store = [&](uint32_t i, bool hit, const TravState &) {
     if (hit) slots[__float_as_uint(so[i].w)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   };
-  persistent_trace<true, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
+  if (PERSIST)
+    persistent_trace<true, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
+  else
+    grid_trace<true, COUNT>(a.view, top, a.ntop, n, load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[4], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[5], (unsigned long long)c.refs);
     atomicAdd(&a.tcount[6], (unsigned long long)c.tris);
     atomicAdd(&a.tcount[7], (unsigned long long)rays);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// counting sort of a queue by key: histogram -> exclusive scan -> scatter with per-block
+// range reservations (one global atomic per block chunk and non-empty bin)
+__global__ void __launch_bounds__(256) k_bin_hist(const uint32_t *__restrict__ keys, const uint32_t *count,
+                                                 uint32_t *__restrict__ hist) {
+  __shared__ uint32_t h[kBins];
+  for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const uint32_t n = *count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(&h[keys[i] & (kBins - 1)], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kBins; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// single block of 1024 threads: hist -> cursor (exclusive prefix sum)
+__global__ void __launch_bounds__(1024) k_bin_scan(const uint32_t *__restrict__ hist, uint32_t *__restrict__ cursor) {
+  __shared__ uint32_t part[1024];
+  const int per = kBins / 1024;
+  uint32_t loc[kBins / 1024];
+  uint32_t sum = 0;
+  for (int k = 0; k < per; ++k) {
+    loc[k] = sum;
+    sum += hist[threadIdx.x * per + k];
+  }
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t base = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+  for (int k = 0; k < per; ++k) cursor[threadIdx.x * per + k] = base + loc[k];
+}
+
+template <int NF4>
+__global__ void __launch_bounds__(256) k_bin_scatter(const uint32_t *__restrict__ keys, const uint32_t *count,
+                                                    uint32_t *__restrict__ cursor, const float4 *__restrict__ in0,
+                                                    const float4 *__restrict__ in1, const float4 *__restrict__ in2,
+                                                    float4 *__restrict__ out0, float4 *__restrict__ out1,
+                                                    float4 *__restrict__ out2) {
+  constexpr int kPer = 16;                 // entries per thread per chunk
+  constexpr int kChunk = 256 * kPer;
+  __shared__ uint32_t h[kBins];
+  const uint32_t n = *count;
+  for (uint32_t c0 = blockIdx.x * kChunk; c0 < n; c0 += gridDim.x * kChunk) {
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    uint32_t key[kPer], rank[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      uint32_t i = c0 + k * 256 + threadIdx.x;
+      key[k] = i < n ? (keys[i] & (kBins - 1)) : 0u;
+      rank[k] = i < n ? atomicAdd(&h[key[k]], 1u) : 0u;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x)
+      if (h[i]) h[i] = atomicAdd(&cursor[i], h[i]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      uint32_t i = c0 + k * 256 + threadIdx.x;
+      if (i < n) {
+        uint32_t pos = h[key[k]] + rank[k];
+        out0[pos] = in0[i];
+        if (NF4 > 1) out1[pos] = in1[i];
+        if (NF4 > 2) out2[pos] = in2[i];
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -415,6 +549,8 @@ struct Workspace {
   void *block = nullptr;
   float4 *path_L = nullptr, *qo[2] = {}, *qd[2] = {}, *qt[2] = {}, *qhit = nullptr;
   float4 *so = nullptr, *sd = nullptr, *slots = nullptr;
+  float4 *qo_u = nullptr, *qd_u = nullptr, *qt_u = nullptr, *so_u = nullptr, *sd_u = nullptr;
+  uint32_t *qkey = nullptr, *skey = nullptr, *hist = nullptr, *cursor = nullptr;  // hist/cursor: kBins each
   int64_t slot_cap = 0;  // light-sample slots
   uint32_t *counters = nullptr;
   unsigned long long *stats = nullptr;   // 4
@@ -426,21 +562,29 @@ struct Workspace {
   }
 };
 
+// process-wide tuning knobs (mgpu_tune_set)
+struct Tuning {
+  std::atomic<int> persistent{0};     // persistent warp-level traversal with ray refill
+  std::atomic<int> bin_shadow{1};     // counting-sort shadow rays by (light, origin cell)
+  std::atomic<int> bin_extension{1};  // counting-sort extension rays by (octant, origin cell)
+};
+static Tuning g_tune;
+
 static thread_local Workspace *t_ws = nullptr;
 static thread_local mgpu_render_stats t_stats{};
 static thread_local cudaStream_t t_stats_stream = nullptr;
 static thread_local bool t_stats_pending = false;
 
 // Per-kernel timing with CUDA events recorded on the launching stream around every launch.
-enum { kProfGenerate = 0, kProfExtend, kProfShade, kProfShadow, kProfAccumulate, kProfClasses };
+enum { kProfGenerate = 0, kProfExtend, kProfShade, kProfShadow, kProfAccumulate, kProfBin, kProfClasses };
 struct Profiler {
   bool enabled = false;
   std::vector<cudaEvent_t> pool;
   size_t used = 0;
   std::vector<std::pair<int, size_t>> marks;  // (class, index of begin event); end = begin + 1
   cudaStream_t stream = nullptr;
-  double ms[kProfClasses] = {0, 0, 0, 0, 0};
-  uint64_t launches[kProfClasses] = {0, 0, 0, 0, 0};
+  double ms[kProfClasses] = {0, 0, 0, 0, 0, 0};
+  uint64_t launches[kProfClasses] = {0, 0, 0, 0, 0, 0};
   cudaEvent_t next() {
     if (used == pool.size()) {
       cudaEvent_t e;
@@ -491,9 +635,11 @@ static int ensure_workspace(int64_t paths, int64_t slots) {
   w->device = dev;
   w->cap = paths;
   w->slot_cap = slots;
-  size_t per = (size_t)paths * sizeof(float4);
-  size_t total = per * 8 + (size_t)slots * 3 * sizeof(float4) + 12 * sizeof(unsigned long long) +
-                 kNumCounters * sizeof(uint32_t) + 256;
+  // float4 arrays: path_L, 2 x (qo, qd, qt), qhit, unsorted (qo, qd, qt) = 11 per path;
+  // so, sd, slots, unsorted (so, sd) = 5 per light sample
+  size_t f4 = (size_t)paths * 11 + (size_t)slots * 5;
+  size_t u32 = (size_t)paths + (size_t)slots + 2 * kBins + kNumCounters;
+  size_t total = f4 * sizeof(float4) + 12 * sizeof(unsigned long long) + u32 * sizeof(uint32_t) + 1024;
   cudaError_t e = cudaMalloc(&w->block, total);
   if (e != cudaSuccess) {
     delete w;
@@ -503,10 +649,17 @@ static int ensure_workspace(int64_t paths, int64_t slots) {
   w->path_L = f; f += paths;
   for (int k = 0; k < 2; ++k) { w->qo[k] = f; f += paths; w->qd[k] = f; f += paths; w->qt[k] = f; f += paths; }
   w->qhit = f; f += paths;
+  w->qo_u = f; f += paths; w->qd_u = f; f += paths; w->qt_u = f; f += paths;
   w->so = f; f += slots; w->sd = f; f += slots; w->slots = f; f += slots;
+  w->so_u = f; f += slots; w->sd_u = f; f += slots;
   w->stats = (unsigned long long *)f;
   w->tcount = w->stats + 4;
-  w->counters = (uint32_t *)(w->tcount + 8);
+  uint32_t *u = (uint32_t *)(w->tcount + 8);
+  w->qkey = u; u += paths;
+  w->skey = u; u += slots;
+  w->hist = u; u += kBins;
+  w->cursor = u; u += kBins;
+  w->counters = u;
   e = cudaMallocHost(&w->h_counters, 64);
   if (e != cudaSuccess) {
     delete w;
@@ -600,12 +753,24 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   for (int k = 0; k < 2; ++k) { a.qo[k] = w->qo[k]; a.qd[k] = w->qd[k]; a.qt[k] = w->qt[k]; }
   a.qhit = w->qhit;
   a.so = w->so; a.sd = w->sd; a.slots = w->slots;
+  a.qo_u = w->qo_u; a.qd_u = w->qd_u; a.qt_u = w->qt_u; a.so_u = w->so_u; a.sd_u = w->sd_u;
+  a.qkey = w->qkey; a.skey = w->skey;
+  a.bin_ext = g_tune.bin_extension.load();
+  a.bin_sh = g_tune.bin_shadow.load();
+  {
+    int nlp = 1;
+    while (nlp < std::min(sc->nlight, 16)) nlp <<= 1;
+    int lb = 0;
+    while ((1 << lb) < nlp) ++lb;
+    a.sh_cell_bits = 12 - lb;  // light index in the top bits, origin cell below
+  }
   a.counters = w->counters;
   a.stats = w->stats;
   a.tcount = w->tcount;
 
-  auto kext = k_extend<COUNT>;
-  auto kshw = k_shadow<COUNT>;
+  const bool persist = g_tune.persistent.load() != 0;
+  auto kext = persist ? k_extend<COUNT, true> : k_extend<COUNT, false>;
+  auto kshw = persist ? k_shadow<COUNT, true> : k_shadow<COUNT, false>;
   size_t smem = (size_t)a.ntop * sizeof(uint4);
   if (smem > 48 * 1024) {
     MGPU_CUDA(cudaFuncSetAttribute(kext, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -616,6 +781,7 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   const int g_sha = grid_for((const void *)k_shade, 0);
   const int g_shw = grid_for((const void *)kshw, smem);
   const int g_acc = grid_for((const void *)k_accumulate, 0);
+  const int g_bin = device_sm_count() * 4;
 
   mgpu_render_stats stats{};
   uint64_t launches = 0;
@@ -646,6 +812,27 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
           m = pf.begin(kProfShade, st);
           k_shade<<<g_sha, kBlock, 0, st>>>(a, b);
           pf.end(m, st);
+          if (a.bin_sh || a.bin_ext) {
+            m = pf.begin(kProfBin, st);
+            if (a.bin_sh) {
+              MGPU_CUDA(cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st));
+              k_bin_hist<<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->hist);
+              k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
+              k_bin_scatter<2><<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->cursor, w->so_u, w->sd_u,
+                                                      nullptr, w->so, w->sd, nullptr);
+              launches += 3;
+            }
+            if (a.bin_ext && b + 1 < max_b) {
+              const int nx = (b + 1) & 1;
+              MGPU_CUDA(cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st));
+              k_bin_hist<<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->hist);
+              k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
+              k_bin_scatter<3><<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->cursor, w->qo_u,
+                                                      w->qd_u, w->qt_u, w->qo[nx], w->qd[nx], w->qt[nx]);
+              launches += 3;
+            }
+            pf.end(m, st);
+          }
           m = pf.begin(kProfShadow, st);
           kshw<<<g_shw, kBlock, smem, st>>>(a, b);
           pf.end(m, st);
@@ -723,12 +910,32 @@ int mgpu_profile_enable(int enable) {
   return MGPU_OK;
 }
 
-int mgpu_profile_read(double *ms5, uint64_t *launches5) {
-  if (!ms5 || !launches5) return fail(MGPU_E_INVALID, "mgpu_profile_read: null argument");
+int mgpu_profile_read(double *ms6, uint64_t *launches6) {
+  if (!ms6 || !launches6) return fail(MGPU_E_INVALID, "mgpu_profile_read: null argument");
   Profiler &p = t_prof;
   int rc = p.flush();
   if (rc != MGPU_OK) return rc;
-  for (int k = 0; k < kProfClasses; ++k) { ms5[k] = p.ms[k]; launches5[k] = p.launches[k]; }
+  for (int k = 0; k < kProfClasses; ++k) { ms6[k] = p.ms[k]; launches6[k] = p.launches[k]; }
+  return MGPU_OK;
+}
+
+int mgpu_tune_set(const char *key, int64_t value) {
+  if (!key) return fail(MGPU_E_INVALID, "mgpu_tune_set: null key");
+  std::string k(key);
+  if (k == "persistent") g_tune.persistent.store(value != 0);
+  else if (k == "bin_shadow") g_tune.bin_shadow.store(value != 0);
+  else if (k == "bin_extension") g_tune.bin_extension.store(value != 0);
+  else return fail(MGPU_E_INVALID, "mgpu_tune_set: unknown key " + k);
+  return MGPU_OK;
+}
+
+int mgpu_tune_get(const char *key, int64_t *value) {
+  if (!key || !value) return fail(MGPU_E_INVALID, "mgpu_tune_get: null argument");
+  std::string k(key);
+  if (k == "persistent") *value = g_tune.persistent.load();
+  else if (k == "bin_shadow") *value = g_tune.bin_shadow.load();
+  else if (k == "bin_extension") *value = g_tune.bin_extension.load();
+  else return fail(MGPU_E_INVALID, "mgpu_tune_get: unknown key " + k);
   return MGPU_OK;
 }
 

@@ -218,16 +218,27 @@ def render_counted(dscene: DeviceScene, settings: RenderSettings, film: Film, st
     return {k: int(v) for k, v in zip(keys, out)}
 
 
-KERNELS = ("generate", "extend", "shade", "shadow", "accumulate")
+KERNELS = ("generate", "extend", "shade", "shadow", "accumulate", "binning")
 
 
 def profile_enable(enable: bool = True) -> None:
     N.check(N.load().mgpu_profile_enable(1 if enable else 0))
 
 
+def tune(key: str, value: int) -> None:
+    """Process-wide tuning knob (persistent, bin_shadow, bin_extension); results are unchanged."""
+    N.check(N.load().mgpu_tune_set(key.encode(), int(value)))
+
+
+def tune_get(key: str) -> int:
+    v = C.c_int64()
+    N.check(N.load().mgpu_tune_get(key.encode(), C.byref(v)))
+    return int(v.value)
+
+
 def profile_read() -> dict:
-    ms = np.zeros(5, np.float64)
-    n = np.zeros(5, np.uint64)
+    ms = np.zeros(6, np.float64)
+    n = np.zeros(6, np.uint64)
     N.check(N.load().mgpu_profile_read(N.ptr(ms), N.ptr(n)))
     return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(KERNELS)}
 

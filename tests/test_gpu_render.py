@@ -97,6 +97,30 @@ def test_film_determinism_and_pass_splits(cuda):
     assert stats["paths"] == W * H * 16 and stats["extension_rays"] >= W * H * 16
 
 
+def test_tuning_knobs_do_not_change_the_image(cuda):
+    # queue binning and persistent traversal reorder work, never the result
+    s = scenegen.random_scene(12, 20000)
+    acc = pt.Accel(s)
+    ds = pt.DeviceScene(s, acc)
+    st = pt.RenderSettings(48, 40, 8, max_depth=6, rr_start_depth=3, seed=4)
+    raws = []
+    saved = {k: pt.tune_get(k) for k in ("persistent", "bin_shadow", "bin_extension")}
+    try:
+        for persist in (0, 1):
+            for bins in ((0, 0), (1, 0), (1, 1)):
+                pt.tune("persistent", persist)
+                pt.tune("bin_shadow", bins[0])
+                pt.tune("bin_extension", bins[1])
+                f = pt.Film(48, 40)
+                pt.render(ds, st, f)
+                raws.append(f.raw())
+    finally:
+        for k, v in saved.items():
+            pt.tune(k, v)
+    for r in raws[1:]:
+        assert np.array_equal(raws[0], r)
+
+
 def test_renderer_plugin_object(cuda):
     from milton_gb300.plugin import load_dynamic_renderer
     from milton_gb300._native import LIB_PATH
