@@ -35,6 +35,13 @@
  *   constants              M/common/arch.h:120-137 (EPSILON 1e-7, double), M/common/utilities.h:240 (EQ),
  *                          M/materials/IndexOfRefraction.cpp:16 (AIR = 1.0003)
  *
+ * Parity unpinned against the reference itself: Milton ships no golden vectors or known-answer
+ * tests for this path, and its sources need Boost, Qt 4 and OpenGL headers (external libraries)
+ * to compile, so no reference build exists to compare with.  This restatement is pinned instead by
+ * the Random123 Philox known answers, brute-force ray queries, an analytic direct-lighting known
+ * answer and BSDF property checks (tests/test_oracle.py), and its kd builder agrees node by node
+ * with the product's.
+ *
  * Random numbers.  The reference draws from one global boost::mt19937 (M/stats/Random.cpp:22-56),
  * which is not reproducible across threads.  The oracle and the GPU path instead draw every
  * uniform from Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
