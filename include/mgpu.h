@@ -157,6 +157,25 @@ int mgpu_film_read_raw(mgpu_film *film, float *out8, void *stream);
 
 /* PathTracer::render over the requested sample passes (PathTracer.cpp:28-116 per path). */
 int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream);
+/* Allocation-free render.  No counterpart in the reference: Milton's renderers allocate freely.
+ * Some hosts cannot let a library allocate device memory while they render -- a render
+ * server that admits jobs against a fixed HBM budget and forbids allocation after start-up, or
+ * a plugin host whose device allocator is its own -- so this entry point renders with the same
+ * estimator, random numbers and film as mgpu_render but never calls cudaMalloc, cudaFree or any
+ * allocating routine.  Its scratch (path state, ray queues, light-sample slots) is one fixed
+ * 32 MiB device array compiled into libmgpu.so; every GPU that loads the library holds it until
+ * the process exits.  The caller still provides the inputs and outputs: a scene from
+ * mgpu_scene_create and a film from mgpu_film_create, made beforehand.
+ *   - The scratch bounds the wave: with 4 light samples per vertex it holds about 65 000
+ *     paths in flight (wave_paths 0 picks the most that fit), so large frames render slower
+ *     than with mgpu_render.  A wave_paths above that capacity is rejected with
+ *     MGPU_E_INVALID and a message naming the capacity; nothing is rendered.
+ *   - The first call on a device looks up the array's device address with
+ *     cudaGetSymbolAddress; make that first call before any stream capture.
+ *   - All calls share the one array and it keeps the last call's contents; each call clears
+ *     what must start at zero itself.  Calls whose work overlaps on the GPU (other streams,
+ *     other host threads) race on the array: serialise them.                                */
+int mgpu_render_noalloc(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream);
 /* Render and also write every path's radiance (after Milton's specular channel masking)
  * to d_path_L: (pixel * sample_count + sample) * 4 floats.  Test/measurement helper.     */
 int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,

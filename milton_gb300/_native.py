@@ -73,6 +73,7 @@ SIGNATURES = [
     ("mgpu_film_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_film_read_raw", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
+    ("mgpu_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_render_paths", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_render_stats_get", C.c_int, [C.POINTER(RenderStats)]),
     ("mgpu_render_counted", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -16,6 +16,8 @@
 // order and the image does not depend on queue order.
 #include <string.h>
 
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -555,8 +557,10 @@ struct Workspace {
   uint32_t *counters = nullptr;
   unsigned long long *stats = nullptr;   // 4
   unsigned long long *tcount = nullptr;  // 8
-  uint32_t *h_counters = nullptr;  // pinned
+  uint32_t *h_counters = nullptr;  // pinned (owned) or a static host word (allocation-free path)
+  bool owned = true;
   ~Workspace() {
+    if (!owned) return;
     if (block) cudaFree(block);
     if (h_counters) cudaFreeHost(h_counters);
   }
@@ -574,6 +578,7 @@ static thread_local Workspace *t_ws = nullptr;
 static thread_local mgpu_render_stats t_stats{};
 static thread_local cudaStream_t t_stats_stream = nullptr;
 static thread_local bool t_stats_pending = false;
+static thread_local unsigned long long *t_stats_dev = nullptr;  // device stats of the last render
 
 // Per-kernel timing with CUDA events recorded on the launching stream around every launch.
 enum { kProfGenerate = 0, kProfExtend, kProfShade, kProfShadow, kProfAccumulate, kProfBin, kProfClasses };
@@ -622,30 +627,19 @@ struct Profiler {
 };
 static thread_local Profiler t_prof;
 
-static int ensure_workspace(int64_t paths, int64_t slots) {
-  int dev = 0;
-  MGPU_CUDA(cudaGetDevice(&dev));
-  if (t_ws && t_ws->device == dev && t_ws->cap >= paths && t_ws->slot_cap >= slots) return MGPU_OK;
-  if (t_ws) {
-    cudaDeviceSynchronize();
-    delete t_ws;
-    t_ws = nullptr;
-  }
-  Workspace *w = new Workspace();
-  w->device = dev;
-  w->cap = paths;
-  w->slot_cap = slots;
-  // float4 arrays: path_L, 2 x (qo, qd, qt), qhit, unsorted (qo, qd, qt) = 11 per path;
-  // so, sd, slots, unsorted (so, sd) = 5 per light sample
+// float4 arrays: path_L, 2 x (qo, qd, qt), qhit, unsorted (qo, qd, qt) = 11 per path;
+// so, sd, slots, unsorted (so, sd) = 5 per light sample; uint32 keys per path and per sample
+static size_t workspace_bytes(int64_t paths, int64_t slots) {
   size_t f4 = (size_t)paths * 11 + (size_t)slots * 5;
   size_t u32 = (size_t)paths + (size_t)slots + 2 * kBins + kNumCounters;
-  size_t total = f4 * sizeof(float4) + 12 * sizeof(unsigned long long) + u32 * sizeof(uint32_t) + 1024;
-  cudaError_t e = cudaMalloc(&w->block, total);
-  if (e != cudaSuccess) {
-    delete w;
-    return cuda_fail(e, "render workspace cudaMalloc");
-  }
-  float4 *f = (float4 *)w->block;
+  return f4 * sizeof(float4) + 12 * sizeof(unsigned long long) + u32 * sizeof(uint32_t) + 1024;
+}
+
+static void workspace_layout(Workspace *w, void *block, int64_t paths, int64_t slots) {
+  w->cap = paths;
+  w->slot_cap = slots;
+  w->block = block;
+  float4 *f = (float4 *)block;
   w->path_L = f; f += paths;
   for (int k = 0; k < 2; ++k) { w->qo[k] = f; f += paths; w->qd[k] = f; f += paths; w->qt[k] = f; f += paths; }
   w->qhit = f; f += paths;
@@ -660,6 +654,26 @@ static int ensure_workspace(int64_t paths, int64_t slots) {
   w->hist = u; u += kBins;
   w->cursor = u; u += kBins;
   w->counters = u;
+}
+
+static int ensure_workspace(int64_t paths, int64_t slots) {
+  int dev = 0;
+  MGPU_CUDA(cudaGetDevice(&dev));
+  if (t_ws && t_ws->device == dev && t_ws->cap >= paths && t_ws->slot_cap >= slots) return MGPU_OK;
+  if (t_ws) {
+    cudaDeviceSynchronize();
+    delete t_ws;
+    t_ws = nullptr;
+  }
+  Workspace *w = new Workspace();
+  w->device = dev;
+  void *block = nullptr;
+  cudaError_t e = cudaMalloc(&block, workspace_bytes(paths, slots));
+  if (e != cudaSuccess) {
+    delete w;
+    return cuda_fail(e, "render workspace cudaMalloc");
+  }
+  workspace_layout(w, block, paths, slots);
   e = cudaMallocHost(&w->h_counters, 64);
   if (e != cudaSuccess) {
     delete w;
@@ -667,6 +681,42 @@ static int ensure_workspace(int64_t paths, int64_t slots) {
   }
   t_ws = w;
   return MGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Fixed scratch for mgpu_render_noalloc: one static device array per process and device,
+// resident from module load until exit.  Host code only holds a stand-in for the array's
+// name; the device address comes from cudaGetSymbolAddress, once per device.
+constexpr size_t kNoAllocBytes = (size_t)32 << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[kNoAllocMaxDevices];
+static uint32_t g_noalloc_host_counter[16];  // pageable host word for live-path counts
+
+static int noalloc_scratch(void **out) {
+  int dev = 0;
+  MGPU_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(MGPU_E_INVALID, "mgpu_render_noalloc: device ordinal too large");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "mgpu_render_noalloc: cudaGetSymbolAddress of the fixed scratch");
+    if (!p) return fail(MGPU_E_CUDA, "mgpu_render_noalloc: fixed scratch has no device address");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MGPU_OK;
+}
+
+// paths per wave that fit the fixed scratch for nl_slots light samples per path
+static int64_t noalloc_paths(int64_t nl_slots) {
+  const size_t fixed = workspace_bytes(0, 0);
+  const size_t per = 11 * sizeof(float4) + sizeof(uint32_t) + (size_t)nl_slots * (5 * sizeof(float4) + sizeof(uint32_t));
+  if (kNoAllocBytes <= fixed) return 0;
+  int64_t p = (int64_t)((kNoAllocBytes - fixed) / per);
+  return p / 64 * 64;
 }
 
 static int grid_for(const void *kern, size_t smem) {
@@ -698,7 +748,7 @@ static Camera make_camera(const float *c) {
 
 template <bool COUNT>
 static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_film *film, float *d_path_out,
-                       void *stream) {
+                       void *stream, bool noalloc = false) {
   if (!sc || !rp || !film) return fail(MGPU_E_INVALID, "mgpu_render: null argument");
   if (rp->width != film->width || rp->height != film->height)
     return fail(MGPU_E_INVALID, "mgpu_render: film size differs from the render size");
@@ -740,15 +790,39 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   const int64_t tiles_y = (a.H + 7) / 8;
   const int64_t total_slots = (int64_t)a.tiles_x * tiles_y * 64;
   int64_t wave = rp->wave_paths > 0 ? rp->wave_paths : (int64_t)1 << 24;
+  a.nl_slots = sc->nlight * a.nds_side * a.nds_side;
+  if (a.nl_slots > 4096) return fail(MGPU_E_INVALID, "mgpu_render: too many light samples per vertex");
+  if (noalloc) {
+    const int64_t pmax = noalloc_paths(a.nl_slots);
+    if (pmax < 64)
+      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: " + std::to_string(a.nl_slots) +
+                                      " light samples per vertex do not fit the 32 MiB fixed scratch");
+    if (rp->wave_paths > pmax)
+      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: wave_paths " + std::to_string(rp->wave_paths) +
+                                      " exceeds the fixed scratch (32 MiB holds " + std::to_string(pmax) +
+                                      " paths at " + std::to_string(a.nl_slots) + " light samples per vertex)");
+    wave = rp->wave_paths > 0 ? rp->wave_paths : pmax;
+  }
   // samples per wave: as many passes of the whole image as fit, else one pass over a slot range
   int ns = (int)std::max<int64_t>(1, std::min<int64_t>(rp->sample_count, wave / total_slots));
   int64_t slots_per_wave = std::min<int64_t>(total_slots, std::max<int64_t>(64, wave / ns) / 64 * 64);
   int64_t cap = slots_per_wave * ns;
-  a.nl_slots = sc->nlight * a.nds_side * a.nds_side;
-  if (a.nl_slots > 4096) return fail(MGPU_E_INVALID, "mgpu_render: too many light samples per vertex");
-  int rc = ensure_workspace(cap, std::max<int64_t>(1, cap * a.nl_slots));
-  if (rc != MGPU_OK) return rc;
-  Workspace *w = t_ws;
+  Workspace fixed_ws;
+  Workspace *w = nullptr;
+  if (noalloc) {
+    void *base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc != MGPU_OK) return rc;
+    fixed_ws.owned = false;
+    MGPU_CUDA(cudaGetDevice(&fixed_ws.device));
+    workspace_layout(&fixed_ws, base, cap, std::max<int64_t>(1, cap * a.nl_slots));
+    fixed_ws.h_counters = g_noalloc_host_counter;
+    w = &fixed_ws;
+  } else {
+    int rc = ensure_workspace(cap, std::max<int64_t>(1, cap * a.nl_slots));
+    if (rc != MGPU_OK) return rc;
+    w = t_ws;
+  }
   a.path_L = w->path_L;
   for (int k = 0; k < 2; ++k) { a.qo[k] = w->qo[k]; a.qd[k] = w->qd[k]; a.qt[k] = w->qt[k]; }
   a.qhit = w->qhit;
@@ -788,7 +862,8 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   const int max_b = rp->max_depth > 0 ? std::min(rp->max_depth, kHardCap) : kHardCap;
   a.max_b = max_b;
   MGPU_CUDA(cudaMemsetAsync(w->stats, 0, 12 * sizeof(unsigned long long), st));
-  Profiler &pf = t_prof;
+  Profiler off;  // the allocation-free path records no events
+  Profiler &pf = noalloc ? off : t_prof;
   for (int s0 = rp->sample_begin; s0 < rp->sample_begin + rp->sample_count; s0 += ns) {
     a.s0 = s0;
     a.ns = std::min(ns, rp->sample_begin + rp->sample_count - s0);
@@ -855,6 +930,7 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   stats.kernel_launches = launches;
   t_stats = stats;
   t_stats_stream = st;
+  t_stats_dev = w->stats;
   t_stats_pending = true;
   return MGPU_OK;
 }
@@ -875,6 +951,12 @@ int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params,
   return render_impl<false>(scene, params, film, d_path_L, stream);
 }
 
+// Allocation-free render: the same estimator and film as mgpu_render, over the fixed 32 MiB
+// scratch instead of a cudaMalloc'd workspace.  See include/mgpu.h for the contract.
+int mgpu_render_noalloc(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream) {
+  return render_impl<false>(scene, params, film, nullptr, stream, true);
+}
+
 int mgpu_render_counted(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film,
                         uint64_t *counts8, void *stream) {
   if (!counts8) return fail(MGPU_E_INVALID, "mgpu_render_counted: null output");
@@ -887,10 +969,10 @@ int mgpu_render_counted(const mgpu_scene *scene, const mgpu_render_params *param
 
 int mgpu_render_stats_get(mgpu_render_stats *out) {
   if (!out) return fail(MGPU_E_INVALID, "mgpu_render_stats_get: null argument");
-  if (t_stats_pending && t_ws) {
+  if (t_stats_pending && t_stats_dev) {
     unsigned long long h[4];
     MGPU_CUDA(cudaStreamSynchronize(t_stats_stream));
-    MGPU_CUDA(cudaMemcpy(h, t_ws->stats, sizeof(h), cudaMemcpyDeviceToHost));
+    MGPU_CUDA(cudaMemcpy(h, t_stats_dev, sizeof(h), cudaMemcpyDeviceToHost));
     t_stats.extension_rays = h[0];
     t_stats.shadow_rays = h[1];
     t_stats.truncated_paths = h[2];

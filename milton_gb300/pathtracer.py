@@ -208,6 +208,16 @@ def render(dscene: DeviceScene, settings: RenderSettings, film: Film, camera: np
                                       _stream_handle(stream)))
 
 
+def render_noalloc(dscene: DeviceScene, settings: RenderSettings, film: Film, camera: np.ndarray | None = None,
+                   stream=None) -> None:
+    """mgpu_render_noalloc: like render(), but over the library's fixed 32 MiB device scratch
+    instead of allocating a workspace (for hosts that forbid device allocation while rendering;
+    calls must not overlap on the GPU)."""
+    lib = N.load()
+    p = settings.to_c(dscene.scene.camera if camera is None else camera)
+    N.check(lib.mgpu_render_noalloc(dscene.handle, C.byref(p), film.handle, _stream_handle(stream)))
+
+
 def render_counted(dscene: DeviceScene, settings: RenderSettings, film: Film, stream=None) -> dict:
     """Render with traversal counters (slower; measurement only)."""
     lib = N.load()
