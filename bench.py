@@ -273,10 +273,15 @@ def run_ours(args):
     dom = max(kern, key=lambda k: kern[k][0])
     kms, kn, kbytes = kern[dom]
     achieved = (kbytes / max(kn, 1)) / ((kms / max(kn, 1)) / 1e3) / 1e9
+    # DRAM traffic per launch: the ncu capture of the same kernel on the small case gives DRAM
+    # bytes per ray (profiles/traffic_per_ray.json); scaled here by the rays of an average launch
     traffic = None
-    tfile = ROOT / "profiles" / "traffic_per_launch.json"
+    tfile = ROOT / "profiles" / "traffic_per_ray.json"
     if tfile.exists():
-        traffic = json.loads(tfile.read_text()).get(dom)
+        per_ray = json.loads(tfile.read_text()).get(dom, {}).get("dram_bytes_per_ray")
+        rays_total = ext_rays_total if dom == "extend" else sh_rays_total
+        if per_ray:
+            traffic = per_ray * rays_total / max(kn, 1)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -305,7 +310,10 @@ def run_ours(args):
             "value": cpu["mpaths"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
             "sample": (f"rows {CPU_ROWS[0]}-{CPU_ROWS[1] - 1} of the mid frame (32 x 1024 px x 64 spp = "
                        f"{cpu['paths']} paths), FP64 oracle, same seed"), "seconds": round(cpu["seconds"], 2)}
-        out["parity"] = {"rmse_vs_fp64_same_samples": rmse, "image_mean": float(cpu["mean"].mean())}
+        out["parity"] = {"rmse_vs_fp64_same_samples": rmse, "oracle_rows_mean": float(cpu["mean"].mean()),
+                         "gpu_rows_mean": float(gpu_rows.mean()),
+                         "note": "same seed and counter RNG: paths agree unless FP32 and FP64 take "
+                                 "different discrete decisions"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -327,7 +335,9 @@ def run_profile_case(args):
     for _ in range(2):
         pt.render(ds, st, film)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": "mid 512x512x4spp x2", **pt.render_stats()}))
+    ext, sh = pt.wave_queues(MAX_DEPTH)
+    print(json.dumps({"profile_case": "mid 512x512x4spp x2", **pt.render_stats(),
+                      "extension_rays_per_bounce": ext.tolist(), "shadow_rays_per_bounce": sh.tolist()}))
     return 0
 
 

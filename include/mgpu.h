@@ -181,6 +181,9 @@ int mgpu_render_noalloc(const mgpu_scene *scene, const mgpu_render_params *param
 int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,
                       void *stream);
 int mgpu_render_stats_get(mgpu_render_stats *out); /* stats of the last render on this thread (synchronises) */
+/* Queue sizes per bounce of the last wave of the last render on this thread (synchronises):
+ * ext[b] = live paths traced at bounce b, shadow[b] = shadow rays queued at bounce b.       */
+int mgpu_render_wave_queues(uint32_t *ext, uint32_t *shadow, int32_t max_bounces);
 /* Render with traversal counters: counts8 = extension {nodes, leaf refs, triangles, rays},
  * shadow {nodes, leaf refs, triangles, rays} summed over the render (synchronises).
  * Measurement helper for the memory roofline; slower than mgpu_render.                   */

@@ -76,6 +76,7 @@ SIGNATURES = [
     ("mgpu_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_render_paths", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_render_stats_get", C.c_int, [C.POINTER(RenderStats)]),
+    ("mgpu_render_wave_queues", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     ("mgpu_render_counted", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_profile_enable", C.c_int, [C.c_int]),
     ("mgpu_profile_read", C.c_int, [C.c_void_p, C.c_void_p]),

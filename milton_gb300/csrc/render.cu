@@ -579,6 +579,7 @@ static thread_local mgpu_render_stats t_stats{};
 static thread_local cudaStream_t t_stats_stream = nullptr;
 static thread_local bool t_stats_pending = false;
 static thread_local unsigned long long *t_stats_dev = nullptr;  // device stats of the last render
+static thread_local uint32_t *t_counters_dev = nullptr;          // queue counters of its last wave
 
 // Per-kernel timing with CUDA events recorded on the launching stream around every launch.
 enum { kProfGenerate = 0, kProfExtend, kProfShade, kProfShadow, kProfAccumulate, kProfBin, kProfClasses };
@@ -931,6 +932,7 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   t_stats = stats;
   t_stats_stream = st;
   t_stats_dev = w->stats;
+  t_counters_dev = w->counters;
   t_stats_pending = true;
   return MGPU_OK;
 }
@@ -964,6 +966,17 @@ int mgpu_render_counted(const mgpu_scene *scene, const mgpu_render_params *param
   if (rc != MGPU_OK) return rc;
   MGPU_CUDA(cudaStreamSynchronize(as_stream(stream)));
   MGPU_CUDA(cudaMemcpy(counts8, t_ws->tcount, 8 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  return MGPU_OK;
+}
+
+int mgpu_render_wave_queues(uint32_t *ext, uint32_t *shadow, int32_t max_bounces) {
+  if (!ext || !shadow || max_bounces <= 0) return fail(MGPU_E_INVALID, "mgpu_render_wave_queues: bad argument");
+  if (!t_stats_dev) return fail(MGPU_E_STATE, "mgpu_render_wave_queues: nothing rendered on this thread");
+  MGPU_CUDA(cudaStreamSynchronize(t_stats_stream));
+  const uint32_t *ctr = t_counters_dev;
+  int n = std::min(max_bounces, kHardCap);
+  MGPU_CUDA(cudaMemcpy(ext, ctr + kCtrRay, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  MGPU_CUDA(cudaMemcpy(shadow, ctr + kCtrNee, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
   return MGPU_OK;
 }
 

@@ -253,6 +253,14 @@ def profile_read() -> dict:
     return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(KERNELS)}
 
 
+def wave_queues(max_bounces: int = 16) -> tuple[np.ndarray, np.ndarray]:
+    """Per-bounce extension and shadow queue sizes of the last wave rendered on this thread."""
+    ext = np.zeros(max_bounces, np.uint32)
+    sh = np.zeros(max_bounces, np.uint32)
+    N.check(N.load().mgpu_render_wave_queues(N.ptr(ext), N.ptr(sh), max_bounces))
+    return ext, sh
+
+
 def render_stats() -> dict:
     s = N.RenderStats()
     N.check(N.load().mgpu_render_stats_get(C.byref(s)))
