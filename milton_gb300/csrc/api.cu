@@ -120,6 +120,10 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
       return fail(MGPU_E_INVALID, "mgpu_scene_create: unknown material type at material " + std::to_string(i));
   }
   const KdTree &tr = accel->tree;
+  // device layout of the tree: leaf slots point into the leaf-ordered triangle records
+  std::vector<Pair> dpairs;
+  std::vector<F4> ltris;
+  kd_device_layout(tr, desc->tri_v, desc->tri_flags, dpairs, ltris);
   // host staging: triangles (3 x float4) and shading records (3 x float4)
   std::vector<F4> tris((size_t)T * 3);
   std::vector<float4> shade((size_t)T * 3);
@@ -150,9 +154,9 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     }
   }
   size_t off_pairs = 0;
-  size_t sz_pairs = tr.pairs.size() * sizeof(Pair);
+  size_t sz_pairs = dpairs.size() * sizeof(Pair);
   size_t off_refs = align_up(off_pairs + sz_pairs, 256);
-  size_t sz_refs = std::max<size_t>(tr.refs.size(), 1) * sizeof(uint32_t);
+  size_t sz_refs = std::max<size_t>(ltris.size(), 1) * sizeof(F4);
   size_t off_tris = align_up(off_refs + sz_refs, 256);
   size_t sz_tris = std::max<size_t>(tris.size(), 1) * sizeof(F4);
   size_t off_shade = align_up(off_tris + sz_tris, 256);
@@ -178,8 +182,8 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     if (n == 0) return cudaSuccess;
     return cudaMemcpyAsync(base + off, src, n, cudaMemcpyHostToDevice, st);
   };
-  e = up(off_pairs, tr.pairs.data(), sz_pairs);
-  if (e == cudaSuccess) e = up(off_refs, tr.refs.data(), tr.refs.size() * sizeof(uint32_t));
+  e = up(off_pairs, dpairs.data(), sz_pairs);
+  if (e == cudaSuccess) e = up(off_refs, ltris.data(), ltris.size() * sizeof(F4));
   if (e == cudaSuccess) e = up(off_tris, tris.data(), tris.size() * sizeof(F4));
   if (e == cudaSuccess) e = up(off_shade, shade.data(), shade.size() * sizeof(float4));
   if (e == cudaSuccess) e = up(off_mats, desc->materials, sz_mats);
@@ -193,12 +197,12 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     return cuda_fail(e, "mgpu_scene_create: upload");
   }
   s->view.pairs = (const Pair *)(base + off_pairs);
-  s->view.refs = (const uint32_t *)(base + off_refs);
+  s->view.ltris = (const F4 *)(base + off_refs);
   s->view.tris = (const F4 *)(base + off_tris);
   for (int k = 0; k < 3; ++k) { s->view.bmin[k] = (float)tr.bmin[k]; s->view.bmax[k] = (float)tr.bmax[k]; }
   s->view.ntri = T;
   s->view.npairs = tr.pairs.size();
-  s->view.nrefs = tr.refs.size();
+  s->view.nrefs = ltris.size() / 3;
   s->d_shade = (float4 *)(base + off_shade);
   s->d_mats = (float *)(base + off_mats);
   s->d_lights = (float *)(base + off_lights);

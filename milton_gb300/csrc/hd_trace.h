@@ -7,10 +7,13 @@
 //                            interior: w0 = child_pair << 2 | axis (0..2), w1 = split (float bits)
 //                            leaf:     w0 = count << 2 | 3, w1 = first ref (count > 1) or the
 //                                      triangle itself (count == 1)
-//   refs   uint32[nrefs]   leaf triangle lists, each stored in reverse of Milton's list order so
-//                          that a forward scan visits primitives in the order kdTreeAccel's
-//                          `for (i = n; i--;)` loop does (kdTreeAccel.cpp:973-996).
-//   tris   float4[3*ntri]  v0, v1, v2 (world space); v0.w carries the triangle flags.
+//   ltris  float4[3*nref]  leaf triangle records in leaf order, so a leaf's triangles are one
+//                          contiguous run read without an index indirection: (v0, prim id),
+//                          (v1, flags), (v2, 0).  Each leaf's run is in reverse of Milton's list
+//                          order, so a forward scan visits primitives in the order kdTreeAccel's
+//                          `for (i = n; i--;)` loop does (kdTreeAccel.cpp:973-996).  On the device
+//                          a leaf slot's w1 is the index of its first record.
+//   tris   float4[3*ntri]  v0, v1, v2 by primitive id (read by shading, not by traversal).
 //
 // The traversal follows kdTreeAccel::getIntersection / intersects (kdTreeAccel.cpp:893-1094):
 // root slab clip, near/far ordering by the sign of (split - origin) and the direction, a stack
@@ -41,8 +44,8 @@ struct Pair {
 
 struct SceneView {
   const Pair *pairs;
-  const uint32_t *refs;
-  const F4 *tris;          // 3 per triangle
+  const F4 *ltris;         // 3 per leaf triangle record, leaf order
+  const F4 *tris;          // 3 per triangle, by primitive id
   float bmin[3], bmax[3];  // root bounds
   int64_t ntri;
   uint64_t npairs, nrefs;
@@ -120,10 +123,17 @@ MGPU_HD bool intersect_tri(const RayPre &p, V3 v0, V3 v1, V3 v2, bool culled, fl
   if (culled && det < 0.0f) return false;
   float Az = p.sz * Akz, Bz = p.sz * Bkz, Cz = p.sz * Ckz;
   float T = U * Az + Vv * Bz + W * Cz;
+  // range test before dividing: t = T / det in (tmin, tbest) <=> T' in (tmin det', tbest det')
+  // with det' = |det| and T' = T sign(det)
+  float adet = fabsf(det);
+  float sT = det < 0.0f ? -T : T;
+  if (!(sT > tmin * adet && sT < tbest * adet)) return false;
+#if defined(__CUDA_ARCH__)
+  float rcp = __frcp_rn(det);
+#else
   float rcp = 1.0f / det;
-  float t = T * rcp;
-  if (!(t > tmin && t < tbest)) return false;
-  t_out = t;
+#endif
+  t_out = T * rcp;
   b1_out = Vv * rcp;
   b2_out = W * rcp;
   return true;
@@ -256,7 +266,7 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, cons
     } else {
       // near child = the side of the origin (Milton's ordering by the signs of diff and d)
       bool rev = diff <= 0.0f ? (dinv <= 0.0f) : (dinv < 0.0f);
-      float slack = kCellEps * fmaxf(fabsf(tmin), fabsf(tmax));
+      float slack = kCellEps * tmax;    // cells lie at t >= 0, so tmax bounds |t| in the cell
       if (dt > tmax + slack) {          // far child not reached inside this cell
         n0 = rev ? pr.b0 : pr.a0; n1 = rev ? pr.b1 : pr.a1; both = false;
       } else if (dt < tmin - slack) {   // near child lies behind the cell
@@ -281,16 +291,16 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, cons
   if (COUNT) cnt->nodes++;
   const uint32_t count = w0 >> 2;
   for (uint32_t i = 0; i < count; ++i) {
-    uint32_t tri = (count == 1) ? w1 : load_u32(s.refs, (uint64_t)w1 + i);
-    if (COUNT) { cnt->refs += (count == 1) ? 0u : 1u; cnt->tris++; }
-    F4 a = load_f4(s.tris, 3 * (int64_t)tri + 0);
-    F4 b = load_f4(s.tris, 3 * (int64_t)tri + 1);
-    F4 c = load_f4(s.tris, 3 * (int64_t)tri + 2);
-    bool culled = (f_bits(a.w) & 1u) != 0u;
+    if (COUNT) cnt->tris++;
+    const int64_t r = 3 * ((int64_t)w1 + i);
+    F4 a = load_f4(s.ltris, r + 0);
+    F4 b = load_f4(s.ltris, r + 1);
+    F4 c = load_f4(s.ltris, r + 2);
+    bool culled = (f_bits(b.w) & 1u) != 0u;
     float t, b1, b2;
     if (intersect_tri(st.pre, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), culled, st.ray_tmin, st.best, t,
                       b1, b2)) {
-      st.best = t; st.best_prim = (int32_t)tri; st.bb1 = b1; st.bb2 = b2;
+      st.best = t; st.best_prim = (int32_t)f_bits(a.w); st.bb1 = b1; st.bb2 = b2;
       if (ANY) return true;
     }
   }

@@ -366,6 +366,40 @@ bool kd_build(const float *v, int64_t ntri, const KdParams &p, KdTree &out, cons
   return true;
 }
 
+void kd_device_layout(const KdTree &t, const float *v, const uint32_t *flags, std::vector<Pair> &pairs_out,
+                      std::vector<F4> &ltris_out) {
+  pairs_out = t.pairs;
+  ltris_out.clear();
+  size_t nref = 0;
+  for (const Pair &p : t.pairs) {
+    if ((p.a0 & 3u) == kLeafTag) nref += p.a0 >> 2;
+    if ((p.b0 & 3u) == kLeafTag) nref += p.b0 >> 2;
+  }
+  ltris_out.reserve(nref * 3);
+  auto emit = [&](uint32_t &w0, uint32_t &w1) {
+    if ((w0 & 3u) != kLeafTag) return;
+    uint32_t count = w0 >> 2;
+    uint32_t first = (uint32_t)(ltris_out.size() / 3);
+    for (uint32_t i = 0; i < count; ++i) {
+      uint32_t tri = count == 1 ? w1 : t.refs[(size_t)w1 + i];
+      const float *p = v + (size_t)tri * 9;
+      uint32_t fl = flags ? flags[tri] : 0u;
+      F4 a, b, c;
+      a.x = p[0]; a.y = p[1]; a.z = p[2]; memcpy(&a.w, &tri, 4);
+      b.x = p[3]; b.y = p[4]; b.z = p[5]; memcpy(&b.w, &fl, 4);
+      c.x = p[6]; c.y = p[7]; c.z = p[8]; c.w = 0.0f;
+      ltris_out.push_back(a);
+      ltris_out.push_back(b);
+      ltris_out.push_back(c);
+    }
+    w1 = count ? first : 0u;
+  };
+  for (Pair &p : pairs_out) {
+    emit(p.a0, p.a1);
+    emit(p.b0, p.b1);
+  }
+}
+
 void kd_serialize(const KdTree &t, int32_t *kind, float *split, int32_t *count, int32_t *prims, int64_t *n_nodes,
                   int64_t *n_prims) {
   int64_t ni = 0, np = 0;

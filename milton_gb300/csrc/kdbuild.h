@@ -42,4 +42,10 @@ bool kd_build(const float *v, int64_t ntri, const KdParams &p, KdTree &out, cons
 void kd_serialize(const KdTree &t, int32_t *kind, float *split, int32_t *count, int32_t *prims, int64_t *n_nodes,
                   int64_t *n_prims);
 
+// Device layout: a copy of the pair records whose leaf slots point into ltris (w1 = first
+// record), and the leaf triangle records themselves (3 x F4 each: (v0, prim id), (v1, flags),
+// (v2, 0)), leaves in pair order, each leaf's run in the reversed (Milton iteration) order.
+void kd_device_layout(const KdTree &t, const float *v, const uint32_t *flags, std::vector<Pair> &pairs_out,
+                      std::vector<F4> &ltris_out);
+
 }  // namespace mgpu

@@ -28,15 +28,18 @@ int hc_trace(const float *v, const uint32_t *flags, int64_t ntri, const float *r
       if (k == 0 && flags) memcpy(&q.w, &flags[i], 4);
       tris[3 * i + k] = q;
     }
+  std::vector<Pair> dpairs;
+  std::vector<F4> ltris;
+  kd_device_layout(t, v, flags, dpairs, ltris);
   SceneView s;
-  s.pairs = t.pairs.data();
-  s.refs = t.refs.data();
+  s.pairs = dpairs.data();
+  s.ltris = ltris.data();
   s.tris = tris.data();
   for (int k = 0; k < 3; ++k) { s.bmin[k] = (float)t.bmin[k]; s.bmax[k] = (float)t.bmax[k]; }
   s.ntri = ntri;
   s.npairs = t.pairs.size();
-  s.nrefs = t.refs.size();
-  const Pair *top = use_top ? t.pairs.data() : nullptr;
+  s.nrefs = ltris.size() / 3;
+  const Pair *top = use_top ? dpairs.data() : nullptr;
   uint32_t ntop = use_top ? t.top_pairs : 0;
   for (int64_t i = 0; i < n; ++i) {
     const float *r = rays + 8 * i;
