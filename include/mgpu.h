@@ -126,7 +126,10 @@ int mgpu_accel_serialize(const mgpu_accel *accel, int32_t *kind, float *split, i
                          int64_t *n_nodes, int64_t *n_prims);
 int mgpu_accel_destroy(mgpu_accel *accel);
 
-/* Upload accel + scene to the current device (stream-ordered copies from host memory). */
+/* Upload accel + scene to the current device.  The triangle arrays uploaded are the ones the
+ * accel captured at build time (tree layout with leaf-ordered triangle records, triangles by id,
+ * shading records; page-locked on the first upload); desc supplies the materials and lights and
+ * must describe the same triangles.  Returns after the copies complete.                   */
 int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void *stream, mgpu_scene **out);
 int mgpu_scene_destroy(mgpu_scene *scene);
 int mgpu_scene_bytes(const mgpu_scene *scene, uint64_t *out);

@@ -32,7 +32,64 @@ int device_sm_count() {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Device-ready copies of the scene's triangles: tree layout with leaf-ordered records,
+// triangles by id (3 x float4, v0.w = flags) and shading records (3 x float4: (n0, material),
+// (n1, light), (n2, 0)).
+static void stage_device_arrays(const mgpu_scene_desc *desc, mgpu_accel *a) {
+  const int64_t T = desc->ntri;
+  kd_device_layout(a->tree, desc->tri_v, desc->tri_flags, a->dpairs, a->ltris);
+  a->tris.resize((size_t)T * 3);
+  a->shade.resize((size_t)T * 3);
+  for (int64_t t = 0; t < T; ++t) {
+    const float *v = desc->tri_v + t * 9;
+    uint32_t fl = desc->tri_flags ? desc->tri_flags[t] : 0u;
+    for (int k = 0; k < 3; ++k) {
+      F4 q; q.x = v[3 * k]; q.y = v[3 * k + 1]; q.z = v[3 * k + 2]; q.w = 0.0f;
+      if (k == 0) memcpy(&q.w, &fl, 4);
+      a->tris[3 * t + k] = q;
+    }
+    V3 e1 = v3(v[3] - v[0], v[4] - v[1], v[5] - v[2]);
+    V3 e2 = v3(v[6] - v[0], v[7] - v[1], v[8] - v[2]);
+    V3 fn = normalize(cross(e1, e2));
+    int32_t mat = desc->tri_mat[t];
+    int32_t li = desc->tri_light ? desc->tri_light[t] : -1;
+    for (int k = 0; k < 3; ++k) {
+      float4 q;
+      if (desc->tri_n) {
+        const float *n = desc->tri_n + t * 9 + 3 * k;
+        q = make_float4(n[0], n[1], n[2], 0.0f);
+      } else {
+        q = make_float4(fn.x, fn.y, fn.z, 0.0f);
+      }
+      if (k == 0) memcpy(&q.w, &mat, 4);
+      if (k == 1) memcpy(&q.w, &li, 4);
+      a->shade[3 * t + k] = q;
+    }
+  }
+}
+
+static void register_staging(mgpu_accel *a) {
+  // page-locked staging makes every later upload a direct DMA; failure just leaves it pageable
+  if (a->registered) return;
+  a->registered = true;
+  auto reg = [](void *p, size_t n) {
+    if (n) cudaHostRegister(p, n, cudaHostRegisterDefault);
+  };
+  reg(a->dpairs.data(), a->dpairs.size() * sizeof(Pair));
+  reg(a->ltris.data(), a->ltris.size() * sizeof(F4));
+  reg(a->tris.data(), a->tris.size() * sizeof(F4));
+  reg(a->shade.data(), a->shade.size() * sizeof(float4));
+  cudaGetLastError();  // clear a failed registration
+}
+
 }  // namespace mgpu
+
+mgpu_accel::~mgpu_accel() {
+  if (!registered) return;
+  for (void *p : {(void *)dpairs.data(), (void *)ltris.data(), (void *)tris.data(), (void *)shade.data()})
+    if (p) cudaHostUnregister(p);
+  cudaGetLastError();
+}
 
 using namespace mgpu;
 
@@ -53,6 +110,7 @@ int mgpu_accel_build(const mgpu_scene_desc *desc, const mgpu_kd_params *params, 
     p.empty_bias = params->empty_bias;
     p.threads = params->threads;
   }
+  if (desc->ntri > 0 && !desc->tri_mat) return fail(MGPU_E_INVALID, "mgpu_accel_build: missing material indices");
   mgpu_accel *a = new (std::nothrow) mgpu_accel();
   if (!a) return fail(MGPU_E_NOMEM, "mgpu_accel_build: out of host memory");
   const char *err = nullptr;
@@ -61,11 +119,12 @@ int mgpu_accel_build(const mgpu_scene_desc *desc, const mgpu_kd_params *params, 
       delete a;
       return fail(MGPU_E_INVALID, std::string("mgpu_accel_build: ") + err);
     }
+    a->ntri = desc->ntri;
+    stage_device_arrays(desc, a);
   } catch (const std::bad_alloc &) {
     delete a;
     return fail(MGPU_E_NOMEM, "mgpu_accel_build: out of host memory");
   }
-  a->ntri = desc->ntri;
   *out = a;
   return MGPU_OK;
 }
@@ -120,39 +179,11 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
       return fail(MGPU_E_INVALID, "mgpu_scene_create: unknown material type at material " + std::to_string(i));
   }
   const KdTree &tr = accel->tree;
-  // device layout of the tree: leaf slots point into the leaf-ordered triangle records
-  std::vector<Pair> dpairs;
-  std::vector<F4> ltris;
-  kd_device_layout(tr, desc->tri_v, desc->tri_flags, dpairs, ltris);
-  // host staging: triangles (3 x float4) and shading records (3 x float4)
-  std::vector<F4> tris((size_t)T * 3);
-  std::vector<float4> shade((size_t)T * 3);
-  for (int64_t t = 0; t < T; ++t) {
-    const float *v = desc->tri_v + t * 9;
-    uint32_t fl = desc->tri_flags ? desc->tri_flags[t] : 0u;
-    for (int k = 0; k < 3; ++k) {
-      F4 q; q.x = v[3 * k]; q.y = v[3 * k + 1]; q.z = v[3 * k + 2]; q.w = 0.0f;
-      if (k == 0) memcpy(&q.w, &fl, 4);
-      tris[3 * t + k] = q;
-    }
-    V3 e1 = v3(v[3] - v[0], v[4] - v[1], v[5] - v[2]);
-    V3 e2 = v3(v[6] - v[0], v[7] - v[1], v[8] - v[2]);
-    V3 fn = normalize(cross(e1, e2));
-    int32_t mat = desc->tri_mat[t];
-    int32_t li = desc->tri_light ? desc->tri_light[t] : -1;
-    for (int k = 0; k < 3; ++k) {
-      float4 q;
-      if (desc->tri_n) {
-        const float *n = desc->tri_n + t * 9 + 3 * k;
-        q = make_float4(n[0], n[1], n[2], 0.0f);
-      } else {
-        q = make_float4(fn.x, fn.y, fn.z, 0.0f);
-      }
-      if (k == 0) memcpy(&q.w, &mat, 4);
-      if (k == 1) memcpy(&q.w, &li, 4);
-      shade[3 * t + k] = q;
-    }
-  }
+  mgpu_accel *acc = const_cast<mgpu_accel *>(accel);
+  register_staging(acc);
+  const std::vector<Pair> &dpairs = accel->dpairs;
+  const std::vector<F4> &ltris = accel->ltris, &tris = accel->tris;
+  const std::vector<float4> &shade = accel->shade;
   size_t off_pairs = 0;
   size_t sz_pairs = dpairs.size() * sizeof(Pair);
   size_t off_refs = align_up(off_pairs + sz_pairs, 256);
@@ -189,7 +220,7 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   if (e == cudaSuccess) e = up(off_mats, desc->materials, sz_mats);
   if (e == cudaSuccess && desc->nlight > 0) e = up(off_lights, desc->lights, (size_t)desc->nlight * 16 * sizeof(float));
   if (e == cudaSuccess) e = cudaMemsetAsync(base + off_err, 0, 256, st);
-  // the staging vectors die at return: wait for the copies
+  // materials and lights are the caller's pageable arrays: wait for the copies
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cudaFree(s->d_block);

@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <string>
+#include <vector>
 
 #include "../../include/mgpu.h"
 #include "hd_shade.h"
@@ -39,6 +40,14 @@ int device_sm_count();
 struct mgpu_accel {
   mgpu::KdTree tree;
   int64_t ntri = 0;
+  // device-ready host staging, built once with the tree and uploaded by every mgpu_scene_create:
+  // pairs with leaf slots pointing into ltris, leaf-ordered triangle records, triangles by id
+  // and shading records.  Registered as page-locked memory on the first upload.
+  std::vector<mgpu::Pair> dpairs;
+  std::vector<mgpu::F4> ltris, tris;
+  std::vector<float4> shade;
+  bool registered = false;
+  ~mgpu_accel();
 };
 
 struct mgpu_scene {
