@@ -215,17 +215,33 @@ struct TravState {
   int sp;
 };
 
+MGPU_HD float safe_rcp(float d) {
+  const float tiny = 1e-30f;
+  if (d == 0.0f) d = f_bits(d) ? -tiny : tiny;  // keeps the sign of -0
+  return 1.0f / d;
+}
+
 // returns false when the ray misses the scene (no step needed)
 MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32_t ntop, TravState &st) {
   st.best = r.tmax;
   st.best_prim = -1;
   st.bb1 = st.bb2 = 0.0f;
   if (s.ntri <= 0) return false;
-  st.inv = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
-  float t0, t1;
-  if (!clip_root(s, r, st.inv, t0, t1)) return false;
-  st.tmin = fmaxf(t0, r.tmin);
-  st.tmax = fminf(t1, r.tmax);
+  {
+    V3 inv = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+    float t0, t1;
+    if (!clip_root(s, r, inv, t0, t1)) return false;
+    st.tmin = fmaxf(t0, r.tmin);
+    st.tmax = fminf(t1, r.tmax);
+  }
+  // reciprocal direction for the split planes: a zero component becomes a huge finite value of
+  // the same sign, so a ray parallel to a plane gets dt = +-huge (only the side holding its
+  // origin) without a special case per node.  Milton's traversal instead evaluates 0 * inf and,
+  // for a +0 component, can descend into the wrong child (kdTreeAccel.cpp:933-960).
+  st.inv = v3(safe_rcp(r.d.x), safe_rcp(r.d.y), safe_rcp(r.d.z));
+  float t0 = st.tmin, t1 = st.tmax;
+  (void)t0;
+  (void)t1;
   if (st.tmin > st.tmax) return false;
   st.ray_tmin = r.tmin;
   st.pre = precompute(r);
@@ -254,26 +270,16 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, cons
     Pair pr = load_pair(s, top, ntop, w0 >> 2);
     uint32_t n0, n1;
     bool both;
-    float dt = diff * dinv;
-    if (isinf(dinv)) {
-      // ray parallel to the split plane: only the side holding the origin (both if the ray
-      // lies in the plane).  Milton's traversal evaluates 0 * inf here and, for a +0
-      // direction component, descends into the wrong child.
-      both = diff == 0.0f;
-      bool right = diff < 0.0f;
-      n0 = right ? pr.b0 : pr.a0; n1 = right ? pr.b1 : pr.a1;
-      dt = tmax;
+    const float dt = diff * dinv;
+    // near child = the side of the origin (Milton's ordering by the signs of diff and d)
+    const bool rev = diff <= 0.0f ? (dinv <= 0.0f) : (dinv < 0.0f);
+    const float slack = kCellEps * tmax;  // cells lie at t >= 0, so tmax bounds |t| in the cell
+    if (dt > tmax + slack) {              // far child not reached inside this cell
+      n0 = rev ? pr.b0 : pr.a0; n1 = rev ? pr.b1 : pr.a1; both = false;
+    } else if (dt < tmin - slack) {       // near child lies behind the cell
+      n0 = rev ? pr.a0 : pr.b0; n1 = rev ? pr.a1 : pr.b1; both = false;
     } else {
-      // near child = the side of the origin (Milton's ordering by the signs of diff and d)
-      bool rev = diff <= 0.0f ? (dinv <= 0.0f) : (dinv < 0.0f);
-      float slack = kCellEps * tmax;    // cells lie at t >= 0, so tmax bounds |t| in the cell
-      if (dt > tmax + slack) {          // far child not reached inside this cell
-        n0 = rev ? pr.b0 : pr.a0; n1 = rev ? pr.b1 : pr.a1; both = false;
-      } else if (dt < tmin - slack) {   // near child lies behind the cell
-        n0 = rev ? pr.a0 : pr.b0; n1 = rev ? pr.a1 : pr.b1; both = false;
-      } else {
-        n0 = rev ? pr.b0 : pr.a0; n1 = rev ? pr.b1 : pr.a1; both = true;
-      }
+      n0 = rev ? pr.b0 : pr.a0; n1 = rev ? pr.b1 : pr.a1; both = true;
     }
     if (both) {
       // near child first, far child on the stack

@@ -14,10 +14,24 @@ extern "C" {
 
 // Builds the product tree over v (ntri*9) and traces n rays (n*8 floats) with the FP32 traversal.
 // hits: n*4 floats (t, prim bits, b1, b2); occ: n bytes (any hit); counts: n*4 uint32.
+int hc_trace_kd(const float *v, const uint32_t *flags, int64_t ntri, const float *rays, int64_t n, float *hits,
+                uint8_t *occ, uint32_t *counts, uint32_t max_depth, int use_top, uint32_t min_prims, double cost_trav,
+                double empty_bias);
+
 int hc_trace(const float *v, const uint32_t *flags, int64_t ntri, const float *rays, int64_t n, float *hits,
              uint8_t *occ, uint32_t *counts, uint32_t max_depth, int use_top) {
+  return hc_trace_kd(v, flags, ntri, rays, n, hits, occ, counts, max_depth, use_top, 3, 1.0, 0.9);
+}
+
+// same, with the kd build parameters exposed
+int hc_trace_kd(const float *v, const uint32_t *flags, int64_t ntri, const float *rays, int64_t n, float *hits,
+                uint8_t *occ, uint32_t *counts, uint32_t max_depth, int use_top, uint32_t min_prims, double cost_trav,
+                double empty_bias) {
   KdParams p;
   p.max_depth = max_depth;
+  p.min_prims = min_prims;
+  p.cost_traversal = cost_trav;
+  p.empty_bias = empty_bias;
   KdTree t;
   const char *err = nullptr;
   if (!kd_build(v, ntri, p, t, &err)) return -1;
