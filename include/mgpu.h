@@ -179,6 +179,18 @@ int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_
  *     what must start at zero itself.  Calls whose work overlaps on the GPU (other streams,
  *     other host threads) race on the array: serialise them.                                */
 int mgpu_render_noalloc(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream);
+/* Batched rendering: render requests of different scenes, resolutions and sample counts share
+ * waves, so scenes too small to fill the GPU alone render together; each request's film gets
+ * exactly the image mgpu_render would give it.  With every request at a fixed max_depth the
+ * whole launch sequence is captured in one CUDA graph and launched once (use_graph = 1).
+ * No counterpart in the reference (Milton renders one scene per process).                  */
+typedef struct mgpu_batch mgpu_batch;
+int mgpu_batch_create(mgpu_batch **out);
+int mgpu_batch_add(mgpu_batch *batch, const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film);
+int mgpu_batch_set(mgpu_batch *batch, int64_t wave_paths, int32_t use_graph); /* wave_paths 0 = automatic */
+int mgpu_batch_render(mgpu_batch *batch, void *stream);
+int mgpu_batch_clear(mgpu_batch *batch);
+int mgpu_batch_destroy(mgpu_batch *batch);
 /* Render and also write every path's radiance (after Milton's specular channel masking)
  * to d_path_L: (pixel * sample_count + sample) * 4 floats.  Test/measurement helper.     */
 int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,

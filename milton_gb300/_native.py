@@ -74,6 +74,12 @@ SIGNATURES = [
     ("mgpu_film_read_raw", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
+    ("mgpu_batch_create", C.c_int, [C.POINTER(C.c_void_p)]),
+    ("mgpu_batch_add", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderParams), C.c_void_p]),
+    ("mgpu_batch_set", C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),
+    ("mgpu_batch_render", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("mgpu_batch_clear", C.c_int, [C.c_void_p]),
+    ("mgpu_batch_destroy", C.c_int, [C.c_void_p]),
     ("mgpu_render_paths", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_render_stats_get", C.c_int, [C.POINTER(RenderStats)]),
     ("mgpu_render_wave_queues", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),

@@ -1,0 +1,65 @@
+"""Autotuner for the wavefront renderer: picks the wave size (paths in flight, i.e. queue
+capacity) and the traversal kernel shape (grid-stride or persistent warps) and queue binning by
+timing a short calibration render of the actual requests, and caches the choice per workload
+size class.  Results never depend on these knobs (every path draws its own counter-based random
+numbers and each film sums its samples in sample order), only speed does."""
+from __future__ import annotations
+
+import itertools
+import math
+
+from . import pathtracer as pt
+
+WAVES = (1 << 21, 1 << 22, 1 << 23, 1 << 24)
+SHAPES = ((0, 1, 1), (1, 1, 1), (0, 0, 0))  # (persistent, bin_shadow, bin_extension)
+
+_cache: dict = {}
+
+
+def _size_class(requests) -> tuple:
+    paths = sum(st.width * st.height for _, st in requests)
+    tris = sum(ds.scene.ntri for ds, _ in requests)
+    return (int(math.log2(max(paths, 1))), int(math.log2(max(tris, 1))))
+
+
+def tune(requests, stream=None, calib_samples: int = 1, waves=WAVES, shapes=SHAPES) -> dict:
+    """requests: list of (DeviceScene, RenderSettings).  Returns {"wave_paths", "persistent",
+    "bin_shadow", "bin_extension", "ms"} for the fastest calibration render and applies the
+    kernel-shape knobs process-wide."""
+    import torch
+    key = _size_class(requests)
+    if key in _cache:
+        best = _cache[key]
+        _apply(best)
+        return best
+    films = [pt.Film(st.width, st.height) for _, st in requests]
+    best = None
+    for wave, shape in itertools.product(waves, shapes):
+        _apply({"persistent": shape[0], "bin_shadow": shape[1], "bin_extension": shape[2]})
+        b = pt.Batch(wave_paths=wave, use_graph=True)
+        for (ds, st), f in zip(requests, films):
+            c = pt.RenderSettings(st.width, st.height, st.spp, sample_begin=0, sample_count=min(calib_samples, st.spp),
+                                  max_depth=st.max_depth or 8, rr_start_depth=st.rr_start_depth, seed=st.seed)
+            b.add(ds, c, f)
+        b.render(stream)  # warm
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.render(stream)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if best is None or ms < best["ms"]:
+            best = {"wave_paths": wave, "persistent": shape[0], "bin_shadow": shape[1], "bin_extension": shape[2],
+                    "ms": ms}
+        b.close()
+    for f in films:
+        f.close()
+    _cache[key] = best
+    _apply(best)
+    return best
+
+
+def _apply(cfg: dict) -> None:
+    for k in ("persistent", "bin_shadow", "bin_extension"):
+        pt.tune(k, int(cfg[k]))

@@ -336,12 +336,16 @@ MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *to
 
 #if defined(__CUDACC__)
 // Grid-stride traversal: every thread traces rays i, i + stride, ... to completion.
-template <bool ANY, bool COUNT, class Load, class Store>
-__device__ __forceinline__ void grid_trace(const SceneView &s, const Pair *top, uint32_t ntop, uint32_t n, Load load,
+//   view(i)                 the scene of the i-th ray (one scene, or a batch job's scene)
+//   load(i, ray)            fills the i-th ray of the batch
+//   store(i, found, state)  consumes the i-th result
+template <bool ANY, bool COUNT, class View, class Load, class Store>
+__device__ __forceinline__ void grid_trace(View view, const Pair *top, uint32_t ntop, uint32_t n, Load load,
                                            Store store, TraceCounts *cnt, uint32_t &rays_done) {
   TravState st;
   TravEntry stack[kMaxStack];
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const SceneView &s = view(i);
     Ray r;
     load(i, r);
     ++rays_done;
@@ -359,16 +363,15 @@ __device__ __forceinline__ void grid_trace(const SceneView &s, const Pair *top, 
 // Traversal on GPUs", HPG 2009): every lane owns one ray; after each leaf step, lanes whose
 // ray finished take new rays from a global counter with one warp-aggregated atomicAdd, so a
 // warp never idles behind its slowest ray.  All 32 lanes of every warp must call this.
-//   load(i, ray)            fills the i-th ray of the batch
-//   store(i, found, state)  consumes the i-th result
-template <bool ANY, bool COUNT, class Load, class Store>
-__device__ __forceinline__ void persistent_trace(const SceneView &s, const Pair *top, uint32_t ntop, uint32_t n,
+template <bool ANY, bool COUNT, class View, class Load, class Store>
+__device__ __forceinline__ void persistent_trace(View view, const Pair *top, uint32_t ntop, uint32_t n,
                                                  uint32_t *fetch, Load load, Store store, TraceCounts *cnt,
                                                  uint32_t &rays_done) {
   const unsigned kFull = 0xFFFFFFFFu;
   const int lane = threadIdx.x & 31;
   TravState st;
   TravEntry stack[kMaxStack];
+  const SceneView *sv = nullptr;
   uint32_t idx = 0;
   bool have = false, exhausted = false;
   for (;;) {
@@ -383,10 +386,11 @@ __device__ __forceinline__ void persistent_trace(const SceneView &s, const Pair 
         uint32_t my = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
         if (my < n) {
           idx = my;
+          sv = &view(idx);
           Ray r;
           load(idx, r);
           ++rays_done;
-          if (trav_init(s, r, top, ntop, st)) have = true;
+          if (trav_init(*sv, r, top, ntop, st)) have = true;
           else store(idx, false, st);
         } else {
           exhausted = true;
@@ -394,7 +398,7 @@ __device__ __forceinline__ void persistent_trace(const SceneView &s, const Pair 
       }
     }
     if (__all_sync(kFull, exhausted && !have)) break;
-    if (have && trav_step<ANY, COUNT>(s, st, stack, top, ntop, cnt)) {
+    if (have && trav_step<ANY, COUNT>(*sv, st, stack, top, ntop, cnt)) {
       store(idx, st.best_prim >= 0, st);
       have = false;
     }

@@ -1,21 +1,28 @@
 // render.cu -- wavefront path tracer: generate -> (extend -> shade -> shadow)* -> accumulate.
 //
-// One wave = a range of pixel slots (8x8 tiles, row-major tile order) x a range of sample
-// passes.  Per path the state is split in two:
+// Work is organised in waves of paths.  A wave holds one or more job chunks; a chunk is a range
+// of pixel slots (8x8 tiles, row-major tile order) x a range of sample passes of one render job
+// (one scene, camera, film and set of PathTracer parameters).  A plain render is one job; a batch
+// (mgpu_batch_*) packs the chunks of many jobs of uneven size into shared waves, so small scenes
+// fill the GPU together.  Per-chunk parameters live in a device array of JobArgs; every path
+// records its chunk in path_job[], and every kernel reads its chunk's scene and parameters there.
+//
+// Per path the state is split in two:
 //   path_L[p]     float4  radiance accumulated so far (rgb) + path flags (w) -- path-indexed,
-//                          updated by shade (emission) and shadow (direct light), read once by
-//                          accumulate;
-//   ray queue     3 x float4 per live path (origin + path index, direction, throughput + depth
-//                          state), compacted every bounce by warp ballot + one atomicAdd per warp.
+//                          updated by shade (emission, folded direct light), read by accumulate;
+//   ray queue     3 x float4 per live path (origin + path index, direction + chunk, throughput +
+//                          depth state), compacted every bounce by warp ballot + one atomicAdd per
+//                          warp.
 // Direct light (DirectIllumination::evaluate over all lights x noDirectSamples,
 // DirectIllumination.cpp:46-138) is split in two: shade samples every light, evaluates the BSDF,
 // writes each sample's contribution into the path's slot for that sample and queues one shadow
 // ray per non-zero contribution; the shadow kernel is a plain any-hit query that zeroes the slot
 // of an occluded sample.  The next kernel to see the path (shade at the next bounce, or
 // accumulate) folds its slots into the radiance in slot order, so every sum runs in a fixed
-// order and the image does not depend on queue order.
+// order and the image does not depend on queue order, wave size or batch composition.
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -33,56 +40,83 @@ constexpr int kCtrFetchSh = 3 * (kHardCap + 8);    // ... and of the persistent 
 constexpr int kCtrTrunc = 4 * (kHardCap + 8);
 constexpr int kNumCounters = kCtrTrunc + 8;
 constexpr float kShadowMargin = 1e-4f;  // shadow rays stop this fraction short of the light
+constexpr int kBins = 4096;             // queue binning keys
 
-struct RenderArgs {
+// One job chunk of a wave (device memory).
+struct JobArgs {
   SceneView view;
-  uint32_t ntop;
   const float4 *shade;
   const float4 *mats;    // 4 per material
   const float4 *lights;  // 4 per light
-  int32_t nlight;
+  int32_t nlight, nl_slots, sh_cell_bits;
   Camera cam;
   Rng rng;
-  int32_t W, H, spp, side, s2;
-  int32_t nds, nds_side;
-  int32_t max_depth, rr_start, efficient;
-  int32_t tiles_x;
-  int64_t slot0, nslots;
-  int32_t s0, ns;        // samples [s0, s0 + ns) of this wave
+  int32_t W, H, spp, side, s2, nds, nds_side, max_depth, rr_start, efficient, tiles_x;
+  int32_t s0, ns;                 // samples [s0, s0 + ns) of this chunk
   int32_t sample_begin, sample_count;
+  int64_t slot0, nslots;          // slots [slot0, slot0 + nslots)
+  int64_t path_base;              // first wave path of the chunk
+  int64_t slot_base;              // first accumulate slot of the chunk in the wave
+  float4 *film_sum, *film_c;
+  float4 *path_out;               // optional per-path radiance
+};
+
+// One wave (kernel parameter).
+struct RenderArgs {
+  const JobArgs *jobs;
+  int32_t njobs;
+  int64_t npaths, nslots;         // paths and accumulate slots in the wave
+  int32_t nl_stride;              // light-sample slots per path (max over the wave's chunks)
+  uint32_t *path_job;
   float4 *path_L;
   float4 *qo[2], *qd[2], *qt[2];
   float4 *qhit;
-  float4 *so, *sd;       // shadow ray queue: origin + slot index, direction + tmax
-  float4 *qo_u, *qd_u, *qt_u;  // unsorted next-ray queue (binning on)
-  float4 *so_u, *sd_u;         // unsorted shadow queue (binning on)
-  uint32_t *qkey, *skey;       // bin keys of the unsorted queues
-  int32_t bin_ext, bin_sh;     // counting-sort the queues by (direction octant | light, origin cell)
-  int32_t sh_cell_bits;        // Morton bits of the origin cell in the shadow key
-  float4 *slots;         // nl_slots per path: direct-light contribution per light sample
-  int32_t nl_slots;      // nlight * nds_side^2
+  float4 *so, *sd;               // shadow ray queue: origin + slot index, direction + tmax
+  float4 *slots;                 // nl_stride per path: direct-light contribution per light sample
+  float4 *qo_u, *qd_u, *qt_u;    // unsorted next-ray queue (binning on)
+  float4 *so_u, *sd_u;           // unsorted shadow queue (binning on)
+  uint32_t *qkey, *skey;         // bin keys of the unsorted queues
+  int32_t bin_ext, bin_sh;       // counting-sort the queues by (direction octant | light, origin cell)
   uint32_t *counters;
-  unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] truncated paths, [3] bounces
-  unsigned long long *tcount; // counted mode: ext nodes, refs, tris, rays; shadow nodes, refs, tris, rays
+  unsigned long long *stats;     // [0] extension rays, [1] shadow rays, [2] truncated paths, [3] bounces
+  unsigned long long *tcount;    // counted mode: ext nodes, refs, tris, rays; shadow nodes, refs, tris, rays
   int32_t max_b;
-  float4 *film_sum, *film_c;
-  float4 *path_out;      // optional
 };
 
-__device__ __forceinline__ bool slot_pixel(const RenderArgs &a, int64_t slot, int &x, int &y) {
+__device__ __forceinline__ bool slot_pixel(const JobArgs &J, int64_t slot, int &x, int &y) {
   int64_t tile = slot >> 6;
   int within = (int)(slot & 63);
-  x = (int)(tile % a.tiles_x) * 8 + (within & 7);
-  y = (int)(tile / a.tiles_x) * 8 + (within >> 3);
-  return x < a.W && y < a.H;
+  x = (int)(tile % J.tiles_x) * 8 + (within & 7);
+  y = (int)(tile / J.tiles_x) * 8 + (within >> 3);
+  return x < J.W && y < J.H;
 }
 
-// global path id (pixel * spp + sample) for wave-local path p
-__device__ __forceinline__ uint64_t path_id(const RenderArgs &a, int64_t p, int &x, int &y, int &s) {
-  int64_t slot = a.slot0 + p / a.ns;
-  s = a.s0 + (int)(p % a.ns);
-  slot_pixel(a, slot, x, y);
-  return ((uint64_t)y * a.W + x) * (uint64_t)a.spp + (uint64_t)s;
+// global path id (pixel * spp + sample) for wave path p of chunk J
+__device__ __forceinline__ uint64_t path_id(const JobArgs &J, int64_t p, int &x, int &y, int &s) {
+  const int64_t lp = p - J.path_base;
+  const int64_t slot = J.slot0 + lp / J.ns;
+  s = J.s0 + (int)(lp % J.ns);
+  slot_pixel(J, slot, x, y);
+  return ((uint64_t)y * J.W + x) * (uint64_t)J.spp + (uint64_t)s;
+}
+
+// chunk holding wave path p / accumulate slot q (binary search over the sorted bases)
+__device__ __forceinline__ int job_of_path(const RenderArgs &a, int64_t p) {
+  int lo = 0, hi = a.njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (a.jobs[mid].path_base <= p) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int job_of_slot(const RenderArgs &a, int64_t q) {
+  int lo = 0, hi = a.njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (a.jobs[mid].slot_base <= q) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 // warp-aggregated queue append: returns the slot for this lane (valid only if want)
@@ -98,73 +132,58 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
   return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
-__device__ __forceinline__ Material load_mat(const RenderArgs &a, int i) {
+__device__ __forceinline__ Material load_mat(const JobArgs &J, int i) {
   float m[16];
   float4 *mm = reinterpret_cast<float4 *>(m);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) mm[k] = __ldg(a.mats + 4 * i + k);
+  for (int k = 0; k < 4; ++k) mm[k] = __ldg(J.mats + 4 * i + k);
   return material_from(m);
 }
 
-__device__ __forceinline__ Light load_light(const RenderArgs &a, int i) {
+__device__ __forceinline__ Light load_light(const JobArgs &J, int i) {
   float l[16];
   float4 *ll = reinterpret_cast<float4 *>(l);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) ll[k] = __ldg(a.lights + 4 * i + k);
+  for (int k = 0; k < 4; ++k) ll[k] = __ldg(J.lights + 4 * i + k);
   return light_from(l);
-}
-
-__device__ __forceinline__ void load_top(const RenderArgs &a) {
-  extern __shared__ uint4 smem_top[];
-  for (uint32_t i = threadIdx.x; i < a.ntop; i += blockDim.x)
-    smem_top[i] = __ldg(reinterpret_cast<const uint4 *>(a.view.pairs) + i);
-  __syncthreads();
-}
-
-__device__ __forceinline__ const Pair *top_ptr(const RenderArgs &a) {
-  extern __shared__ uint4 smem_top[];
-  return a.ntop ? reinterpret_cast<const Pair *>(smem_top) : nullptr;
 }
 
 // Binning keys (kBins = 4096).  Ray coherence: rays of one warp should start close together
 // and head the same way, so that they visit the same nodes.  Keys combine the direction
 // octant (extension rays) or the light index (shadow rays) with the Morton code of the
 // origin's cell in a 16x16x16 grid over the scene bounds.
-constexpr int kBins = 4096;
-
 __device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> every third bit
   return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
 }
 
-__device__ __forceinline__ uint32_t morton12(const RenderArgs &a, V3 p) {
-  const float *lo = a.view.bmin, *hi = a.view.bmax;
+__device__ __forceinline__ uint32_t morton12(const SceneView &s, V3 p) {
   uint32_t c[3];
   const float pp[3] = {p.x, p.y, p.z};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    float ext = hi[k] - lo[k];
-    float f = ext > 0.0f ? (pp[k] - lo[k]) / ext : 0.0f;
+    float ext = s.bmax[k] - s.bmin[k];
+    float f = ext > 0.0f ? (pp[k] - s.bmin[k]) / ext : 0.0f;
     int q = (int)(f * 16.0f);
     c[k] = (uint32_t)min(max(q, 0), 15);
   }
   return (spread4(c[0]) << 2) | (spread4(c[1]) << 1) | spread4(c[2]);
 }
 
-__device__ __forceinline__ uint32_t ext_key(const RenderArgs &a, V3 o, V3 d) {
+__device__ __forceinline__ uint32_t ext_key(const JobArgs &J, V3 o, V3 d) {
   uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-  return (oct << 9) | (morton12(a, o) >> 3);
+  return (oct << 9) | (morton12(J.view, o) >> 3);
 }
 
-__device__ __forceinline__ uint32_t sh_key(const RenderArgs &a, int light, V3 o) {
-  uint32_t cell = morton12(a, o) >> (12 - a.sh_cell_bits);
-  return (((uint32_t)light << a.sh_cell_bits) | cell) & (kBins - 1);
+__device__ __forceinline__ uint32_t sh_key(const JobArgs &J, int light, V3 o) {
+  uint32_t cell = morton12(J.view, o) >> (12 - J.sh_cell_bits);
+  return (((uint32_t)light << J.sh_cell_bits) | cell) & (kBins - 1);
 }
 
 // ---------------------------------------------------------------------------------------
 // generate: camera rays for every path of the wave (RayTracer::sample, RayTracer.cpp:19-30;
 // SuperSampleGenerator strata, SuperSampleGenerator.cpp:60-90)
 __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
-  const int64_t n = a.nslots * a.ns;
+  const int64_t n = a.npaths;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
     int64_t p = base + threadIdx.x;
@@ -172,22 +191,25 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
     bool live = false;
     float4 o4 = make_float4(0, 0, 0, 0), d4 = o4;
     if (valid) {
+      const int j = job_of_path(a, p);
+      const JobArgs &J = a.jobs[j];
+      a.path_job[p] = (uint32_t)j;
       int x, y, s;
-      uint64_t pid = path_id(a, p, x, y, s);
-      live = x < a.W && y < a.H;
+      uint64_t pid = path_id(J, p, x, y, s);
+      live = x < J.W && y < J.H;
       uint32_t flags = 0;
       if (live) {
-        uint64_t pix = (uint64_t)y * a.W + x;
-        int k = s % a.s2;
-        F4u j = uniforms(a.rng, pix * (uint64_t)a.s2 + (uint64_t)k, kDepthJitter, 0);
-        float px = ((float)x + ((float)(k % a.side) + j.a) / (float)a.side) / (float)a.W;
-        float py = ((float)y + ((float)(k / a.side) + j.b) / (float)a.side) / (float)a.H;
-        F4u ui = uniforms(a.rng, pid, kDepthPathInit, 0);
+        uint64_t pix = (uint64_t)y * J.W + x;
+        int k = s % J.s2;
+        F4u jt = uniforms(J.rng, pix * (uint64_t)J.s2 + (uint64_t)k, kDepthJitter, 0);
+        float px = ((float)x + ((float)(k % J.side) + jt.a) / (float)J.side) / (float)J.W;
+        float py = ((float)y + ((float)(k / J.side) + jt.b) / (float)J.side) / (float)J.H;
+        F4u ui = uniforms(J.rng, pid, kDepthPathInit, 0);
         uint32_t ior = min((uint32_t)(ui.a * 3.0f), 2u);
         flags = ior;
-        V3 d = camera_dir(a.cam, px, py);
-        o4 = make_float4(a.cam.eye.x, a.cam.eye.y, a.cam.eye.z, __int_as_float((int)p));
-        d4 = make_float4(d.x, d.y, d.z, 0.0f);
+        V3 d = camera_dir(J.cam, px, py);
+        o4 = make_float4(J.cam.eye.x, J.cam.eye.y, J.cam.eye.z, __int_as_float((int)p));
+        d4 = make_float4(d.x, d.y, d.z, __int_as_float(j));
       }
       a.path_L[p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(flags));
     }
@@ -203,13 +225,16 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
 // extend: closest hit for the live queue of bounce b
 template <bool COUNT, bool PERSIST>
 __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
-  load_top(a);
-  const Pair *top = top_ptr(a);
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
   float4 *qhit = a.qhit;
   TraceCounts c = {0, 0, 0, 0};
   uint32_t rays = 0;
+  const bool single = a.njobs == 1;
+  const SceneView *view0 = &a.jobs[0].view;
+  auto view_of = [&](uint32_t i) -> const SceneView & {
+    return single ? *view0 : a.jobs[__float_as_int(qd[i].w)].view;
+  };
   auto load = [&](uint32_t i, Ray &r) {
     float4 o = qo[i], d = qd[i];
     r.o = v3(o.x, o.y, o.z);
@@ -222,9 +247,9 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
                           hit ? st.bb2 : 0.0f);
   };
   if (PERSIST)
-    persistent_trace<false, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
+    persistent_trace<false, COUNT>(view_of, nullptr, 0, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
   else
-    grid_trace<false, COUNT>(a.view, top, a.ntop, n, load, store, &c, rays);
+    grid_trace<false, COUNT>(view_of, nullptr, 0, n, load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[0], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[1], (unsigned long long)c.refs);
@@ -235,9 +260,9 @@ __global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
 
 // shade: pending direct light, emission, light sampling, BSDF sample and Russian roulette
 // (PathTracer.cpp:36-115, DirectIllumination.cpp:46-138)
-__device__ __forceinline__ V3 fold_slots(const RenderArgs &a, int64_t p, V3 L) {
-  const float4 *sl = a.slots + p * a.nl_slots;
-  for (int k = 0; k < a.nl_slots; ++k) {
+__device__ __forceinline__ V3 fold_slots(const RenderArgs &a, int nl, int64_t p, V3 L) {
+  const float4 *sl = a.slots + p * a.nl_stride;
+  for (int k = 0; k < nl; ++k) {
     float4 c = sl[k];
     L = L + v3(c.x, c.y, c.z);
   }
@@ -248,7 +273,6 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const int cur = b & 1, nxt = (b + 1) & 1;
   const uint32_t stride = gridDim.x * blockDim.x;
-  const int s2n = a.nds_side * a.nds_side;
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
     uint32_t i = base + threadIdx.x;
     bool valid = i < n;
@@ -256,13 +280,15 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
     float4 no_o, no_d, no_t;
     int64_t p = 0;
     uint64_t pid = 0;
-    int depth = 0, self = -1;
+    int depth = 0, self = -1, j = 0;
     V3 P = v3(0, 0, 0), ns = P, ng = P, d = P, thr = P;
     Material m;
     m.type = 0;
     if (valid) {
       float4 o4 = a.qo[cur][i], d4 = a.qd[cur][i], t4 = a.qt[cur][i], h4 = a.qhit[i];
       p = (int64_t)__float_as_int(o4.w);
+      j = __float_as_int(d4.w);
+      const JobArgs &J = a.jobs[j];
       uint32_t state = __float_as_uint(t4.w);
       depth = (int)(state & 0xFFFFu);
       bool ec = (state >> 16) & 1u;
@@ -273,43 +299,43 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
       uint32_t flags = __float_as_uint(L4.w);
       V3 L = v3(L4.x, L4.y, L4.z);
       if (flags & kFlagNeePending) {
-        L = fold_slots(a, p, L);
+        L = fold_slots(a, J.nl_slots, p, L);
         flags &= ~kFlagNeePending;
       }
       if (prim >= 0) {
         int x, y, s;
-        pid = path_id(a, p, x, y, s);
+        pid = path_id(J, p, x, y, s);
         float t = h4.x, b1 = h4.z, b2 = h4.w, b0 = 1.0f - b1 - b2;
-        float4 va = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim);
-        float4 vb = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim + 1);
-        float4 vc = __ldg(reinterpret_cast<const float4 *>(a.view.tris) + 3 * (int64_t)prim + 2);
-        float4 s0 = __ldg(a.shade + 3 * (int64_t)prim), s1 = __ldg(a.shade + 3 * (int64_t)prim + 1),
-               s2 = __ldg(a.shade + 3 * (int64_t)prim + 2);
+        float4 va = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim);
+        float4 vb = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim + 1);
+        float4 vc = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim + 2);
+        float4 s0 = __ldg(J.shade + 3 * (int64_t)prim), s1 = __ldg(J.shade + 3 * (int64_t)prim + 1),
+               s2 = __ldg(J.shade + 3 * (int64_t)prim + 2);
         V3 v0 = v3(va.x, va.y, va.z), v1 = v3(vb.x, vb.y, vb.z), v2 = v3(vc.x, vc.y, vc.z);
         P = v0 * b0 + v1 * b1 + v2 * b2;
         ns = normalize(v3(s0.x, s0.y, s0.z) * b0 + v3(s1.x, s1.y, s1.z) * b1 + v3(s2.x, s2.y, s2.z) * b2);
         ng = normalize(cross(v1 - v0, v2 - v0));
         int mi = __float_as_int(s0.w);
         self = __float_as_int(s1.w);
-        m = load_mat(a, mi);
+        m = load_mat(J, mi);
         bool spec = is_specular(m);
         if (spec) flags |= kFlagSpecular;
         if (self >= 0) {
-          Light lt = load_light(a, self);
+          Light lt = load_light(J, self);
           V3 Le = emitted(lt.Le, ns, -d);
-          if (!a.efficient || depth == 0) L = L + mul(thr, Le);
+          if (!J.efficient || depth == 0) L = L + mul(thr, Le);
           else if (ec) L = L + mul(thr, Le) * (lt.area / (t * t));
         }
-        if (a.efficient && !spec && a.nlight > 0) {
+        if (J.efficient && !spec && J.nlight > 0) {
           do_nee = true;
           flags |= kFlagNeePending;
         }
-        F4u u = uniforms(a.rng, pid, (uint32_t)depth, 0);
+        F4u u = uniforms(J.rng, pid, (uint32_t)depth, 0);
         V3 wo, fs;
         int ev = bsdf_sample(m, ns, d, flags & kFlagIorMask, u.a, u.b, u.c, wo, fs);
         if (ev > 0) {
-          float pc = depth < a.rr_start ? (nonzero(fs) ? 1.0f : 0.0f) : fminf(0.95f, maxc(fs));
-          bool capped = (a.max_depth > 0 && depth + 1 >= a.max_depth);
+          float pc = depth < J.rr_start ? (nonzero(fs) ? 1.0f : 0.0f) : fminf(0.95f, maxc(fs));
+          bool capped = (J.max_depth > 0 && depth + 1 >= J.max_depth);
           if (!capped && u.d < pc) {
             if (depth + 1 >= kHardCap) {
               flags |= kFlagTruncated;
@@ -321,7 +347,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
               bool nec = spec && dot(ns, wo) > kEps;
               V3 org = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
               no_o = make_float4(org.x, org.y, org.z, o4.w);
-              no_d = make_float4(wo.x, wo.y, wo.z, 0.0f);
+              no_d = make_float4(wo.x, wo.y, wo.z, d4.w);
               no_t = make_float4(nthr.x, nthr.y, nthr.z, __uint_as_float((uint32_t)(depth + 1) | (nec ? 0x10000u : 0u)));
             }
           }
@@ -329,34 +355,36 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
       }
       a.path_L[p] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
     }
+    const JobArgs &J = a.jobs[j];
     uint32_t q = warp_append(&a.counters[kCtrRay + b + 1], want_next);
     if (want_next) {
       if (a.bin_ext) {
         a.qo_u[q] = no_o;
         a.qd_u[q] = no_d;
         a.qt_u[q] = no_t;
-        a.qkey[q] = ext_key(a, v3(no_o.x, no_o.y, no_o.z), v3(no_d.x, no_d.y, no_d.z));
+        a.qkey[q] = ext_key(J, v3(no_o.x, no_o.y, no_o.z), v3(no_d.x, no_d.y, no_d.z));
       } else {
         a.qo[nxt][q] = no_o;
         a.qd[nxt][q] = no_d;
         a.qt[nxt][q] = no_t;
       }
     }
-    // light samples: every lane of the warp runs the same k loop (uniform trip count), so the
-    // warp-aggregated append stays converged
-    const float inv_nds = 1.0f / (float)a.nds;
-    for (int k = 0; k < a.nl_slots; ++k) {
+    // light samples: every lane of the warp runs the same k loop (uniform trip count: the
+    // wave's stride), so the warp-aggregated append stays converged
+    const int s2n = J.nds_side * J.nds_side;
+    const float inv_nds = 1.0f / (float)J.nds;
+    for (int k = 0; k < a.nl_stride; ++k) {
       bool want = false;
       float4 so4, sd4;
-      if (do_nee) {
+      if (do_nee && k < J.nl_slots) {
         int li = k / s2n, within = k - li * s2n;
-        int sy = within / a.nds_side, sx = within - sy * a.nds_side;
+        int sy = within / J.nds_side, sx = within - sy * J.nds_side;
         V3 c = v3(0.0f, 0.0f, 0.0f);
         if (li != self) {
-          Light lt = load_light(a, li);
-          F4u u = uniforms(a.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
-          float ux = ((float)sx + ((k & 1) ? u.c : u.a)) / (float)a.nds_side;
-          float uy = ((float)sy + ((k & 1) ? u.d : u.b)) / (float)a.nds_side;
+          Light lt = load_light(J, li);
+          F4u u = uniforms(J.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
+          float ux = ((float)sx + ((k & 1) ? u.c : u.a)) / (float)J.nds_side;
+          float uy = ((float)sy + ((k & 1) ? u.d : u.b)) / (float)J.nds_side;
           V3 lp = lt.center + lt.ex * (ux - 0.5f) + lt.ez * (uy - 0.5f);
           V3 wo = lp - P;
           float t = length(wo);
@@ -369,19 +397,19 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
             if (nonzero(c)) {
               want = true;
               V3 org = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
-              so4 = make_float4(org.x, org.y, org.z, __uint_as_float((uint32_t)(p * a.nl_slots + k)));
+              so4 = make_float4(org.x, org.y, org.z, __uint_as_float((uint32_t)(p * a.nl_stride + k)));
               sd4 = make_float4(wo.x, wo.y, wo.z, t * (1.0f - kShadowMargin));
             }
           }
         }
-        a.slots[p * a.nl_slots + k] = make_float4(c.x, c.y, c.z, 0.0f);
+        a.slots[p * a.nl_stride + k] = make_float4(c.x, c.y, c.z, 0.0f);
       }
       uint32_t e = warp_append(&a.counters[kCtrNee + b], want);
       if (want) {
         if (a.bin_sh) {
           a.so_u[e] = so4;
           a.sd_u[e] = sd4;
-          a.skey[e] = sh_key(a, k / s2n, P);
+          a.skey[e] = sh_key(J, k / s2n, P);
         } else {
           a.so[e] = so4;
           a.sd[e] = sd4;
@@ -394,13 +422,18 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
 // shadow: any-hit query per queued light sample; an occluded sample's slot is zeroed
 template <bool COUNT, bool PERSIST>
 __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
-  load_top(a);
-  const Pair *top = top_ptr(a);
   const uint32_t n = a.counters[kCtrNee + b];
   const float4 *so = a.so, *sd = a.sd;
   float4 *slots = a.slots;
   TraceCounts c = {0, 0, 0, 0};
   uint32_t rays = 0;
+  const bool single = a.njobs == 1;
+  const SceneView *view0 = &a.jobs[0].view;
+  auto view_of = [&](uint32_t i) -> const SceneView & {
+    if (single) return *view0;
+    const uint32_t slot = __float_as_uint(so[i].w);
+    return a.jobs[a.path_job[slot / (uint32_t)a.nl_stride]].view;
+  };
   auto load = [&](uint32_t i, Ray &r) {
     float4 o = so[i], d = sd[i];
     r.o = v3(o.x, o.y, o.z);
@@ -412,9 +445,9 @@ __global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
     if (hit) slots[__float_as_uint(so[i].w)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   };
   if (PERSIST)
-    persistent_trace<true, COUNT>(a.view, top, a.ntop, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
+    persistent_trace<true, COUNT>(view_of, nullptr, 0, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
   else
-    grid_trace<true, COUNT>(a.view, top, a.ntop, n, load, store, &c, rays);
+    grid_trace<true, COUNT>(view_of, nullptr, 0, n, load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[4], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[5], (unsigned long long)c.refs);
@@ -503,14 +536,13 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint32_t *__restrict_
 // (ProgressiveFilterValue::addSample, ProgressiveFilterValue.h:33-36, box weight 1)
 __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    unsigned long long ext = 0, bounces = 0;
+    unsigned long long ext = 0, bounces = 0, sh = 0;
     for (int b = 0; b < a.max_b; ++b) {
       uint32_t c = a.counters[kCtrRay + b];
       ext += c;
       bounces += c ? 1ull : 0ull;
+      sh += a.counters[kCtrNee + b];
     }
-    unsigned long long sh = 0;
-    for (int b = 0; b < a.max_b; ++b) sh += a.counters[kCtrNee + b];
     a.stats[0] += ext;
     a.stats[1] += sh;
     a.stats[2] += a.counters[kCtrTrunc];
@@ -518,27 +550,29 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
   }
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.nslots; q += stride) {
+    const JobArgs &J = a.jobs[job_of_slot(a, q)];
+    const int64_t lq = q - J.slot_base;
     int x, y;
-    if (!slot_pixel(a, a.slot0 + q, x, y)) continue;
-    int64_t pix = (int64_t)y * a.W + x;
-    float4 S = a.film_sum[pix], C = a.film_c[pix];
-    for (int si = 0; si < a.ns; ++si) {
-      const int64_t p = q * a.ns + si;
+    if (!slot_pixel(J, J.slot0 + lq, x, y)) continue;
+    int64_t pix = (int64_t)y * J.W + x;
+    float4 S = J.film_sum[pix], C = J.film_c[pix];
+    for (int si = 0; si < J.ns; ++si) {
+      const int64_t p = J.path_base + lq * J.ns + si;
       float4 L4 = a.path_L[p];
       V3 L = v3(L4.x, L4.y, L4.z);
-      if (__float_as_uint(L4.w) & kFlagNeePending) L = fold_slots(a, p, L);
+      if (__float_as_uint(L4.w) & kFlagNeePending) L = fold_slots(a, J.nl_slots, p, L);
       L = apply_mask(L, __float_as_uint(L4.w));
-      if (a.path_out) {
-        int s = a.s0 + si - a.sample_begin;
-        a.path_out[pix * a.sample_count + s] = make_float4(L.x, L.y, L.z, L4.w);
+      if (J.path_out) {
+        int s = J.s0 + si - J.sample_begin;
+        J.path_out[pix * J.sample_count + s] = make_float4(L.x, L.y, L.z, L4.w);
       }
       float yx = L.x - C.x, tx = S.x + yx; C.x = (tx - S.x) - yx; S.x = tx;
       float yy = L.y - C.y, ty = S.y + yy; C.y = (ty - S.y) - yy; S.y = ty;
       float yz = L.z - C.z, tz = S.z + yz; C.z = (tz - S.z) - yz; S.z = tz;
     }
-    S.w += (float)a.ns;
-    a.film_sum[pix] = S;
-    a.film_c[pix] = C;
+    S.w += (float)J.ns;
+    J.film_sum[pix] = S;
+    J.film_c[pix] = C;
   }
 }
 
@@ -547,13 +581,16 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
 
 struct Workspace {
   int device = -1;
-  int64_t cap = 0;  // paths
+  int64_t cap = 0;       // paths
+  int64_t slot_cap = 0;  // light-sample slots
+  int64_t job_cap = 0;   // JobArgs entries
   void *block = nullptr;
   float4 *path_L = nullptr, *qo[2] = {}, *qd[2] = {}, *qt[2] = {}, *qhit = nullptr;
   float4 *so = nullptr, *sd = nullptr, *slots = nullptr;
   float4 *qo_u = nullptr, *qd_u = nullptr, *qt_u = nullptr, *so_u = nullptr, *sd_u = nullptr;
   uint32_t *qkey = nullptr, *skey = nullptr, *hist = nullptr, *cursor = nullptr;  // hist/cursor: kBins each
-  int64_t slot_cap = 0;  // light-sample slots
+  uint32_t *path_job = nullptr;
+  JobArgs *jobs = nullptr;
   uint32_t *counters = nullptr;
   unsigned long long *stats = nullptr;   // 4
   unsigned long long *tcount = nullptr;  // 8
@@ -629,16 +666,19 @@ struct Profiler {
 static thread_local Profiler t_prof;
 
 // float4 arrays: path_L, 2 x (qo, qd, qt), qhit, unsorted (qo, qd, qt) = 11 per path;
-// so, sd, slots, unsorted (so, sd) = 5 per light sample; uint32 keys per path and per sample
-static size_t workspace_bytes(int64_t paths, int64_t slots) {
+// so, sd, slots, unsorted (so, sd) = 5 per light sample; uint32 keys per path and per sample,
+// path_job per path; JobArgs entries
+static size_t workspace_bytes(int64_t paths, int64_t slots, int64_t jobs) {
   size_t f4 = (size_t)paths * 11 + (size_t)slots * 5;
-  size_t u32 = (size_t)paths + (size_t)slots + 2 * kBins + kNumCounters;
-  return f4 * sizeof(float4) + 12 * sizeof(unsigned long long) + u32 * sizeof(uint32_t) + 1024;
+  size_t u32 = (size_t)paths * 2 + (size_t)slots + 2 * kBins + kNumCounters;
+  return f4 * sizeof(float4) + (size_t)jobs * sizeof(JobArgs) + 12 * sizeof(unsigned long long) +
+         u32 * sizeof(uint32_t) + 1024;
 }
 
-static void workspace_layout(Workspace *w, void *block, int64_t paths, int64_t slots) {
+static void workspace_layout(Workspace *w, void *block, int64_t paths, int64_t slots, int64_t jobs) {
   w->cap = paths;
   w->slot_cap = slots;
+  w->job_cap = jobs;
   w->block = block;
   float4 *f = (float4 *)block;
   w->path_L = f; f += paths;
@@ -647,21 +687,27 @@ static void workspace_layout(Workspace *w, void *block, int64_t paths, int64_t s
   w->qo_u = f; f += paths; w->qd_u = f; f += paths; w->qt_u = f; f += paths;
   w->so = f; f += slots; w->sd = f; f += slots; w->slots = f; f += slots;
   w->so_u = f; f += slots; w->sd_u = f; f += slots;
-  w->stats = (unsigned long long *)f;
+  w->jobs = (JobArgs *)f;  // JobArgs is a multiple of 8 bytes; float4 alignment holds
+  w->stats = (unsigned long long *)(w->jobs + jobs);
   w->tcount = w->stats + 4;
   uint32_t *u = (uint32_t *)(w->tcount + 8);
   w->qkey = u; u += paths;
+  w->path_job = u; u += paths;
   w->skey = u; u += slots;
   w->hist = u; u += kBins;
   w->cursor = u; u += kBins;
   w->counters = u;
 }
 
-static int ensure_workspace(int64_t paths, int64_t slots) {
+static int ensure_workspace(int64_t paths, int64_t slots, int64_t jobs) {
   int dev = 0;
   MGPU_CUDA(cudaGetDevice(&dev));
-  if (t_ws && t_ws->device == dev && t_ws->cap >= paths && t_ws->slot_cap >= slots) return MGPU_OK;
+  if (t_ws && t_ws->device == dev && t_ws->cap >= paths && t_ws->slot_cap >= slots && t_ws->job_cap >= jobs)
+    return MGPU_OK;
   if (t_ws) {
+    paths = std::max(paths, t_ws->cap);
+    slots = std::max(slots, t_ws->slot_cap);
+    jobs = std::max(jobs, t_ws->job_cap);
     cudaDeviceSynchronize();
     delete t_ws;
     t_ws = nullptr;
@@ -669,12 +715,12 @@ static int ensure_workspace(int64_t paths, int64_t slots) {
   Workspace *w = new Workspace();
   w->device = dev;
   void *block = nullptr;
-  cudaError_t e = cudaMalloc(&block, workspace_bytes(paths, slots));
+  cudaError_t e = cudaMalloc(&block, workspace_bytes(paths, slots, jobs));
   if (e != cudaSuccess) {
     delete w;
     return cuda_fail(e, "render workspace cudaMalloc");
   }
-  workspace_layout(w, block, paths, slots);
+  workspace_layout(w, block, paths, slots, jobs);
   e = cudaMallocHost(&w->h_counters, 64);
   if (e != cudaSuccess) {
     delete w;
@@ -689,6 +735,7 @@ static int ensure_workspace(int64_t paths, int64_t slots) {
 // resident from module load until exit.  Host code only holds a stand-in for the array's
 // name; the device address comes from cudaGetSymbolAddress, once per device.
 constexpr size_t kNoAllocBytes = (size_t)32 << 20;  // 32 MiB
+constexpr int64_t kNoAllocJobs = 256;              // chunk descriptors kept in the scratch
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 constexpr int kNoAllocMaxDevices = 64;
 static std::mutex g_noalloc_mu;
@@ -713,8 +760,9 @@ static int noalloc_scratch(void **out) {
 
 // paths per wave that fit the fixed scratch for nl_slots light samples per path
 static int64_t noalloc_paths(int64_t nl_slots) {
-  const size_t fixed = workspace_bytes(0, 0);
-  const size_t per = 11 * sizeof(float4) + sizeof(uint32_t) + (size_t)nl_slots * (5 * sizeof(float4) + sizeof(uint32_t));
+  const size_t fixed = workspace_bytes(0, 0, kNoAllocJobs);
+  const size_t per = 11 * sizeof(float4) + 2 * sizeof(uint32_t) +
+                     (size_t)nl_slots * (5 * sizeof(float4) + sizeof(uint32_t));
   if (kNoAllocBytes <= fixed) return 0;
   int64_t p = (int64_t)((kNoAllocBytes - fixed) / per);
   return p / 64 * 64;
@@ -747,187 +795,305 @@ static Camera make_camera(const float *c) {
   return k;
 }
 
-template <bool COUNT>
-static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_film *film, float *d_path_out,
-                       void *stream, bool noalloc = false) {
-  if (!sc || !rp || !film) return fail(MGPU_E_INVALID, "mgpu_render: null argument");
-  if (rp->width != film->width || rp->height != film->height)
+// A render request: one scene, parameters, film, optional per-path output.
+struct Job {
+  const mgpu_scene *scene;
+  mgpu_render_params p;
+  mgpu_film *film;
+  float *path_out;
+};
+
+static int validate(const Job &j) {
+  const mgpu_render_params *rp = &j.p;
+  if (!j.scene || !j.film) return fail(MGPU_E_INVALID, "mgpu_render: null argument");
+  if (rp->width != j.film->width || rp->height != j.film->height)
     return fail(MGPU_E_INVALID, "mgpu_render: film size differs from the render size");
   if (rp->width <= 0 || rp->height <= 0 || rp->spp <= 0 || rp->sample_count < 0 || rp->sample_begin < 0 ||
       rp->no_direct_samples <= 0 || rp->max_depth < 0 || rp->rr_start_depth < 0)
     return fail(MGPU_E_INVALID, "mgpu_render: bad parameters");
-  if (rp->sample_count == 0) return MGPU_OK;
   if ((int64_t)rp->sample_begin + rp->sample_count > (int64_t)1 << 30)
     return fail(MGPU_E_INVALID, "mgpu_render: sample range too large");
-  cudaStream_t st = as_stream(stream);
-  RenderArgs a;
-  memset(&a, 0, sizeof(a));
-  a.view = sc->view;
-  a.ntop = sc->top_pairs;
-  a.shade = sc->d_shade;
-  a.mats = (const float4 *)sc->d_mats;
-  a.lights = (const float4 *)sc->d_lights;
-  a.nlight = sc->nlight;
-  a.cam = make_camera(rp->camera);
-  a.rng.k0 = (uint32_t)rp->seed;
-  a.rng.k1 = (uint32_t)(rp->seed >> 32);
-  a.rng.stream = rp->stream_id;
-  a.W = rp->width;
-  a.H = rp->height;
-  a.spp = rp->spp;
-  a.side = std::max(1, (int)sqrt((double)rp->spp));
-  a.s2 = a.side * a.side;
-  a.nds = rp->no_direct_samples;
-  a.nds_side = std::max(1, (int)sqrt((double)rp->no_direct_samples));
-  a.max_depth = rp->max_depth;
-  a.rr_start = rp->rr_start_depth;
-  a.efficient = rp->efficient_direct;
-  a.tiles_x = (a.W + 7) / 8;
-  a.sample_begin = rp->sample_begin;
-  a.sample_count = rp->sample_count;
-  a.film_sum = film->d_sum;
-  a.film_c = film->d_c;
-  a.path_out = (float4 *)d_path_out;
-  const int64_t tiles_y = (a.H + 7) / 8;
-  const int64_t total_slots = (int64_t)a.tiles_x * tiles_y * 64;
-  int64_t wave = rp->wave_paths > 0 ? rp->wave_paths : (int64_t)1 << 24;
-  a.nl_slots = sc->nlight * a.nds_side * a.nds_side;
-  if (a.nl_slots > 4096) return fail(MGPU_E_INVALID, "mgpu_render: too many light samples per vertex");
-  if (noalloc) {
-    const int64_t pmax = noalloc_paths(a.nl_slots);
-    if (pmax < 64)
-      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: " + std::to_string(a.nl_slots) +
-                                      " light samples per vertex do not fit the 32 MiB fixed scratch");
-    if (rp->wave_paths > pmax)
-      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: wave_paths " + std::to_string(rp->wave_paths) +
-                                      " exceeds the fixed scratch (32 MiB holds " + std::to_string(pmax) +
-                                      " paths at " + std::to_string(a.nl_slots) + " light samples per vertex)");
-    wave = rp->wave_paths > 0 ? rp->wave_paths : pmax;
+  int nds_side = std::max(1, (int)sqrt((double)rp->no_direct_samples));
+  if ((int64_t)j.scene->nlight * nds_side * nds_side > 4096)
+    return fail(MGPU_E_INVALID, "mgpu_render: too many light samples per vertex");
+  return MGPU_OK;
+}
+
+// the job-level part of JobArgs
+static JobArgs job_args(const Job &j) {
+  const mgpu_scene *sc = j.scene;
+  const mgpu_render_params *rp = &j.p;
+  JobArgs J;
+  memset(&J, 0, sizeof(J));
+  J.view = sc->view;
+  J.shade = sc->d_shade;
+  J.mats = (const float4 *)sc->d_mats;
+  J.lights = (const float4 *)sc->d_lights;
+  J.nlight = sc->nlight;
+  J.cam = make_camera(rp->camera);
+  J.rng.k0 = (uint32_t)rp->seed;
+  J.rng.k1 = (uint32_t)(rp->seed >> 32);
+  J.rng.stream = rp->stream_id;
+  J.W = rp->width;
+  J.H = rp->height;
+  J.spp = rp->spp;
+  J.side = std::max(1, (int)sqrt((double)rp->spp));
+  J.s2 = J.side * J.side;
+  J.nds = rp->no_direct_samples;
+  J.nds_side = std::max(1, (int)sqrt((double)rp->no_direct_samples));
+  J.nl_slots = sc->nlight * J.nds_side * J.nds_side;
+  J.max_depth = rp->max_depth;
+  J.rr_start = rp->rr_start_depth;
+  J.efficient = rp->efficient_direct;
+  J.tiles_x = (J.W + 7) / 8;
+  J.sample_begin = rp->sample_begin;
+  J.sample_count = rp->sample_count;
+  J.film_sum = j.film->d_sum;
+  J.film_c = j.film->d_c;
+  J.path_out = (float4 *)j.path_out;
+  int nlp = 1;
+  while (nlp < std::min(sc->nlight, 16)) nlp <<= 1;
+  int lb = 0;
+  while ((1 << lb) < nlp) ++lb;
+  J.sh_cell_bits = 12 - lb;  // light index in the top bits, origin cell below
+  return J;
+}
+
+struct Wave {
+  std::vector<JobArgs> chunks;
+  int64_t npaths = 0, nslots = 0;
+  int32_t nl_stride = 1;
+  int32_t max_b = 1;
+  bool unlimited = false;  // a chunk has no depth cap: drain by reading the live count
+};
+
+// Splits every job into chunks (sample passes outer, slot ranges inner, as many passes of the
+// whole image as fit a wave) and packs them into waves of at most `cap` paths.  Two chunks of
+// one job that share pixels never go into the same wave (their accumulate threads would race
+// on the film); chunks of one job keep their sample order across waves.
+static void pack_waves(const std::vector<Job> &jobs, int64_t cap, std::vector<Wave> &waves) {
+  waves.clear();
+  Wave cur;
+  std::vector<int> last_job_wave(jobs.size(), -1);
+  auto flush = [&]() {
+    if (!cur.chunks.empty()) waves.push_back(cur);
+    cur = Wave();
+  };
+  for (size_t ji = 0; ji < jobs.size(); ++ji) {
+    const Job &job = jobs[ji];
+    if (job.p.sample_count == 0) continue;
+    JobArgs base = job_args(job);
+    const int64_t total_slots = (int64_t)base.tiles_x * ((base.H + 7) / 8) * 64;
+    const int ns = (int)std::max<int64_t>(1, std::min<int64_t>(job.p.sample_count, cap / total_slots));
+    const int64_t spw = std::min<int64_t>(total_slots, std::max<int64_t>(64, cap / ns) / 64 * 64);
+    bool job_in_cur = false;
+    for (int s0 = job.p.sample_begin; s0 < job.p.sample_begin + job.p.sample_count; s0 += ns) {
+      const int nsc = std::min(ns, job.p.sample_begin + job.p.sample_count - s0);
+      for (int64_t slot0 = 0; slot0 < total_slots; slot0 += spw) {
+        const int64_t nsl = std::min(spw, total_slots - slot0);
+        const int64_t np = nsl * nsc;
+        // a new sample range of a job already in this wave would revisit its pixels
+        const bool conflict = job_in_cur && slot0 == 0;
+        if (cur.npaths + np > cap || conflict) {
+          flush();
+          job_in_cur = false;
+        }
+        JobArgs J = base;
+        J.s0 = s0;
+        J.ns = nsc;
+        J.slot0 = slot0;
+        J.nslots = nsl;
+        J.path_base = cur.npaths;
+        J.slot_base = cur.nslots;
+        cur.chunks.push_back(J);
+        cur.npaths += np;
+        cur.nslots += nsl;
+        cur.nl_stride = std::max(cur.nl_stride, std::max(1, J.nl_slots));
+        if (job.p.max_depth > 0) cur.max_b = std::max(cur.max_b, std::min(job.p.max_depth, kHardCap));
+        else cur.unlimited = true;
+        job_in_cur = true;
+      }
+    }
   }
-  // samples per wave: as many passes of the whole image as fit, else one pass over a slot range
-  int ns = (int)std::max<int64_t>(1, std::min<int64_t>(rp->sample_count, wave / total_slots));
-  int64_t slots_per_wave = std::min<int64_t>(total_slots, std::max<int64_t>(64, wave / ns) / 64 * 64);
-  int64_t cap = slots_per_wave * ns;
+  flush();
+  for (auto &w : waves)
+    if (w.unlimited) w.max_b = kHardCap;
+}
+
+// Renders a list of jobs.  noalloc: use the fixed scratch instead of the cached workspace.
+template <bool COUNT>
+static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc, int64_t wave_req,
+                       uint64_t *graph_launches = nullptr, bool capture = false) {
+  for (const Job &j : jobs) {
+    int rc = validate(j);
+    if (rc != MGPU_OK) return rc;
+  }
+  cudaStream_t st = as_stream(stream);
+  int32_t nl_max = 1;
+  for (const Job &j : jobs)
+    nl_max = std::max(nl_max, std::max(1, job_args(j).nl_slots));
+  int64_t wave = wave_req > 0 ? wave_req : (int64_t)1 << 24;
+  if (noalloc) {
+    const int64_t pmax = noalloc_paths(nl_max);
+    if (pmax < 64)
+      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: " + std::to_string(nl_max) +
+                                      " light samples per vertex do not fit the 32 MiB fixed scratch");
+    if (wave_req > pmax)
+      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: wave_paths " + std::to_string(wave_req) +
+                                      " exceeds the fixed scratch (32 MiB holds " + std::to_string(pmax) +
+                                      " paths at " + std::to_string(nl_max) + " light samples per vertex)");
+    wave = wave_req > 0 ? wave_req : pmax;
+  }
+  std::vector<Wave> waves;
+  pack_waves(jobs, wave, waves);
+  if (waves.empty()) return MGPU_OK;
+  int64_t cap = 0, ncap = 0;
+  for (auto &w : waves) {
+    cap = std::max(cap, w.npaths);
+    ncap += (int64_t)w.chunks.size();
+  }
   Workspace fixed_ws;
   Workspace *w = nullptr;
   if (noalloc) {
+    if (ncap > kNoAllocJobs)
+      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: more than " + std::to_string(kNoAllocJobs) + " chunks");
     void *base = nullptr;
     int rc = noalloc_scratch(&base);
     if (rc != MGPU_OK) return rc;
     fixed_ws.owned = false;
     MGPU_CUDA(cudaGetDevice(&fixed_ws.device));
-    workspace_layout(&fixed_ws, base, cap, std::max<int64_t>(1, cap * a.nl_slots));
+    workspace_layout(&fixed_ws, base, cap, std::max<int64_t>(1, cap * nl_max), kNoAllocJobs);
     fixed_ws.h_counters = g_noalloc_host_counter;
     w = &fixed_ws;
   } else {
-    int rc = ensure_workspace(cap, std::max<int64_t>(1, cap * a.nl_slots));
+    int rc = ensure_workspace(cap, std::max<int64_t>(1, cap * nl_max), ncap);
     if (rc != MGPU_OK) return rc;
     w = t_ws;
   }
-  a.path_L = w->path_L;
-  for (int k = 0; k < 2; ++k) { a.qo[k] = w->qo[k]; a.qd[k] = w->qd[k]; a.qt[k] = w->qt[k]; }
-  a.qhit = w->qhit;
-  a.so = w->so; a.sd = w->sd; a.slots = w->slots;
-  a.qo_u = w->qo_u; a.qd_u = w->qd_u; a.qt_u = w->qt_u; a.so_u = w->so_u; a.sd_u = w->sd_u;
-  a.qkey = w->qkey; a.skey = w->skey;
-  a.bin_ext = g_tune.bin_extension.load();
-  a.bin_sh = g_tune.bin_shadow.load();
-  {
-    int nlp = 1;
-    while (nlp < std::min(sc->nlight, 16)) nlp <<= 1;
-    int lb = 0;
-    while ((1 << lb) < nlp) ++lb;
-    a.sh_cell_bits = 12 - lb;  // light index in the top bits, origin cell below
-  }
-  a.counters = w->counters;
-  a.stats = w->stats;
-  a.tcount = w->tcount;
+  // all chunk descriptors of this render go up in one copy (before any capture)
+  std::vector<JobArgs> all;
+  all.reserve((size_t)ncap);
+  for (auto &wv : waves) all.insert(all.end(), wv.chunks.begin(), wv.chunks.end());
+  MGPU_CUDA(cudaMemcpyAsync(w->jobs, all.data(), all.size() * sizeof(JobArgs), cudaMemcpyHostToDevice, st));
+  MGPU_CUDA(cudaStreamSynchronize(st));  // `all` is pageable and dies at return
 
   const bool persist = g_tune.persistent.load() != 0;
   auto kext = persist ? k_extend<COUNT, true> : k_extend<COUNT, false>;
   auto kshw = persist ? k_shadow<COUNT, true> : k_shadow<COUNT, false>;
-  size_t smem = (size_t)a.ntop * sizeof(uint4);
-  if (smem > 48 * 1024) {
-    MGPU_CUDA(cudaFuncSetAttribute(kext, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MGPU_CUDA(cudaFuncSetAttribute(kshw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  }
   const int g_gen = grid_for((const void *)k_generate, 0);
-  const int g_ext = grid_for((const void *)kext, smem);
+  const int g_ext = grid_for((const void *)kext, 0);
   const int g_sha = grid_for((const void *)k_shade, 0);
-  const int g_shw = grid_for((const void *)kshw, smem);
+  const int g_shw = grid_for((const void *)kshw, 0);
   const int g_acc = grid_for((const void *)k_accumulate, 0);
   const int g_bin = device_sm_count() * 4;
+  const int bin_ext = g_tune.bin_extension.load(), bin_sh = g_tune.bin_shadow.load();
+
+  bool any_unlimited = false;
+  for (auto &wv : waves) any_unlimited |= wv.unlimited;
+  cudaGraph_t graph = nullptr;
+  const bool use_graph = capture && !any_unlimited && !noalloc;
+  if (use_graph) MGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
 
   mgpu_render_stats stats{};
   uint64_t launches = 0;
-  const int max_b = rp->max_depth > 0 ? std::min(rp->max_depth, kHardCap) : kHardCap;
-  a.max_b = max_b;
-  MGPU_CUDA(cudaMemsetAsync(w->stats, 0, 12 * sizeof(unsigned long long), st));
-  Profiler off;  // the allocation-free path records no events
-  Profiler &pf = noalloc ? off : t_prof;
-  for (int s0 = rp->sample_begin; s0 < rp->sample_begin + rp->sample_count; s0 += ns) {
-    a.s0 = s0;
-    a.ns = std::min(ns, rp->sample_begin + rp->sample_count - s0);
-    for (int64_t slot0 = 0; slot0 < total_slots; slot0 += slots_per_wave) {
-      a.slot0 = slot0;
-      a.nslots = std::min(slots_per_wave, total_slots - slot0);
-      MGPU_CUDA(cudaMemsetAsync(w->counters, 0, kNumCounters * sizeof(uint32_t), st));
-      int m = pf.begin(kProfGenerate, st);
-      k_generate<<<g_gen, kBlock, 0, st>>>(a);
-      pf.end(m, st);
-      ++launches;
-      int b = 0;
-      while (b < max_b) {
-        // with a fixed depth cap every bounce is launched blind; without one, check the live
-        // count every 4 bounces and stop when the wave has drained
-        int chunk = rp->max_depth > 0 ? max_b : std::min(4, max_b - b);
-        for (int k = 0; k < chunk; ++k, ++b) {
-          m = pf.begin(kProfExtend, st);
-          kext<<<g_ext, kBlock, smem, st>>>(a, b);
-          pf.end(m, st);
-          m = pf.begin(kProfShade, st);
-          k_shade<<<g_sha, kBlock, 0, st>>>(a, b);
-          pf.end(m, st);
-          if (a.bin_sh || a.bin_ext) {
-            m = pf.begin(kProfBin, st);
-            if (a.bin_sh) {
-              MGPU_CUDA(cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st));
-              k_bin_hist<<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->hist);
-              k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
-              k_bin_scatter<2><<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->cursor, w->so_u, w->sd_u,
-                                                      nullptr, w->so, w->sd, nullptr);
-              launches += 3;
-            }
-            if (a.bin_ext && b + 1 < max_b) {
-              const int nx = (b + 1) & 1;
-              MGPU_CUDA(cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st));
-              k_bin_hist<<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->hist);
-              k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
-              k_bin_scatter<3><<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->cursor, w->qo_u,
-                                                      w->qd_u, w->qt_u, w->qo[nx], w->qd[nx], w->qt[nx]);
-              launches += 3;
-            }
-            pf.end(m, st);
+  Profiler off;  // the allocation-free and graph paths record no events
+  Profiler &pf = (noalloc || use_graph) ? off : t_prof;
+  cudaError_t err = cudaMemsetAsync(w->stats, 0, 12 * sizeof(unsigned long long), st);
+  size_t job_off = 0;
+  for (size_t wi = 0; wi < waves.size() && err == cudaSuccess; ++wi) {
+    const Wave &wv = waves[wi];
+    RenderArgs a;
+    memset(&a, 0, sizeof(a));
+    a.jobs = w->jobs + job_off;
+    a.njobs = (int32_t)wv.chunks.size();
+    job_off += wv.chunks.size();
+    a.npaths = wv.npaths;
+    a.nslots = wv.nslots;
+    a.nl_stride = wv.nl_stride;
+    a.path_job = w->path_job;
+    a.path_L = w->path_L;
+    for (int k = 0; k < 2; ++k) { a.qo[k] = w->qo[k]; a.qd[k] = w->qd[k]; a.qt[k] = w->qt[k]; }
+    a.qhit = w->qhit;
+    a.so = w->so; a.sd = w->sd; a.slots = w->slots;
+    a.qo_u = w->qo_u; a.qd_u = w->qd_u; a.qt_u = w->qt_u; a.so_u = w->so_u; a.sd_u = w->sd_u;
+    a.qkey = w->qkey; a.skey = w->skey;
+    a.bin_ext = bin_ext;
+    a.bin_sh = bin_sh;
+    a.counters = w->counters;
+    a.stats = w->stats;
+    a.tcount = w->tcount;
+    a.max_b = wv.max_b;
+    const int max_b = wv.max_b;
+    err = cudaMemsetAsync(w->counters, 0, kNumCounters * sizeof(uint32_t), st);
+    int m = pf.begin(kProfGenerate, st);
+    k_generate<<<g_gen, kBlock, 0, st>>>(a);
+    pf.end(m, st);
+    ++launches;
+    int b = 0;
+    while (b < max_b && err == cudaSuccess) {
+      // with a fixed depth cap every bounce is launched blind; without one, check the live
+      // count every 4 bounces and stop when the wave has drained
+      int chunk = wv.unlimited ? std::min(4, max_b - b) : max_b;
+      for (int k = 0; k < chunk; ++k, ++b) {
+        m = pf.begin(kProfExtend, st);
+        kext<<<g_ext, kBlock, 0, st>>>(a, b);
+        pf.end(m, st);
+        m = pf.begin(kProfShade, st);
+        k_shade<<<g_sha, kBlock, 0, st>>>(a, b);
+        pf.end(m, st);
+        if (a.bin_sh || a.bin_ext) {
+          m = pf.begin(kProfBin, st);
+          if (a.bin_sh) {
+            cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st);
+            k_bin_hist<<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->hist);
+            k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
+            k_bin_scatter<2><<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->cursor, w->so_u, w->sd_u,
+                                                    nullptr, w->so, w->sd, nullptr);
+            launches += 3;
           }
-          m = pf.begin(kProfShadow, st);
-          kshw<<<g_shw, kBlock, smem, st>>>(a, b);
+          if (a.bin_ext && b + 1 < max_b) {
+            const int nx = (b + 1) & 1;
+            cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st);
+            k_bin_hist<<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->hist);
+            k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
+            k_bin_scatter<3><<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->cursor, w->qo_u,
+                                                    w->qd_u, w->qt_u, w->qo[nx], w->qd[nx], w->qt[nx]);
+            launches += 3;
+          }
           pf.end(m, st);
-          launches += 3;
         }
-        if (rp->max_depth > 0) break;
-        MGPU_CUDA(cudaMemcpyAsync(w->h_counters, w->counters + kCtrRay + b, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        MGPU_CUDA(cudaStreamSynchronize(st));
-        if (w->h_counters[0] == 0) break;
+        m = pf.begin(kProfShadow, st);
+        kshw<<<g_shw, kBlock, 0, st>>>(a, b);
+        pf.end(m, st);
+        launches += 3;
       }
-      m = pf.begin(kProfAccumulate, st);
-      k_accumulate<<<g_acc, kBlock, 0, st>>>(a);
-      pf.end(m, st);
-      ++launches;
-      MGPU_CUDA(cudaGetLastError());
+      if (!wv.unlimited) break;
+      err = cudaMemcpyAsync(w->h_counters, w->counters + kCtrRay + b, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+      if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+      if (err != cudaSuccess || w->h_counters[0] == 0) break;
     }
+    m = pf.begin(kProfAccumulate, st);
+    k_accumulate<<<g_acc, kBlock, 0, st>>>(a);
+    pf.end(m, st);
+    ++launches;
+    if (err == cudaSuccess) err = cudaGetLastError();
   }
+  if (use_graph) {
+    cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    if (err == cudaSuccess) err = ec;
+    if (err == cudaSuccess) {
+      cudaGraphExec_t exec = nullptr;
+      err = cudaGraphInstantiate(&exec, graph, 0);
+      if (err == cudaSuccess) err = cudaGraphLaunch(exec, st);
+      if (exec) cudaGraphExecDestroy(exec);
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (graph_launches) *graph_launches += 1;
+  }
+  if (err != cudaSuccess) return cuda_fail(err, "render");
   g_launches.fetch_add(launches);
-  stats.paths = (uint64_t)a.W * a.H * (uint64_t)rp->sample_count;
+  stats.paths = 0;
+  for (const Job &j : jobs) stats.paths += (uint64_t)j.p.width * j.p.height * (uint64_t)j.p.sample_count;
   stats.kernel_launches = launches;
   t_stats = stats;
   t_stats_stream = st;
@@ -937,41 +1103,106 @@ static int render_impl(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_
   return MGPU_OK;
 }
 
+template <bool COUNT>
+static int render_one(const mgpu_scene *sc, const mgpu_render_params *rp, mgpu_film *film, float *d_path_out,
+                      void *stream, bool noalloc = false) {
+  if (!sc || !rp || !film) return fail(MGPU_E_INVALID, "mgpu_render: null argument");
+  std::vector<Job> jobs(1);
+  jobs[0].scene = sc;
+  jobs[0].p = *rp;
+  jobs[0].film = film;
+  jobs[0].path_out = d_path_out;
+  if (rp->sample_count == 0) return validate(jobs[0]);
+  return render_jobs<COUNT>(jobs, stream, noalloc, rp->wave_paths);
+}
+
 }  // namespace mgpu
+
+// A batch: render requests that share waves (mgpu_batch_*).
+struct mgpu_batch {
+  std::vector<mgpu::Job> jobs;
+  int64_t wave_paths = 0;
+  int use_graph = 1;
+  uint64_t graph_launches = 0;
+};
 
 using namespace mgpu;
 
 extern "C" {
 
 int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream) {
-  return render_impl<false>(scene, params, film, nullptr, stream);
+  return render_one<false>(scene, params, film, nullptr, stream);
 }
 
 int mgpu_render_paths(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, float *d_path_L,
                       void *stream) {
   if (!d_path_L) return fail(MGPU_E_INVALID, "mgpu_render_paths: null path buffer");
-  return render_impl<false>(scene, params, film, d_path_L, stream);
+  return render_one<false>(scene, params, film, d_path_L, stream);
 }
 
 // Allocation-free render: the same estimator and film as mgpu_render, over the fixed 32 MiB
 // scratch instead of a cudaMalloc'd workspace.  See include/mgpu.h for the contract.
 int mgpu_render_noalloc(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream) {
-  return render_impl<false>(scene, params, film, nullptr, stream, true);
+  return render_one<false>(scene, params, film, nullptr, stream, true);
 }
 
 int mgpu_render_counted(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film,
                         uint64_t *counts8, void *stream) {
   if (!counts8) return fail(MGPU_E_INVALID, "mgpu_render_counted: null output");
-  int rc = render_impl<true>(scene, params, film, nullptr, stream);
+  int rc = render_one<true>(scene, params, film, nullptr, stream);
   if (rc != MGPU_OK) return rc;
   MGPU_CUDA(cudaStreamSynchronize(as_stream(stream)));
   MGPU_CUDA(cudaMemcpy(counts8, t_ws->tcount, 8 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
   return MGPU_OK;
 }
 
+int mgpu_batch_create(mgpu_batch **out) {
+  if (!out) return fail(MGPU_E_INVALID, "mgpu_batch_create: null argument");
+  *out = new (std::nothrow) mgpu_batch();
+  if (!*out) return fail(MGPU_E_NOMEM, "mgpu_batch_create: out of host memory");
+  return MGPU_OK;
+}
+
+int mgpu_batch_add(mgpu_batch *b, const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film) {
+  if (!b || !scene || !params || !film) return fail(MGPU_E_INVALID, "mgpu_batch_add: null argument");
+  Job j;
+  j.scene = scene;
+  j.p = *params;
+  j.film = film;
+  j.path_out = nullptr;
+  int rc = validate(j);
+  if (rc != MGPU_OK) return rc;
+  b->jobs.push_back(j);
+  return MGPU_OK;
+}
+
+int mgpu_batch_set(mgpu_batch *b, int64_t wave_paths, int32_t use_graph) {
+  if (!b || wave_paths < 0) return fail(MGPU_E_INVALID, "mgpu_batch_set: bad argument");
+  b->wave_paths = wave_paths;
+  b->use_graph = use_graph;
+  return MGPU_OK;
+}
+
+int mgpu_batch_render(mgpu_batch *b, void *stream) {
+  if (!b) return fail(MGPU_E_INVALID, "mgpu_batch_render: null batch");
+  if (b->jobs.empty()) return MGPU_OK;
+  return render_jobs<false>(b->jobs, stream, false, b->wave_paths, &b->graph_launches, b->use_graph != 0);
+}
+
+int mgpu_batch_clear(mgpu_batch *b) {
+  if (!b) return fail(MGPU_E_INVALID, "mgpu_batch_clear: null batch");
+  b->jobs.clear();
+  return MGPU_OK;
+}
+
+int mgpu_batch_destroy(mgpu_batch *b) {
+  delete b;
+  return MGPU_OK;
+}
+
 int mgpu_render_wave_queues(uint32_t *ext, uint32_t *shadow, int32_t max_bounces) {
   if (!ext || !shadow || max_bounces <= 0) return fail(MGPU_E_INVALID, "mgpu_render_wave_queues: bad argument");
-  if (!t_stats_dev) return fail(MGPU_E_STATE, "mgpu_render_wave_queues: nothing rendered on this thread");
+  if (!t_counters_dev) return fail(MGPU_E_STATE, "mgpu_render_wave_queues: nothing rendered on this thread");
   MGPU_CUDA(cudaStreamSynchronize(t_stats_stream));
   const uint32_t *ctr = t_counters_dev;
   int n = std::min(max_bounces, kHardCap);

@@ -38,7 +38,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(SceneView s, uint32_t nto
     }
     if (COUNT) counts[i] = make_uint4(c.nodes, c.refs, c.tris, c.max_stack);
   };
-  persistent_trace<ANY, COUNT>(s, top, ntop, n, fetch, load, store, &c, done);
+  auto view = [&](uint32_t) -> const SceneView & { return s; };
+  persistent_trace<ANY, COUNT>(view, top, ntop, n, fetch, load, store, &c, done);
 }
 
 template <bool ANY, bool COUNT>

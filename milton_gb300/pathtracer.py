@@ -261,6 +261,41 @@ def wave_queues(max_bounces: int = 16) -> tuple[np.ndarray, np.ndarray]:
     return ext, sh
 
 
+class Batch:
+    """Render requests of different scenes / resolutions / sample counts sharing waves
+    (mgpu_batch_*); each film receives exactly the image render() would give it."""
+
+    def __init__(self, wave_paths: int = 0, use_graph: bool = True):
+        self._lib = N.load()
+        self.handle = C.c_void_p()
+        N.check(self._lib.mgpu_batch_create(C.byref(self.handle)))
+        N.check(self._lib.mgpu_batch_set(self.handle, wave_paths, 1 if use_graph else 0))
+        self._keep = []
+
+    def add(self, dscene: DeviceScene, settings: RenderSettings, film: Film, camera: np.ndarray | None = None):
+        p = settings.to_c(dscene.scene.camera if camera is None else camera)
+        N.check(self._lib.mgpu_batch_add(self.handle, dscene.handle, C.byref(p), film.handle))
+        self._keep.append((dscene, film))
+
+    def render(self, stream=None):
+        N.check(self._lib.mgpu_batch_render(self.handle, _stream_handle(stream)))
+
+    def clear(self):
+        N.check(self._lib.mgpu_batch_clear(self.handle))
+        self._keep = []
+
+    def close(self):
+        if self.handle:
+            self._lib.mgpu_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def render_stats() -> dict:
     s = N.RenderStats()
     N.check(N.load().mgpu_render_stats_get(C.byref(s)))
