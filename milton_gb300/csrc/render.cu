@@ -947,16 +947,24 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   std::vector<Wave> waves;
   pack_waves(jobs, wave, waves);
   if (waves.empty()) return MGPU_OK;
-  int64_t cap = 0, ncap = 0;
+  bool any_unlimited = false;
+  for (auto &wv : waves) any_unlimited |= wv.unlimited;
+  const bool use_graph = capture && !any_unlimited && !noalloc;
+  // chunk descriptors: all of them up front when the launches are captured in a graph (no
+  // host copies inside a capture), else each wave's own before its launches
+  int64_t cap = 0, ncap = 0, nmax = 0;
   for (auto &w : waves) {
     cap = std::max(cap, w.npaths);
     ncap += (int64_t)w.chunks.size();
+    nmax = std::max(nmax, (int64_t)w.chunks.size());
   }
+  const int64_t job_slots = use_graph ? ncap : nmax;
   Workspace fixed_ws;
   Workspace *w = nullptr;
   if (noalloc) {
-    if (ncap > kNoAllocJobs)
-      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: more than " + std::to_string(kNoAllocJobs) + " chunks");
+    if (job_slots > kNoAllocJobs)
+      return fail(MGPU_E_INVALID, "mgpu_render_noalloc: more than " + std::to_string(kNoAllocJobs) +
+                                      " chunks in one wave");
     void *base = nullptr;
     int rc = noalloc_scratch(&base);
     if (rc != MGPU_OK) return rc;
@@ -966,16 +974,17 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
     fixed_ws.h_counters = g_noalloc_host_counter;
     w = &fixed_ws;
   } else {
-    int rc = ensure_workspace(cap, std::max<int64_t>(1, cap * nl_max), ncap);
+    int rc = ensure_workspace(cap, std::max<int64_t>(1, cap * nl_max), job_slots);
     if (rc != MGPU_OK) return rc;
     w = t_ws;
   }
-  // all chunk descriptors of this render go up in one copy (before any capture)
-  std::vector<JobArgs> all;
-  all.reserve((size_t)ncap);
-  for (auto &wv : waves) all.insert(all.end(), wv.chunks.begin(), wv.chunks.end());
-  MGPU_CUDA(cudaMemcpyAsync(w->jobs, all.data(), all.size() * sizeof(JobArgs), cudaMemcpyHostToDevice, st));
-  MGPU_CUDA(cudaStreamSynchronize(st));  // `all` is pageable and dies at return
+  // (a copy from pageable memory returns once the runtime has staged the source)
+  if (use_graph) {
+    std::vector<JobArgs> all;
+    all.reserve((size_t)ncap);
+    for (auto &wv : waves) all.insert(all.end(), wv.chunks.begin(), wv.chunks.end());
+    MGPU_CUDA(cudaMemcpyAsync(w->jobs, all.data(), all.size() * sizeof(JobArgs), cudaMemcpyHostToDevice, st));
+  }
 
   const bool persist = g_tune.persistent.load() != 0;
   auto kext = persist ? k_extend<COUNT, true> : k_extend<COUNT, false>;
@@ -988,10 +997,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   const int g_bin = device_sm_count() * 4;
   const int bin_ext = g_tune.bin_extension.load(), bin_sh = g_tune.bin_shadow.load();
 
-  bool any_unlimited = false;
-  for (auto &wv : waves) any_unlimited |= wv.unlimited;
   cudaGraph_t graph = nullptr;
-  const bool use_graph = capture && !any_unlimited && !noalloc;
   if (use_graph) MGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
 
   mgpu_render_stats stats{};
@@ -1004,9 +1010,15 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
     const Wave &wv = waves[wi];
     RenderArgs a;
     memset(&a, 0, sizeof(a));
-    a.jobs = w->jobs + job_off;
+    if (use_graph) {
+      a.jobs = w->jobs + job_off;
+      job_off += wv.chunks.size();
+    } else {
+      a.jobs = w->jobs;
+      err = cudaMemcpyAsync(w->jobs, wv.chunks.data(), wv.chunks.size() * sizeof(JobArgs), cudaMemcpyHostToDevice, st);
+      if (err != cudaSuccess) break;
+    }
     a.njobs = (int32_t)wv.chunks.size();
-    job_off += wv.chunks.size();
     a.npaths = wv.npaths;
     a.nslots = wv.nslots;
     a.nl_stride = wv.nl_stride;
