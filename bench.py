@@ -321,6 +321,67 @@ def run_ours(args):
     return 0
 
 
+def run_batched(args):
+    """Batched configuration: 64 seeded scenes of uneven size, 128^2-1024^2, 16 spp each.
+    Times the same requests rendered one after another with mgpu_render (plain) and together in
+    one autotuned, graph-captured batch."""
+    import torch
+
+    from milton_gb300 import autotune
+    from milton_gb300 import pathtracer as pt
+    from milton_gb300 import workloads
+    torch.cuda.set_device(0)
+    specs = workloads.batched_specs(SEED)
+    reqs = []
+    t0 = time.perf_counter()
+    for k, sp in enumerate(specs):
+        s = workloads.build_scene(sp)
+        ds = pt.DeviceScene(s, pt.Accel(s))
+        reqs.append((ds, pt.RenderSettings(sp["width"], sp["height"], sp["spp"], max_depth=MAX_DEPTH,
+                                           rr_start_depth=RR_START, seed=SEED, stream_id=k)))
+    setup_s = time.perf_counter() - t0
+    films = [pt.Film(st.width, st.height) for _, st in reqs]
+    paths = sum(st.width * st.height * st.spp for _, st in reqs)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    def plain():
+        for (ds, st), f in zip(reqs, films):
+            f.clear()
+            pt.render(ds, st, f)
+
+    ms_plain = timed(plain)
+    tuned = autotune.tune(reqs)
+    batch = pt.Batch(wave_paths=tuned["wave_paths"], use_graph=True)
+    for (ds, st), f in zip(reqs, films):
+        batch.add(ds, st, f)
+
+    def batched():
+        for f in films:
+            f.clear()
+        batch.render()
+
+    ms_batch = timed(batched)
+    tris = sum(ds.scene.ntri for ds, _ in reqs)
+    out = {"metric": METRIC, "workload": "batched", "value": paths / ms_batch / 1e3, "unit": UNIT,
+           "plain_value": paths / ms_plain / 1e3, "batched_over_plain": ms_plain / ms_batch,
+           "ms_per_step": ms_batch, "plain_ms_per_step": ms_plain, "steps": args.steps, "warmup": args.warmup,
+           "config": {"scenes": len(reqs), "triangles": tris, "paths_per_step": paths,
+                      "setup_s": round(setup_s, 1), "autotuned": tuned}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_profile_case(args):
     """Small case for ncu captures: the mid scene (~143 MB resident, larger than the 129 MB
     L2) at 512 x 512 x 4 spp = 1,048,576 paths per frame, two frames."""
@@ -349,9 +410,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true", help="small two-frame case for ncu captures")
+    ap.add_argument("--workload", default="mid", choices=["mid", "batched"],
+                    help="mid (default, the benchmark line) or batched (64 scenes, batch vs one-by-one)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)
+    if args.workload == "batched":
+        if args.warmup < 3:
+            args.warmup = 3
+        return run_batched(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
