@@ -928,7 +928,8 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
     int rc = validate(j);
     if (rc != MGPU_OK) return rc;
   }
-  cudaStream_t st = as_stream(stream);
+  cudaStream_t caller = as_stream(stream);
+  cudaStream_t st = caller;
   int32_t nl_max = 1;
   for (const Job &j : jobs)
     nl_max = std::max(nl_max, std::max(1, job_args(j).nl_slots));
@@ -997,8 +998,15 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   const int g_bin = device_sm_count() * 4;
   const int bin_ext = g_tune.bin_extension.load(), bin_sh = g_tune.bin_shadow.load();
 
+  // The launches are captured on a private stream (the caller's may be the legacy default
+  // stream, which cannot capture) and the graph is launched on the caller's stream.
   cudaGraph_t graph = nullptr;
-  if (use_graph) MGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  if (use_graph) {
+    static thread_local cudaStream_t t_capture = nullptr;
+    if (!t_capture) MGPU_CUDA(cudaStreamCreateWithFlags(&t_capture, cudaStreamNonBlocking));
+    st = t_capture;
+    MGPU_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  }
 
   mgpu_render_stats stats{};
   uint64_t launches = 0;
@@ -1096,7 +1104,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
     if (err == cudaSuccess) {
       cudaGraphExec_t exec = nullptr;
       err = cudaGraphInstantiate(&exec, graph, 0);
-      if (err == cudaSuccess) err = cudaGraphLaunch(exec, st);
+      if (err == cudaSuccess) err = cudaGraphLaunch(exec, caller);
       if (exec) cudaGraphExecDestroy(exec);
     }
     if (graph) cudaGraphDestroy(graph);
@@ -1108,7 +1116,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   for (const Job &j : jobs) stats.paths += (uint64_t)j.p.width * j.p.height * (uint64_t)j.p.sample_count;
   stats.kernel_launches = launches;
   t_stats = stats;
-  t_stats_stream = st;
+  t_stats_stream = caller;
   t_stats_dev = w->stats;
   t_counters_dev = w->counters;
   t_stats_pending = true;
