@@ -382,6 +382,111 @@ def run_batched(args):
     return 0
 
 
+def run_serving(args):
+    """Serving configuration: a Poisson request stream (200 req/s) over 8 resident scenes of
+    10k-2M triangles, resolutions {256, 512, 1024, 2048}^2, target spp {1, 16, 64, 256}, each
+    job refined progressively until its film's error estimate is at most 0.01 (or the target
+    spp), admitted by a 120 GB budget.  Reports throughput and p50/p99 time-to-target, and
+    times the same jobs (same final sample counts, hence the same images) rendered one after
+    another with mgpu_render (plain)."""
+    import numpy as np
+    import torch
+
+    from milton_gb300 import pathtracer as pt
+    from milton_gb300 import workloads
+    from milton_gb300.serving import Server, ServerSettings, latency_summary, replay
+    torch.cuda.set_device(0)
+    specs, reqs = workloads.serving_requests(SEED, n=args.requests, rate=args.rate)
+    t0 = time.perf_counter()
+    scenes = [workloads.build_scene(sp) for sp in specs]
+    gen_s = time.perf_counter() - t0
+    settings = ServerSettings(hbm_budget=120_000_000_000, tick_paths=args.tick_paths, use_graph=args.graph)
+    srv = Server(settings)
+    ids = [srv.add_scene(s) for s in scenes]
+    t0 = time.perf_counter()
+    for i in ids:
+        srv.prefetch(i)
+    srv.wait_builds()
+    build_s = time.perf_counter() - t0
+    target_rmse = 0.01
+
+    def make_job(r):
+        st = pt.RenderSettings(r["width"], r["height"], min(r["spp"], 16), max_depth=MAX_DEPTH,
+                               rr_start_depth=RR_START, seed=r["seed"], stream_id=r["id"])
+        cam = workloads.request_camera(scenes[r["scene"]].camera, r["seed"])
+        return ids[r["scene"]], st, cam, r["spp"], target_rmse
+
+    # warm-up: every scene uploaded and the wave workspace allocated before the clock starts
+    warm = [dict(id=10_000 + k, arrival=0.0, scene=k, width=256, height=256, spp=1, seed=k)
+            for k in range(len(scenes))]
+    replay(srv, warm, make_job)
+    s0 = srv.stats()
+    check_ids = {r["id"] for r in reqs[:4]}
+    served_imgs = {}
+
+    def on_done(r, jid, info):
+        if r["id"] in check_ids:
+            served_imgs[r["id"]] = srv.read(jid)
+
+    clocks = Clocks(0)
+    clocks.start()
+    infos, t_start = replay(srv, reqs, on_done=on_done, make_job=make_job)
+    clk = clocks.stop()
+    s1 = srv.stats()
+    paths = s1["paths"] - s0["paths"]
+    busy = s1["render_seconds"] - s0["render_seconds"]
+    t_end = max(v["t_done"] for v in infos.values())
+    lat = latency_summary(infos)
+    srv.close()
+
+    # plain: the same jobs, one after another, each alone with mgpu_render
+    dscenes = [pt.DeviceScene(s, pt.Accel(s)) for s in scenes]
+    jobs = []
+    for r in reqs:
+        info = infos[r["id"]]
+        sid, st, cam, _, _ = make_job(r)
+        st.sample_count = info["spp_done"]
+        jobs.append((r, st, cam))
+    films = {}
+    for r, st, cam in jobs:
+        if (st.width, st.height) not in films:
+            films[(st.width, st.height)] = pt.Film(st.width, st.height)
+    same = []
+    for r, st, cam in jobs:  # warm-up and image check
+        if r["id"] in check_ids:
+            f = films[(st.width, st.height)]
+            f.clear()
+            pt.render(dscenes[r["scene"]], st, f, camera=cam)
+            same.append(bool(np.array_equal(f.mean(), served_imgs[r["id"]])))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for r, st, cam in jobs:
+        f = films[(st.width, st.height)]
+        f.clear()
+        pt.render(dscenes[r["scene"]], st, f, camera=cam)
+    e1.record()
+    torch.cuda.synchronize()
+    plain_s = e0.elapsed_time(e1) / 1e3
+    spp_hist = {}
+    for v in infos.values():
+        spp_hist[v["spp_done"]] = spp_hist.get(v["spp_done"], 0) + 1
+    out = {"metric": METRIC, "workload": "serving", "value": paths / busy / 1e6, "unit": UNIT,
+           "wall_value": paths / (t_end - t_start) / 1e6, "plain_value": paths / plain_s / 1e6,
+           "served_over_plain": plain_s / busy, "latency": lat, "images_equal_plain": same,
+           "clocks": clk,
+           "config": {"requests": len(reqs), "rate_per_s": args.rate, "scenes": len(scenes),
+                      "triangles": [s.ntri for s in scenes], "target_rmse": target_rmse,
+                      "hbm_budget": settings.hbm_budget, "tick_paths": settings.tick_paths,
+                      "use_graph": settings.use_graph, "paths": paths, "busy_s": round(busy, 3),
+                      "wall_s": round(t_end - t_start, 3), "plain_s": round(plain_s, 3),
+                      "peak_resident_bytes": s1["peak_resident_bytes"], "ticks": s1["ticks"] - s0["ticks"],
+                      "spp_done_histogram": {str(k): v for k, v in sorted(spp_hist.items())},
+                      "scene_gen_s": round(gen_s, 1), "kd_build_s": round(build_s, 1)}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_profile_case(args):
     """Small case for ncu captures: the mid scene (~143 MB resident, larger than the 129 MB
     L2) at 512 x 512 x 4 spp = 1,048,576 paths per frame, two frames."""
@@ -410,11 +515,18 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true", help="small two-frame case for ncu captures")
-    ap.add_argument("--workload", default="mid", choices=["mid", "batched"],
-                    help="mid (default, the benchmark line) or batched (64 scenes, batch vs one-by-one)")
+    ap.add_argument("--workload", default="mid", choices=["mid", "batched", "serving"],
+                    help="mid (default, the benchmark line), batched (64 scenes, batch vs one-by-one) or "
+                         "serving (Poisson request stream through the render service)")
+    ap.add_argument("--requests", type=int, default=200, help="serving: requests in the stream")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
+    ap.add_argument("--tick-paths", type=int, default=1 << 25, help="serving: paths per scheduling tick")
+    ap.add_argument("--graph", type=int, default=0, help="serving: capture each tick in a CUDA graph")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)
+    if args.workload == "serving":
+        return run_serving(args)
     if args.workload == "batched":
         if args.warmup < 3:
             args.warmup = 3

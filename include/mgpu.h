@@ -133,6 +133,9 @@ int mgpu_accel_destroy(mgpu_accel *accel);
 int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void *stream, mgpu_scene **out);
 int mgpu_scene_destroy(mgpu_scene *scene);
 int mgpu_scene_bytes(const mgpu_scene *scene, uint64_t *out);
+/* Device bytes mgpu_scene_create would allocate for this accel with nmat materials and nlight
+ * lights (admission against a memory budget before uploading).  No reference counterpart. */
+int mgpu_accel_device_bytes(const mgpu_accel *accel, int32_t nmat, int32_t nlight, uint64_t *out);
 /* Tuning: how many of the breadth-first top 16-byte pairs the traversal kernels stage in
  * shared memory per block (0 = none; clamped to what the builder laid out breadth-first). */
 int mgpu_scene_set_top_pairs(mgpu_scene *scene, uint32_t n);
@@ -148,15 +151,23 @@ int mgpu_trace_any(const mgpu_scene *scene, const float *d_rays, uint8_t *d_occl
 int mgpu_trace_closest_counted(const mgpu_scene *scene, const float *d_rays, float *d_hits, uint32_t *d_counts,
                                int64_t n, void *stream);
 
-/* Film: compensated FP32 sums per pixel (rgb sum, count, rgb compensation).                */
+/* Film: compensated FP32 sums per pixel: (rgb sum, sample count) and (rgb Kahan compensation,
+ * sum of squared per-sample luminance (r+g+b)/3, for variance and error estimates).         */
 typedef struct mgpu_film mgpu_film;
 int mgpu_film_create(int32_t width, int32_t height, void *stream, mgpu_film **out);
 int mgpu_film_clear(mgpu_film *film, void *stream);
 int mgpu_film_destroy(mgpu_film *film);
 /* Per-pixel mean in FP64: out = host array of width*height*3 doubles (synchronises). */
 int mgpu_film_read(mgpu_film *film, double *out_mean, void *stream);
-/* Raw device film: 2 float4 per pixel (sum.rgb + count, compensation.rgb) -> host floats. */
+/* Raw device film: 2 float4 per pixel (sum.rgb + count, compensation.rgb + luminance sum of
+ * squares) -> host floats.                                                                  */
 int mgpu_film_read_raw(mgpu_film *film, float *out8, void *stream);
+/* Error estimate of n films in one pass on the device (synchronises): out_rmse[i] =
+ * sqrt(mean over pixels with >= 2 samples of var_pixel / n_pixel), var_pixel the sample
+ * variance of the per-sample luminance (r+g+b)/3 -- the expected RMSE of the film's mean
+ * luminance against the converged image; +inf if no pixel has 2 samples.  Deterministic.
+ * Progressive refinement's stopping test; no counterpart in the reference.                */
+int mgpu_film_error(mgpu_film *const *films, int32_t n, double *out_rmse, void *stream);
 
 /* PathTracer::render over the requested sample passes (PathTracer.cpp:28-116 per path). */
 int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream);

@@ -1,4 +1,4 @@
-"""ctypes binding of libmgpu.so (include/mgpu.h, include/milton_plugin.h).
+"""ctypes binding of libmgpu.so (include/mgpu.h, include/mgpu_server.h, include/milton_plugin.h).
 
 There is no fallback: if the in-tree library is missing, importing this module raises.
 """
@@ -44,6 +44,26 @@ class RenderParams(C.Structure):
                 ("seed", C.c_uint64), ("stream_id", C.c_uint32), ("camera", C.c_float * 11)]
 
 
+class ServerParams(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("tick_paths", C.c_int64), ("max_active", C.c_int32),
+                ("wave_paths", C.c_int32), ("use_graph", C.c_int32), ("build_threads", C.c_int32),
+                ("kd", KdParams)]
+
+
+class ServerJobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("scene", C.c_int32), ("spp_done", C.c_int32), ("reached_target", C.c_int32),
+                ("rmse", C.c_double), ("t_arrival", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("paths", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = ([(n, C.c_uint64) for n in ("resident_bytes", "peak_resident_bytes", "scene_bytes", "film_bytes",
+                                           "paths", "ticks", "admitted", "finished", "failed", "evictions",
+                                           "uploads", "builds")]
+                + [(n, C.c_int32) for n in ("queued", "active", "resident_scenes", "building")]
+                + [("render_seconds", C.c_double)])
+
+
 class RenderStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("paths", "extension_rays", "shadow_rays", "truncated_paths", "bounces",
                                           "kernel_launches")]
@@ -63,6 +83,7 @@ SIGNATURES = [
     ("mgpu_scene_destroy", C.c_int, [C.c_void_p]),
     ("mgpu_scene_bytes", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("mgpu_scene_set_top_pairs", C.c_int, [C.c_void_p, C.c_uint32]),
+    ("mgpu_accel_device_bytes", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]),
     ("mgpu_trace_closest", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("mgpu_trace_any", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("mgpu_trace_closest_counted", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
@@ -72,6 +93,7 @@ SIGNATURES = [
     ("mgpu_film_destroy", C.c_int, [C.c_void_p]),
     ("mgpu_film_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_film_read_raw", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mgpu_film_error", C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_void_p]),
     ("mgpu_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_batch_create", C.c_int, [C.POINTER(C.c_void_p)]),
@@ -89,6 +111,18 @@ SIGNATURES = [
     ("mgpu_tune_set", C.c_int, [C.c_char_p, C.c_int64]),
     ("mgpu_tune_get", C.c_int, [C.c_char_p, C.POINTER(C.c_int64)]),
     ("mgpu_launch_count", C.c_uint64, []),
+    ("mgpu_server_create", C.c_int, [C.POINTER(ServerParams), C.POINTER(C.c_void_p)]),
+    ("mgpu_server_destroy", C.c_int, [C.c_void_p]),
+    ("mgpu_server_clock", C.c_double, [C.c_void_p]),
+    ("mgpu_server_add_scene", C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_int32)]),
+    ("mgpu_server_prefetch", C.c_int, [C.c_void_p, C.c_int32]),
+    ("mgpu_server_submit", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(RenderParams), C.c_int32, C.c_double,
+                                     C.c_double, C.POINTER(C.c_int64)]),
+    ("mgpu_server_step", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
+    ("mgpu_server_job", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(ServerJobInfo)]),
+    ("mgpu_server_read", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("mgpu_server_release", C.c_int, [C.c_void_p, C.c_int64]),
+    ("mgpu_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
     ("plugin_type", C.c_int, []),
     ("plugin_new", C.c_void_p, []),
     ("plugin_delete", None, [C.c_void_p]),

@@ -82,6 +82,85 @@ static void register_staging(mgpu_accel *a) {
   cudaGetLastError();  // clear a failed registration
 }
 
+// Offsets of the arrays in a scene's one device allocation (256-byte aligned each).
+struct SceneLayout {
+  size_t off_pairs, off_refs, off_tris, off_shade, off_mats, off_lights, off_err, total;
+};
+static SceneLayout scene_layout(const mgpu_accel *a, int32_t nmat, int32_t nlight) {
+  SceneLayout L;
+  L.off_pairs = 0;
+  L.off_refs = align_up(L.off_pairs + a->dpairs.size() * sizeof(Pair), 256);
+  L.off_tris = align_up(L.off_refs + std::max<size_t>(a->ltris.size(), 1) * sizeof(F4), 256);
+  L.off_shade = align_up(L.off_tris + std::max<size_t>(a->tris.size(), 1) * sizeof(F4), 256);
+  L.off_mats = align_up(L.off_shade + std::max<size_t>(a->shade.size(), 1) * sizeof(float4), 256);
+  L.off_lights = align_up(L.off_mats + (size_t)std::max(nmat, 0) * 16 * sizeof(float), 256);
+  L.off_err = align_up(L.off_lights + std::max<size_t>((size_t)std::max(nlight, 0), 1) * 16 * sizeof(float), 256);
+  L.total = L.off_err + 256;
+  return L;
+}
+
+// Film error estimate.  Per pixel with n > 1 samples: the sample variance of the per-sample
+// luminance (r+g+b)/3 from the film's sum and sum of squares, divided by n, is the variance
+// of the pixel's mean; the film's estimate is the square root of its average over those
+// pixels (the expected RMSE of the image against the converged one).  Each film is reduced by
+// kErrBlocks blocks in a fixed order, so the value is deterministic.
+struct FilmRef {
+  const float4 *sum;
+  const float4 *c;
+  int64_t npix;
+};
+constexpr int kErrBlocks = 64, kErrThreads = 256;
+
+__global__ void __launch_bounds__(kErrThreads) k_film_error_partial(const FilmRef *films, double2 *partial) {
+  const FilmRef f = films[blockIdx.y];
+  double acc = 0.0, cnt = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kErrThreads + threadIdx.x; i < f.npix; i += (int64_t)kErrBlocks * kErrThreads) {
+    const float4 S = f.sum[i], C = f.c[i];
+    const double n = S.w;
+    if (n > 1.0) {
+      const double mean = ((((double)S.x - C.x) + ((double)S.y - C.y)) + ((double)S.z - C.z)) / (3.0 * n);
+      const double var = fmax((double)C.w / n - mean * mean, 0.0) * n / (n - 1.0);
+      acc += var / n;
+      cnt += 1.0;
+    }
+  }
+  __shared__ double sa[kErrThreads], sc[kErrThreads];
+  sa[threadIdx.x] = acc;
+  sc[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int w = kErrThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sa[threadIdx.x] += sa[threadIdx.x + w];
+      sc[threadIdx.x] += sc[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * kErrBlocks + blockIdx.x] = make_double2(sa[0], sc[0]);
+}
+
+__global__ void k_film_error_final(const double2 *partial, int32_t n, double *out) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n) return;
+  double a = 0.0, c = 0.0;
+  for (int b = 0; b < kErrBlocks; ++b) {
+    const double2 p = partial[(int64_t)f * kErrBlocks + b];
+    a += p.x;
+    c += p.y;
+  }
+  out[f] = c > 0.0 ? sqrt(a / c) : INFINITY;
+}
+
+// per-thread device scratch of the error estimate (grown as needed, per device)
+struct ErrScratch {
+  int device = -1;
+  size_t bytes = 0;
+  void *d = nullptr;
+  ~ErrScratch() {
+    if (d) cudaFree(d);
+  }
+};
+static thread_local ErrScratch t_err;
+
 }  // namespace mgpu
 
 mgpu_accel::~mgpu_accel() {
@@ -184,20 +263,10 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   const std::vector<Pair> &dpairs = accel->dpairs;
   const std::vector<F4> &ltris = accel->ltris, &tris = accel->tris;
   const std::vector<float4> &shade = accel->shade;
-  size_t off_pairs = 0;
-  size_t sz_pairs = dpairs.size() * sizeof(Pair);
-  size_t off_refs = align_up(off_pairs + sz_pairs, 256);
-  size_t sz_refs = std::max<size_t>(ltris.size(), 1) * sizeof(F4);
-  size_t off_tris = align_up(off_refs + sz_refs, 256);
-  size_t sz_tris = std::max<size_t>(tris.size(), 1) * sizeof(F4);
-  size_t off_shade = align_up(off_tris + sz_tris, 256);
-  size_t sz_shade = std::max<size_t>(shade.size(), 1) * sizeof(float4);
-  size_t off_mats = align_up(off_shade + sz_shade, 256);
-  size_t sz_mats = (size_t)desc->nmat * 16 * sizeof(float);
-  size_t off_lights = align_up(off_mats + sz_mats, 256);
-  size_t sz_lights = std::max<size_t>((size_t)desc->nlight, 1) * 16 * sizeof(float);
-  size_t off_err = align_up(off_lights + sz_lights, 256);
-  size_t total = off_err + 256;
+  const SceneLayout L = scene_layout(accel, desc->nmat, desc->nlight);
+  const size_t off_pairs = L.off_pairs, off_refs = L.off_refs, off_tris = L.off_tris, off_shade = L.off_shade,
+               off_mats = L.off_mats, off_lights = L.off_lights, off_err = L.off_err, total = L.total;
+  const size_t sz_pairs = dpairs.size() * sizeof(Pair), sz_mats = (size_t)desc->nmat * 16 * sizeof(float);
 
   mgpu_scene *s = new (std::nothrow) mgpu_scene();
   if (!s) return fail(MGPU_E_NOMEM, "mgpu_scene_create: out of host memory");
@@ -275,6 +344,12 @@ int mgpu_scene_bytes(const mgpu_scene *s, uint64_t *out) {
   return MGPU_OK;
 }
 
+int mgpu_accel_device_bytes(const mgpu_accel *a, int32_t nmat, int32_t nlight, uint64_t *out) {
+  if (!a || !out || nmat < 0 || nlight < 0) return fail(MGPU_E_INVALID, "mgpu_accel_device_bytes: bad argument");
+  *out = scene_layout(a, nmat, nlight).total;
+  return MGPU_OK;
+}
+
 int mgpu_film_create(int32_t width, int32_t height, void *stream, mgpu_film **out) {
   if (!out || width <= 0 || height <= 0 || (int64_t)width * height > (int64_t)1 << 31)
     return fail(MGPU_E_INVALID, "mgpu_film_create: bad size");
@@ -344,6 +419,50 @@ int mgpu_film_read(mgpu_film *f, double *out_mean, void *stream) {
       out_mean[3 * i + 0] = out_mean[3 * i + 1] = out_mean[3 * i + 2] = 0.0;
     }
   }
+  return MGPU_OK;
+}
+
+int mgpu_film_error(mgpu_film *const *films, int32_t n, double *out_rmse, void *stream) {
+  if (n < 0 || n > 65535 || (n > 0 && (!films || !out_rmse)))
+    return fail(MGPU_E_INVALID, "mgpu_film_error: bad argument");
+  if (n == 0) return MGPU_OK;
+  std::vector<FilmRef> refs((size_t)n);
+  for (int32_t i = 0; i < n; ++i) {
+    if (!films[i]) return fail(MGPU_E_INVALID, "mgpu_film_error: null film");
+    refs[i].sum = films[i]->d_sum;
+    refs[i].c = films[i]->d_c;
+    refs[i].npix = (int64_t)films[i]->width * films[i]->height;
+  }
+  const size_t b_refs = align_up((size_t)n * sizeof(FilmRef), 256);
+  const size_t b_part = align_up((size_t)n * kErrBlocks * sizeof(double2), 256);
+  const size_t need = b_refs + b_part + (size_t)n * sizeof(double);
+  int dev = 0;
+  MGPU_CUDA(cudaGetDevice(&dev));
+  if (t_err.device != dev || t_err.bytes < need) {
+    if (t_err.d) {
+      int cur = dev;
+      if (t_err.device != dev) cudaSetDevice(t_err.device);
+      cudaFree(t_err.d);
+      if (t_err.device != dev) cudaSetDevice(cur);
+      t_err.d = nullptr;
+    }
+    t_err.bytes = 0;
+    MGPU_CUDA(cudaMalloc(&t_err.d, need));
+    t_err.device = dev;
+    t_err.bytes = need;
+  }
+  char *base = (char *)t_err.d;
+  FilmRef *d_refs = (FilmRef *)base;
+  double2 *d_part = (double2 *)(base + b_refs);
+  double *d_out = (double *)(base + b_refs + b_part);
+  cudaStream_t st = as_stream(stream);
+  MGPU_CUDA(cudaMemcpyAsync(d_refs, refs.data(), (size_t)n * sizeof(FilmRef), cudaMemcpyHostToDevice, st));
+  k_film_error_partial<<<dim3(kErrBlocks, n), kErrThreads, 0, st>>>(d_refs, d_part);
+  k_film_error_final<<<(n + 127) / 128, 128, 0, st>>>(d_part, n, d_out);
+  g_launches.fetch_add(2);
+  MGPU_CUDA(cudaGetLastError());
+  MGPU_CUDA(cudaMemcpyAsync(out_rmse, d_out, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MGPU_CUDA(cudaStreamSynchronize(st));
   return MGPU_OK;
 }
 

@@ -569,6 +569,9 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
       float yx = L.x - C.x, tx = S.x + yx; C.x = (tx - S.x) - yx; S.x = tx;
       float yy = L.y - C.y, ty = S.y + yy; C.y = (ty - S.y) - yy; S.y = ty;
       float yz = L.z - C.z, tz = S.z + yz; C.z = (tz - S.z) - yz; S.z = tz;
+      // second moment of the per-sample luminance (variance / error estimates), unfused
+      const float lum = __fmul_rn(__fadd_rn(__fadd_rn(L.x, L.y), L.z), 1.0f / 3.0f);
+      C.w = __fadd_rn(C.w, __fmul_rn(lum, lum));
     }
     S.w += (float)J.ns;
     J.film_sum[pix] = S;

@@ -50,17 +50,24 @@ def reduce_films(raw: np.ndarray, group=None) -> np.ndarray:
 
 def kahan_film(paths_rgb: np.ndarray) -> np.ndarray:
     """Host model of the device film: Kahan-add per-path radiance (H, W, S, 3) in FP32 sample
-    order, as k_accumulate does; returns the raw (2, H, W, 4) float32 film."""
+    order, as k_accumulate does, with the plain FP32 sum of squared luminance (r+g+b)/3;
+    returns the raw (2, H, W, 4) float32 film."""
     h, w, n, _ = paths_rgb.shape
     S = np.zeros((h, w, 3), np.float32)
     C = np.zeros((h, w, 3), np.float32)
+    Q = np.zeros((h, w), np.float32)
+    third = np.float32(1.0 / 3.0)
     for k in range(n):
-        y = paths_rgb[:, :, k, :].astype(np.float32) - C
+        L = paths_rgb[:, :, k, :].astype(np.float32)
+        y = L - C
         t = (S + y).astype(np.float32)
         C = ((t - S).astype(np.float32) - y).astype(np.float32)
         S = t
+        lum = (((L[..., 0] + L[..., 1]).astype(np.float32) + L[..., 2]).astype(np.float32) * third).astype(np.float32)
+        Q = (Q + (lum * lum).astype(np.float32)).astype(np.float32)
     raw = np.zeros((2, h, w, 4), np.float32)
     raw[0, ..., :3] = S
     raw[0, ..., 3] = n
     raw[1, ..., :3] = C
+    raw[1, ..., 3] = Q
     return raw

@@ -134,7 +134,8 @@ class DeviceScene:
 
 
 class Film:
-    """Compensated FP32 film (per pixel: rgb sum + count, rgb Kahan compensation)."""
+    """Compensated FP32 film (per pixel: rgb sum + count, rgb Kahan compensation + sum of
+    squared per-sample luminance)."""
 
     def __init__(self, width: int, height: int, stream=None):
         self._lib = N.load()
@@ -155,6 +156,11 @@ class Film:
         N.check(self._lib.mgpu_film_read_raw(self.handle, N.ptr(out), _stream_handle(stream)))
         return out
 
+    def rmse_estimate(self, stream=None) -> float:
+        """Estimated RMSE of the per-pixel mean luminance: sqrt(mean over pixels of the sample
+        variance / n), from the film's second moment."""
+        return rmse_estimate(self.raw(stream))
+
     def close(self):
         if self.handle:
             self._lib.mgpu_film_destroy(self.handle)
@@ -165,6 +171,28 @@ class Film:
             self.close()
         except Exception:
             pass
+
+
+def rmse_estimate(raw: np.ndarray) -> float:
+    """sqrt(mean_pixels(var / n)) of the per-pixel mean luminance, from a raw film."""
+    s, c = raw[0].astype(np.float64), raw[1].astype(np.float64)
+    n = s[..., 3]
+    ok = n > 1
+    if not ok.any():
+        return float("inf")
+    mean = ((s[..., :3] - c[..., :3]).sum(-1) / 3.0)[ok] / n[ok]
+    m2 = c[..., 3][ok] / n[ok]
+    var = np.maximum(m2 - mean * mean, 0.0) * n[ok] / (n[ok] - 1)
+    return float(np.sqrt(np.mean(var / n[ok])))
+
+
+def film_error(films, stream=None) -> np.ndarray:
+    """mgpu_film_error: the device-side rmse_estimate of several films in one pass."""
+    films = list(films)
+    arr = (C.c_void_p * max(1, len(films)))(*[f.handle.value for f in films])
+    out = np.zeros(max(1, len(films)), np.float64)
+    N.check(N.load().mgpu_film_error(arr, len(films), N.ptr(out), _stream_handle(stream)))
+    return out[:len(films)]
 
 
 @dataclass

@@ -200,7 +200,13 @@ def random_scene(seed: int, target_tris: int) -> Scene:
     n_sph = max(1, target_tris // per_sphere)
     nu = 50 if target_tris >= per_sphere else max(4, int(np.sqrt(target_tris / 2)))
     nv = 26 if target_tris >= per_sphere else max(3, nu // 2)
-    centers, radii = _place_spheres(rng, min(n_sph, 1500), 0.05, 1.0, h)
+    if n_sph > 400:
+        # 400 spheres fill the ground; beyond ~1M triangles they are tessellated finer
+        # (a UV sphere of nu x nv has 2 nu (nv - 1) triangles, nu = 2 (nv - 1))
+        nv = int(round(np.sqrt(target_tris / 400 / 4.0))) + 1
+        nu = 2 * (nv - 1)
+        n_sph = 400
+    centers, radii = _place_spheres(rng, n_sph, 0.05, 1.0, h)
     for k, (c, r) in enumerate(zip(centers, radii)):
         u = rng.uniform()
         if u < 0.6:

@@ -5,7 +5,8 @@
   of 8), 16 spp each, max depth 8, RR from depth 3.
 * serving: Poisson arrivals (seeded exponential gaps) at a given rate; each request picks a scene
   (10k-2M triangles), a resolution from {256, 512, 1024, 2048} and a target spp from
-  {1, 16, 64, 256} uniformly.
+  {1, 16, 64, 256} uniformly, and views its scene from its own camera (the scene's camera
+  turned about the vertical axis by a seeded angle).
 """
 from __future__ import annotations
 
@@ -44,3 +45,16 @@ def serving_requests(seed: int = 0, n: int = 64, rate: float = 200.0, tri_lo: in
         reqs.append(dict(id=k, arrival=t, scene=int(rng.integers(n_scenes)), width=side, height=side,
                          spp=int(rng.choice(spps)), seed=int(rng.integers(1 << 30))))
     return scenes, reqs
+
+
+def request_camera(camera, seed: int, max_turn: float = 0.6) -> np.ndarray:
+    """The scene camera turned about the y axis through the origin by a seeded angle in
+    [-max_turn, max_turn] radians (a per-request view of a shared scene)."""
+    a = np.random.default_rng(seed).uniform(-max_turn, max_turn)
+    c, s = np.cos(a), np.sin(a)
+    R = np.array([[c, 0.0, s], [0.0, 1.0, 0.0], [-s, 0.0, c]])
+    out = np.array(camera, np.float32).copy()
+    out[0:3] = R @ np.asarray(camera[0:3], np.float64)
+    look = R @ np.asarray(camera[3:6], np.float64)
+    out[3:6] = look / np.linalg.norm(look)
+    return out
