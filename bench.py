@@ -17,6 +17,10 @@ Printed JSON line (rank 0):
 
 `--impl reference` times the CPU implementation of the path (the oracle port; Milton itself
 does not build here) on the same workload and prints its own line.
+
+Other workloads (`--workload`): plain (the CPU-runnable 256 x 256 x 16 spp frame, same line
+format, CPU baseline over the whole frame), batched (64 scenes rendered one by one and as one
+batch) and serving (a Poisson request stream through the render service, p50/p99 latency).
 """
 from __future__ import annotations
 
@@ -35,15 +39,40 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Mpaths/s at 1 GB300 at fixed RMSE vs FP64 ref; served p50/p99 latency"
 UNIT = "Mpaths/s"
-W_IMG = H_IMG = 1024
-SPP = 64
-MAX_DEPTH = 8
-RR_START = 3
 SEED = 0
-WORKLOAD = ("mid: 1,000,010 triangles (400 seeded UV spheres x 2,500 tris on a 20x20 ground quad), "
-            "60/30/10% Lambertian/modified-Phong/dielectric(IOR 1.5), 4 quad lights, SAH kd-tree "
-            "(Milton defaults), 1024x1024 px, 64 spp, max depth 8, RR from depth 3, fp32")
-CPU_ROWS = (496, 528)   # bounded CPU sample: 32 centre rows x 1024 px x 64 spp
+# The frame workloads: mid (the benchmark line) and plain (the CPU-runnable configuration).
+CONFIGS = {
+    "mid": dict(scene="mid", width=1024, height=1024, spp=64, max_depth=8, rr_start=3,
+                cpu_rows=(496, 528), ref_rows=8,  # bounded CPU samples: 32 / 8 rows of the frame
+                workload=("mid: 1,000,010 triangles (400 seeded UV spheres x 2,500 tris on a 20x20 ground quad), "
+                          "60/30/10% Lambertian/modified-Phong/dielectric(IOR 1.5), 4 quad lights, SAH kd-tree "
+                          "(Milton defaults), 1024x1024 px, 64 spp, max depth 8, RR from depth 3, fp32")),
+    "plain": dict(scene="plain", width=256, height=256, spp=16, max_depth=5, rr_start=3,
+                  cpu_rows=(0, 256), ref_rows=64,  # the whole frame / a quarter of it per step
+                  workload=("plain: closed box of 5 quads + 2 rotated boxes (34 triangles), one 0.25-area quad "
+                            "light of radiance 15, Lambertian albedos U[0.2, 0.8], 256x256 px, 16 spp, max depth 5, "
+                            "RR from depth 3, 40 degree pinhole, fp32")),
+}
+CFG = CONFIGS["mid"]
+W_IMG = H_IMG = CFG["width"]
+SPP = CFG["spp"]
+MAX_DEPTH = CFG["max_depth"]
+RR_START = CFG["rr_start"]
+WORKLOAD = CFG["workload"]
+CPU_ROWS = CFG["cpu_rows"]
+
+
+def _use_config(name: str) -> None:
+    """Points the frame-workload constants at CONFIGS[name]."""
+    global CFG, W_IMG, H_IMG, SPP, MAX_DEPTH, RR_START, WORKLOAD, CPU_ROWS
+    CFG = CONFIGS[name]
+    W_IMG, H_IMG, SPP = CFG["width"], CFG["height"], CFG["spp"]
+    MAX_DEPTH, RR_START, WORKLOAD, CPU_ROWS = CFG["max_depth"], CFG["rr_start"], CFG["workload"], CFG["cpu_rows"]
+
+
+def _frame_scene():
+    from milton_gb300 import scenegen
+    return scenegen.mid(SEED) if CFG["scene"] == "mid" else scenegen.plain(SEED)
 
 
 def _peaks() -> dict:
@@ -126,16 +155,15 @@ def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    from milton_gb300 import scenegen
-    scene = scenegen.mid(SEED)
+    scene = _frame_scene()
     from oracle import pyoracle
     tree = pyoracle.Tree(scene.tri_v)
     threads = os.cpu_count() or 1
-    rows_per_step = 8
+    rows_per_step = CFG["ref_rows"]
     times = []
     paths_per_step = W_IMG * rows_per_step * SPP
     for k in range(args.warmup + args.steps):
-        r0 = (256 + 8 * k) % (H_IMG - rows_per_step)
+        r0 = (H_IMG // 4 + rows_per_step * k) % (H_IMG - rows_per_step + 1)
         t0 = time.perf_counter()
         pyoracle.render(scene, tree, W_IMG, H_IMG, SPP, max_depth=MAX_DEPTH, rr_start=RR_START, seed=SEED,
                         rows=(r0, r0 + rows_per_step), threads=threads)
@@ -144,8 +172,8 @@ def run_reference(args):
             times.append(dt)
     total = sum(times)
     value = paths_per_step * len(times) / total / 1e6
-    sample = (f"each step: {rows_per_step} rows x {W_IMG} px x {SPP} spp = {paths_per_step} paths of the mid "
-              f"frame (rows advance per step), FP64 oracle port, {threads} threads")
+    sample = (f"each step: {rows_per_step} rows x {W_IMG} px x {SPP} spp = {paths_per_step} paths of the "
+              f"{CFG['scene']} frame (rows advance per step), FP64 oracle port, {threads} threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -173,7 +201,7 @@ def run_ours(args):
     dev = torch.cuda.current_device()
     stream = torch.cuda.current_stream()
 
-    scene = scenegen.mid(SEED)
+    scene = _frame_scene()
     t0 = time.perf_counter()
     accel = pt.Accel(scene)
     build_s = time.perf_counter() - t0
@@ -288,7 +316,7 @@ def run_ours(args):
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene generator, no external assets)",
         "config": {"workload": WORKLOAD, "paths_per_step": paths_per_step,
-                   "l2": "256 MiB buffer written before every step; per-wave path state (~870 MB) exceeds L2 too",
+                   "l2": "a 256 MiB buffer (larger than the 129 MB L2) is written before every step",
                    "parallelism": f"replicas x{ws} (independent sample streams, no collective in the step)",
                    "kd_build_s": round(build_s, 3), "kd_nodes": kst["node_pairs"], "kd_refs": kst["refs"],
                    "rays_per_path": (stats["extension_rays"] + stats["shadow_rays"]) / paths_per_step,
@@ -308,8 +336,9 @@ def run_ours(args):
         rmse = float(np.sqrt(((gpu_rows - cpu["mean"]) ** 2).mean()))
         out["cpu_baseline"] = {
             "value": cpu["mpaths"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
-            "sample": (f"rows {CPU_ROWS[0]}-{CPU_ROWS[1] - 1} of the mid frame (32 x 1024 px x 64 spp = "
-                       f"{cpu['paths']} paths), FP64 oracle, same seed"), "seconds": round(cpu["seconds"], 2)}
+            "sample": (f"rows {CPU_ROWS[0]}-{CPU_ROWS[1] - 1} of the {CFG['scene']} frame "
+                       f"({CPU_ROWS[1] - CPU_ROWS[0]} x {W_IMG} px x {SPP} spp = {cpu['paths']} paths), FP64 oracle, "
+                       "same seed"), "seconds": round(cpu["seconds"], 2)}
         out["parity"] = {"rmse_vs_fp64_same_samples": rmse, "oracle_rows_mean": float(cpu["mean"].mean()),
                          "gpu_rows_mean": float(gpu_rows.mean()),
                          "note": "same seed and counter RNG: paths agree unless FP32 and FP64 take "
@@ -515,12 +544,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true", help="small two-frame case for ncu captures")
-    ap.add_argument("--workload", default="mid", choices=["mid", "batched", "serving"],
-                    help="mid (default, the benchmark line), batched (64 scenes, batch vs one-by-one) or "
-                         "serving (Poisson request stream through the render service)")
+    ap.add_argument("--workload", default="mid", choices=["mid", "plain", "batched", "serving"],
+                    help="mid (default, the benchmark line), plain (the CPU-runnable frame), batched (64 scenes, "
+                         "batch vs one-by-one) or serving (Poisson request stream through the render service)")
     ap.add_argument("--requests", type=int, default=200, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
-    ap.add_argument("--tick-paths", type=int, default=1 << 25, help="serving: paths per scheduling tick")
+    ap.add_argument("--tick-paths", type=int, default=1 << 26, help="serving: paths per scheduling tick")
     ap.add_argument("--graph", type=int, default=0, help="serving: capture each tick in a CUDA graph")
     args = ap.parse_args()
     if args.profile_case:
@@ -533,6 +562,7 @@ def main():
         return run_batched(args)
     if args.warmup < 3:
         args.warmup = 3
+    _use_config("plain" if args.workload == "plain" else "mid")
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

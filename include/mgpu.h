@@ -224,7 +224,8 @@ int mgpu_profile_read(double *ms6, uint64_t *launches6);
 /* Process-wide tuning knobs (results do not depend on them):
  *   "persistent"     0/1  persistent warp-level traversal with per-lane ray refill (default 0)
  *   "bin_shadow"     0/1  counting-sort shadow rays by (light, origin cell) (default 1)
- *   "bin_extension"  0/1  counting-sort extension rays by (direction octant, origin cell) (default 1) */
+ *   "bin_extension"  0/1  counting-sort extension rays by (direction octant, origin cell) (default 1)
+ *   "bin_min_paths"  n    waves of fewer paths are not binned (default 2^22)                   */
 int mgpu_tune_set(const char *key, int64_t value);
 int mgpu_tune_get(const char *key, int64_t *value);
 

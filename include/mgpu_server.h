@@ -18,7 +18,8 @@
  *   2. Rendering: active jobs get sample passes up to the tick's path budget -- first one
  *      sample each, least recently served first, then the rest of the budget oldest job first,
  *      never past a job's next checkpoint -- and the passes of all jobs render together in one
- *      batch (mgpu_batch_*: jobs of different scenes share waves).
+ *      batch (mgpu_batch_*: jobs of different scenes share waves; passes are grouped by
+ *      scene so that a wave touches few trees).
  *   3. Checkpoints: a job's checkpoints are its sample counts c0 = min(spp, max_spp),
  *      c(k+1) = min(2 c(k), max_spp), spp being its stratification (noSuperSamples).  At each,
  *      mgpu_film_error estimates the film's RMSE; the job finishes when the estimate is at most
@@ -48,7 +49,7 @@ typedef struct mgpu_server mgpu_server;
 
 typedef struct {
   uint64_t hbm_budget;   /* device bytes for resident scenes and films; 0 = 120e9 */
-  int64_t tick_paths;    /* paths rendered per tick over all jobs; 0 = 2^25 */
+  int64_t tick_paths;    /* paths rendered per tick over all jobs; 0 = 2^26 */
   int32_t max_active;    /* job slots on the device; 0 = 256 */
   int32_t wave_paths;    /* paths in flight per wave; 0 = automatic */
   int32_t use_graph;     /* capture each tick's launches in one CUDA graph */

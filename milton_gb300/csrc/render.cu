@@ -611,6 +611,9 @@ struct Tuning {
   std::atomic<int> persistent{0};     // persistent warp-level traversal with ray refill
   std::atomic<int> bin_shadow{1};     // counting-sort shadow rays by (light, origin cell)
   std::atomic<int> bin_extension{1};  // counting-sort extension rays by (octant, origin cell)
+  // waves of fewer paths skip binning: sorting a few hundred thousand rays costs more (four
+  // latency-bound launches per bounce) than the coherence it buys
+  std::atomic<int64_t> bin_min_paths{(int64_t)1 << 22};
 };
 static Tuning g_tune;
 
@@ -1000,6 +1003,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   const int g_acc = grid_for((const void *)k_accumulate, 0);
   const int g_bin = device_sm_count() * 4;
   const int bin_ext = g_tune.bin_extension.load(), bin_sh = g_tune.bin_shadow.load();
+  const int64_t bin_min = g_tune.bin_min_paths.load();
 
   // The launches are captured on a private stream (the caller's may be the legacy default
   // stream, which cannot capture) and the graph is launched on the caller's stream.
@@ -1040,8 +1044,8 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
     a.so = w->so; a.sd = w->sd; a.slots = w->slots;
     a.qo_u = w->qo_u; a.qd_u = w->qd_u; a.qt_u = w->qt_u; a.so_u = w->so_u; a.sd_u = w->sd_u;
     a.qkey = w->qkey; a.skey = w->skey;
-    a.bin_ext = bin_ext;
-    a.bin_sh = bin_sh;
+    a.bin_ext = wv.npaths >= bin_min ? bin_ext : 0;
+    a.bin_sh = wv.npaths >= bin_min ? bin_sh : 0;
     a.counters = w->counters;
     a.stats = w->stats;
     a.tcount = w->tcount;
@@ -1274,7 +1278,8 @@ int mgpu_tune_set(const char *key, int64_t value) {
   if (k == "persistent") g_tune.persistent.store(value != 0);
   else if (k == "bin_shadow") g_tune.bin_shadow.store(value != 0);
   else if (k == "bin_extension") g_tune.bin_extension.store(value != 0);
-  else return fail(MGPU_E_INVALID, "mgpu_tune_set: unknown key " + k);
+  else if (k == "bin_min_paths" && value >= 0) g_tune.bin_min_paths.store(value);
+  else return fail(MGPU_E_INVALID, "mgpu_tune_set: unknown key or bad value " + k);
   return MGPU_OK;
 }
 
@@ -1284,6 +1289,7 @@ int mgpu_tune_get(const char *key, int64_t *value) {
   if (k == "persistent") *value = g_tune.persistent.load();
   else if (k == "bin_shadow") *value = g_tune.bin_shadow.load();
   else if (k == "bin_extension") *value = g_tune.bin_extension.load();
+  else if (k == "bin_min_paths") *value = g_tune.bin_min_paths.load();
   else return fail(MGPU_E_INVALID, "mgpu_tune_get: unknown key " + k);
   return MGPU_OK;
 }

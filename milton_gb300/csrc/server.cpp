@@ -303,6 +303,8 @@ void plan(mgpu_server *s, std::vector<Pass> &out) {
   }
   for (size_t i = 0; i < act.size(); ++i)
     if (k[i] > 0) out.push_back({act[i], k[i]});
+  // passes of one scene next to each other: a wave then touches fewer trees (L2 reuse)
+  std::stable_sort(out.begin(), out.end(), [](const Pass &a, const Pass &b) { return a.job->scene < b.job->scene; });
 }
 
 }  // namespace
@@ -317,7 +319,7 @@ int mgpu_server_create(const mgpu_server_params *params, mgpu_server **out) {
   if (!s) return fail(MGPU_E_NOMEM, "mgpu_server_create: out of host memory");
   s->p = *params;
   if (s->p.hbm_budget == 0) s->p.hbm_budget = 120000000000ull;
-  if (s->p.tick_paths == 0) s->p.tick_paths = (int64_t)1 << 25;
+  if (s->p.tick_paths == 0) s->p.tick_paths = (int64_t)1 << 26;
   if (s->p.max_active == 0) s->p.max_active = 256;
   if (s->p.build_threads == 0) s->p.build_threads = 2;
   s->t0 = std::chrono::steady_clock::now();

@@ -29,7 +29,7 @@ JOB_STATES = {0: "queued", 1: "active", 2: "done", 3: "failed"}
 @dataclass
 class ServerSettings:
     hbm_budget: int = 120_000_000_000
-    tick_paths: int = 1 << 25
+    tick_paths: int = 1 << 26
     max_active: int = 256
     wave_paths: int = 0
     use_graph: int = 0

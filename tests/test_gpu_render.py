@@ -104,7 +104,8 @@ def test_tuning_knobs_do_not_change_the_image(cuda):
     ds = pt.DeviceScene(s, acc)
     st = pt.RenderSettings(48, 40, 8, max_depth=6, rr_start_depth=3, seed=4)
     raws = []
-    saved = {k: pt.tune_get(k) for k in ("persistent", "bin_shadow", "bin_extension")}
+    saved = {k: pt.tune_get(k) for k in ("persistent", "bin_shadow", "bin_extension", "bin_min_paths")}
+    pt.tune("bin_min_paths", 0)  # bin even this small wave
     try:
         for persist in (0, 1):
             for bins in ((0, 0), (1, 0), (1, 1)):

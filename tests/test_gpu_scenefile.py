@@ -1,0 +1,36 @@
+"""A Milton scene file (tests/scenes/box.js: unit-plane light, culled planes, a Phong cube, a
+dielectric OBJ mesh) loaded by milton_gb300.sceneloader renders on the GPU like the oracle."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from milton_gb300 import sceneloader
+from gpu_util import gpu_render_paths
+
+pytestmark = pytest.mark.gpu
+HERE = Path(__file__).resolve().parent
+
+
+def test_scene_file_renders_like_the_oracle(cuda, oracle):
+    sf = sceneloader.load(str(HERE / "scenes" / "box.js"))
+    r = sceneloader.path_tracer(sf)
+    st = r.settings()
+    mean_g, paths_g, _ = gpu_render_paths(cuda, sf.scene, st)
+    tree = oracle.Tree(sf.scene.tri_v)
+    mean_o, paths_o, _ = oracle.render(sf.scene, tree, st.width, st.height, st.spp, max_depth=st.max_depth,
+                                       rr_start=st.rr_start_depth, seed=st.seed, per_path=True)
+    close = np.abs(paths_g - paths_o) <= 1e-4 + 2e-3 * np.maximum(np.abs(paths_g), np.abs(paths_o))
+    agree = np.all(close, axis=-1).mean()
+    print(f"scene file: path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
+    assert agree >= 0.97
+    assert mean_g.mean() > 0.01  # the light reaches the film
+
+
+def test_path_tracer_object_from_scene_file(cuda):
+    sf = sceneloader.load(str(HERE / "scenes" / "box.js"))
+    r = sceneloader.path_tracer(sf)
+    r.init()
+    r.render()
+    img = r.output()
+    assert img.shape == (sf.height, sf.width, 3) and np.isfinite(img).all() and img.mean() > 0.01
