@@ -72,7 +72,22 @@ typedef struct {
  *   materials  nmat*16 floats: type, kd[3], ks[3], n, ior, transparency, 0...
  *   lights     nlight*16 floats: center[3], ex[3], ez[3], normal[3], area, Le[3]
  *              (a Milton `Plane` under a transform: getPosition(u,v) = center + (u-.5)ex + (v-.5)ez,
- *               Plane.cpp:91-93; Le = power / (area * pi), Emitter.cpp:34-50)              */
+ *               Plane.cpp:91-93; Le = power / (area * pi), Emitter.cpp:34-50)
+ *   light_ext  NULL (every light is a plane) or nlight*16 floats: type, then per type
+ *              MGPU_LIGHT_PLANE     nothing more
+ *              MGPU_LIGHT_TRIANGLE  uv0[2], a[2], b[2], 1/|a x b|: a Milton `Triangle`, with center =
+ *                                   v1, ex = v2 - v1, ez = v3 - v1 (world), normal its normal, area
+ *                                   its object-space area; the light sample (u, v) lands at
+ *                                   v1 + |c x b| ex / |a x b| + |c x a| ez / |a x b|, c = (u, v) - uv0,
+ *                                   a = uv1 - uv0, b = uv2 - uv0 (Triangle::getPosition,
+ *                                   Triangle.cpp:332-354)
+ *              MGPU_LIGHT_MESH      [8] first triangle, [9] triangle count (uint32 bit patterns): a
+ *                                   Milton `Mesh` emitter over that run of the soup; area = its
+ *                                   world-space area; a sample (u, v) picks triangle floor(u count)
+ *                                   and lands at barycentrics (r1, v, r2) / (r1 + v + r2) with two
+ *                                   more uniforms r1, r2, normal = interpolated vertex normals
+ *                                   (Mesh::getPosition / getPoint, Mesh.cpp:436-448,
+ *                                   MeshTriangle::getPosition, MeshTriangle.cpp:299-333)          */
 typedef struct {
   int64_t ntri;
   const float *tri_v;
@@ -84,7 +99,12 @@ typedef struct {
   const float *materials;
   int32_t nlight;
   const float *lights;
+  const float *light_ext;
 } mgpu_scene_desc;
+
+#define MGPU_LIGHT_PLANE 0
+#define MGPU_LIGHT_TRIANGLE 1
+#define MGPU_LIGHT_MESH 2
 
 /* Render parameters.  Defaults mirror Milton's PathTracer/DirectIllumination keys:
  * noDirectSamples 1, efficientDirect 1, no maximum depth, Russian roulette from depth 2

@@ -34,7 +34,8 @@ class KdStats(C.Structure):
 class SceneDesc(C.Structure):
     _fields_ = [("ntri", C.c_int64), ("tri_v", C.c_void_p), ("tri_n", C.c_void_p), ("tri_mat", C.c_void_p),
                 ("tri_light", C.c_void_p), ("tri_flags", C.c_void_p), ("nmat", C.c_int32),
-                ("materials", C.c_void_p), ("nlight", C.c_int32), ("lights", C.c_void_p)]
+                ("materials", C.c_void_p), ("nlight", C.c_int32), ("lights", C.c_void_p),
+                ("light_ext", C.c_void_p)]
 
 
 class RenderParams(C.Structure):

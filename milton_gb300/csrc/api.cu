@@ -94,7 +94,7 @@ static SceneLayout scene_layout(const mgpu_accel *a, int32_t nmat, int32_t nligh
   L.off_shade = align_up(L.off_tris + std::max<size_t>(a->tris.size(), 1) * sizeof(F4), 256);
   L.off_mats = align_up(L.off_shade + std::max<size_t>(a->shade.size(), 1) * sizeof(float4), 256);
   L.off_lights = align_up(L.off_mats + (size_t)std::max(nmat, 0) * 16 * sizeof(float), 256);
-  L.off_err = align_up(L.off_lights + std::max<size_t>((size_t)std::max(nlight, 0), 1) * 16 * sizeof(float), 256);
+  L.off_err = align_up(L.off_lights + std::max<size_t>((size_t)std::max(nlight, 0), 1) * 32 * sizeof(float), 256);
   L.total = L.off_err + 256;
   return L;
 }
@@ -257,6 +257,23 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     if (!(ty == 0.0f || ty == 1.0f || ty == 2.0f))
       return fail(MGPU_E_INVALID, "mgpu_scene_create: unknown material type at material " + std::to_string(i));
   }
+  // device light records: the 16-float base record, then the 16-float extension
+  std::vector<float> lrec((size_t)std::max(desc->nlight, 0) * 32, 0.0f);
+  for (int i = 0; i < desc->nlight; ++i) {
+    memcpy(&lrec[32 * (size_t)i], desc->lights + 16 * (size_t)i, 16 * sizeof(float));
+    if (!desc->light_ext) continue;
+    const float *x = desc->light_ext + 16 * (size_t)i;
+    memcpy(&lrec[32 * (size_t)i + 16], x, 16 * sizeof(float));
+    if (!(x[0] == 0.0f || x[0] == 1.0f || x[0] == 2.0f))
+      return fail(MGPU_E_INVALID, "mgpu_scene_create: unknown light type at light " + std::to_string(i));
+    if (x[0] == 2.0f) {
+      uint32_t first, count;
+      memcpy(&first, x + 8, 4);
+      memcpy(&count, x + 9, 4);
+      if (count == 0 || (uint64_t)first + count > (uint64_t)T)
+        return fail(MGPU_E_INVALID, "mgpu_scene_create: mesh light " + std::to_string(i) + " has a bad triangle run");
+    }
+  }
   const KdTree &tr = accel->tree;
   mgpu_accel *acc = const_cast<mgpu_accel *>(accel);
   register_staging(acc);
@@ -287,7 +304,7 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   if (e == cudaSuccess) e = up(off_tris, tris.data(), tris.size() * sizeof(F4));
   if (e == cudaSuccess) e = up(off_shade, shade.data(), shade.size() * sizeof(float4));
   if (e == cudaSuccess) e = up(off_mats, desc->materials, sz_mats);
-  if (e == cudaSuccess && desc->nlight > 0) e = up(off_lights, desc->lights, (size_t)desc->nlight * 16 * sizeof(float));
+  if (e == cudaSuccess && desc->nlight > 0) e = up(off_lights, lrec.data(), lrec.size() * sizeof(float));
   if (e == cudaSuccess) e = cudaMemsetAsync(base + off_err, 0, 256, st);
   // materials and lights are the caller's pageable arrays: wait for the copies
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

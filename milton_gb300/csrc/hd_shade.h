@@ -36,14 +36,22 @@ MGPU_HD Material material_from(const float *m) {
 
 MGPU_HD bool is_specular(const Material &m) { return m.type == 2; }
 
-// Quad light = Milton `Plane` under a transform
+// Area light: a Milton `Plane` under a transform (type 0), a standalone `Triangle` (type 1) or
+// a `Mesh` (type 2).  Record: 16 floats (center / v1, ex, ez, normal, area, Le) + 16 extension
+// floats (type, triangle uv frame, mesh triangle run).
+constexpr int kLightPlane = 0, kLightTriangle = 1, kLightMesh = 2;
+constexpr uint32_t kMeshLightBlock = 0x4000u;  // RNG block of a mesh light sample's extra pair
+
 struct Light {
   V3 center, ex, ez, normal;
   float area;
   V3 Le;
+  int type;
+  float u0, v0, ax, ay, bx, by, inv_ab;  // Triangle: uv0, a = uv1 - uv0, b = uv2 - uv0, 1/|a x b|
+  uint32_t first, count;                  // Mesh: triangle run in the soup
 };
 
-MGPU_HD Light light_from(const float *l) {
+MGPU_HD Light light_from(const float *l, const float *x) {
   Light r;
   r.center = v3(l[0], l[1], l[2]);
   r.ex = v3(l[3], l[4], l[5]);
@@ -51,7 +59,43 @@ MGPU_HD Light light_from(const float *l) {
   r.normal = normalize(v3(l[9], l[10], l[11]));
   r.area = l[12];
   r.Le = v3(l[13], l[14], l[15]);
+  r.type = (int)x[0];
+  r.u0 = x[1]; r.v0 = x[2]; r.ax = x[3]; r.ay = x[4]; r.bx = x[5]; r.by = x[6]; r.inv_ab = x[7];
+  r.first = f_bits(x[8]);
+  r.count = f_bits(x[9]);
   return r;
+}
+
+// Shape::getPoint for a light sample (u, v): position and normal.  Plane::getPosition
+// (Plane.cpp:91-93); Triangle::getPosition with its uv frame (Triangle.cpp:332-354: both
+// "barycentrics" are magnitudes of 2-D cross products, so (u, v) outside the uv triangle maps
+// outside the triangle, as in the reference); Mesh::getPosition / MeshTriangle::getPosition
+// (Mesh.cpp:436-448, MeshTriangle.cpp:299-333): triangle floor(u count), barycentrics
+// (r1, v, r2) / (r1 + v + r2).  vert(i, k) / nrm(i, k) read vertex k of soup triangle i.
+template <class Vert, class Nrm>
+MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, Vert vert, Nrm nrm, V3 &p, V3 &n) {
+  if (L.type == kLightTriangle) {
+    const float cx = u - L.u0, cy = v - L.v0;
+    const float pb = fabsf(cx * L.by - cy * L.bx) * L.inv_ab;
+    const float pc = fabsf(cx * L.ay - cy * L.ax) * L.inv_ab;
+    p = L.center + L.ex * pb + L.ez * pc;
+    n = L.normal;
+  } else if (L.type == kLightMesh) {
+    uint32_t k = (uint32_t)floorf(u * (float)L.count);
+    if (k > L.count - 1u) k = L.count - 1u;
+    const uint32_t t = L.first + k;
+    float s = r1 + v + r2;
+    float b0 = 1.0f / 3.0f, b1 = 1.0f / 3.0f, b2 = 1.0f / 3.0f;
+    if (s > 0.0f) {
+      const float is = 1.0f / s;
+      b0 = r1 * is; b1 = v * is; b2 = r2 * is;
+    }
+    p = vert(t, 0) * b0 + vert(t, 1) * b1 + vert(t, 2) * b2;
+    n = normalize(nrm(t, 0) * b0 + nrm(t, 1) * b1 + nrm(t, 2) * b2);
+  } else {
+    p = L.center + L.ex * (u - 0.5f) + L.ez * (v - 0.5f);
+    n = L.normal;
+  }
 }
 
 // Pinhole camera (ThinLensCamera::getWorldRay with aperture 0, ThinLensCamera.cpp:131-135)

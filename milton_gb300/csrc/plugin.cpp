@@ -13,7 +13,7 @@ struct mgpu_renderer {
   std::map<std::string, std::string> props;  // PropertyMap (text values)
   // owned copies of the scene arrays
   int64_t ntri = 0;
-  std::vector<float> v, n, mats, lights;
+  std::vector<float> v, n, mats, lights, light_ext;
   std::vector<int32_t> mat, light;
   std::vector<uint32_t> flags;
   bool has_scene = false, has_n = false, has_light = false, has_flags = false;
@@ -56,6 +56,7 @@ struct mgpu_renderer {
     d.materials = mats.data();
     d.nlight = nlight;
     d.lights = lights.data();
+    d.light_ext = light_ext.empty() ? nullptr : light_ext.data();
     return d;
   }
 };
@@ -109,6 +110,8 @@ int mgpu_renderer_set_scene(mgpu_renderer *r, const mgpu_scene_desc *d) {
   r->nlight = d->nlight;
   if (d->nlight > 0) r->lights.assign(d->lights, d->lights + 16 * (size_t)d->nlight);
   else r->lights.assign(16, 0.0f);
+  if (d->nlight > 0 && d->light_ext) r->light_ext.assign(d->light_ext, d->light_ext + 16 * (size_t)d->nlight);
+  else r->light_ext.clear();
   r->has_scene = true;
   r->initted = false;
   return MGPU_OK;

@@ -140,12 +140,13 @@ __device__ __forceinline__ Material load_mat(const JobArgs &J, int i) {
   return material_from(m);
 }
 
+// light records: 8 float4 each (base record, then the extension)
 __device__ __forceinline__ Light load_light(const JobArgs &J, int i) {
-  float l[16];
+  float l[32];
   float4 *ll = reinterpret_cast<float4 *>(l);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) ll[k] = __ldg(J.lights + 4 * i + k);
-  return light_from(l);
+  for (int k = 0; k < 8; ++k) ll[k] = __ldg(J.lights + 8 * i + k);
+  return light_from(l, l + 16);
 }
 
 // Binning keys (kBins = 4096).  Ray coherence: rays of one warp should start close together
@@ -385,14 +386,31 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
           F4u u = uniforms(J.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
           float ux = ((float)sx + ((k & 1) ? u.c : u.a)) / (float)J.nds_side;
           float uy = ((float)sy + ((k & 1) ? u.d : u.b)) / (float)J.nds_side;
-          V3 lp = lt.center + lt.ex * (ux - 0.5f) + lt.ez * (uy - 0.5f);
+          float r1 = 0.0f, r2 = 0.0f;
+          if (lt.type == kLightMesh) {
+            F4u um = uniforms(J.rng, pid, (uint32_t)depth, kMeshLightBlock + (uint32_t)k);
+            r1 = um.a;
+            r2 = um.b;
+          }
+          V3 lp, ln;
+          light_point(
+              lt, ux, uy, r1, r2,
+              [&](uint32_t t, int c) {
+                const float4 q = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)t + c);
+                return v3(q.x, q.y, q.z);
+              },
+              [&](uint32_t t, int c) {
+                const float4 q = __ldg(J.shade + 3 * (int64_t)t + c);
+                return v3(q.x, q.y, q.z);
+              },
+              lp, ln);
           V3 wo = lp - P;
           float t = length(wo);
           wo = wo * (1.0f / t);
-          float cwo = fabsf(dot(ns, wo)), cwi = fabsf(dot(lt.normal, wo));
+          float cwo = fabsf(dot(ns, wo)), cwi = fabsf(dot(ln, wo));
           V3 fr = bsdf_eval(m, ns, d, wo);
           if (cwo > 0.0f && cwi > 0.0f && nonzero(fr)) {
-            V3 Le = emitted(lt.Le, lt.normal, -wo);
+            V3 Le = emitted(lt.Le, ln, -wo);
             c = mul(thr, mul(fr, Le)) * (cwo * cwi / (t * t) * lt.area * inv_nds);
             if (nonzero(c)) {
               want = true;

@@ -32,7 +32,7 @@ enum SceneState { kIdle = 0, kBuilding = 1, kBuilt = 2, kBuildFailed = 3 };
 
 struct SrvScene {
   int64_t ntri = 0;
-  std::vector<float> v, n, mats, lights;
+  std::vector<float> v, n, mats, lights, light_ext;
   std::vector<int32_t> mat, light;
   std::vector<uint32_t> flags;
   int32_t nmat = 0, nlight = 0;
@@ -59,6 +59,7 @@ struct SrvScene {
     d.materials = mats.data();
     d.nlight = nlight;
     d.lights = lights.empty() ? nullptr : lights.data();
+    d.light_ext = light_ext.empty() ? nullptr : light_ext.data();
     return d;
   }
 };
@@ -378,6 +379,7 @@ int mgpu_server_add_scene(mgpu_server *s, const mgpu_scene_desc *d, int32_t *sce
     sc->mats.assign(d->materials, d->materials + 16 * (size_t)d->nmat);
     sc->nlight = d->nlight;
     if (d->nlight > 0) sc->lights.assign(d->lights, d->lights + 16 * (size_t)d->nlight);
+    if (d->nlight > 0 && d->light_ext) sc->light_ext.assign(d->light_ext, d->light_ext + 16 * (size_t)d->nlight);
   } catch (...) {
     return fail(MGPU_E_NOMEM, "mgpu_server_add_scene: out of host memory");
   }

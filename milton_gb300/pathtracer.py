@@ -47,6 +47,7 @@ def _desc(scene: Scene) -> N.SceneDesc:
     d.nlight = len(scene.lights)
     lights = scene.lights if len(scene.lights) else np.zeros((1, 16), np.float32)
     d.lights = N.ptr(lights)
+    d.light_ext = N.ptr(scene.light_ext) if len(scene.lights) else None
     d._keep = (scene, lights)  # keep buffers alive while the struct is used
     return d
 

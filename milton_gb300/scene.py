@@ -11,6 +11,8 @@ A `Scene` holds exactly what crosses the C ABI (``mgpu_scene_desc``):
                                    (``MeshTriangle``, MeshTriangle.cpp:142-167)
 * ``materials`` (M, 16)   float32  type, kd[3], ks[3], n, ior, transparency, 0...
 * ``lights``    (L, 16)   float32  center[3], ex[3], ez[3], normal[3], area, Le[3]
+* ``light_ext`` (L, 16)   float32  type (0 plane, 1 Triangle, 2 Mesh) and its parameters
+                                   (include/mgpu.h); all zeros = planes
 * ``camera``    (11,)     float32  eye[3], look[3], up[3], heightAngle (deg), aspectRatio
 
 Materials use Milton's keys and defaults (Material.cpp:67-92, DiffuseBSDF.cpp:44-46,
@@ -120,6 +122,7 @@ class Scene:
     camera: np.ndarray
     name: str = "scene"
     shapes: list = field(default_factory=list)  # (name, first triangle, count) in ShapeSet order
+    light_ext: np.ndarray | None = None
 
     def __post_init__(self):
         self.tri_v = np.ascontiguousarray(self.tri_v, np.float32).reshape(-1, 3, 3)
@@ -129,6 +132,11 @@ class Scene:
         self.tri_flags = np.ascontiguousarray(self.tri_flags, np.uint32).reshape(-1)
         self.materials = np.ascontiguousarray(self.materials, np.float32).reshape(-1, 16)
         self.lights = np.ascontiguousarray(self.lights, np.float32).reshape(-1, 16)
+        if self.light_ext is None:
+            self.light_ext = np.zeros((len(self.lights), 16), np.float32)
+        self.light_ext = np.ascontiguousarray(self.light_ext, np.float32).reshape(-1, 16)
+        if len(self.light_ext) != len(self.lights):
+            raise ValueError("light_ext needs one row per light")
         self.camera = np.ascontiguousarray(self.camera, np.float32).reshape(11)
         T = self.tri_v.shape[0]
         for name, arr in (("tri_n", self.tri_n), ("tri_mat", self.tri_mat), ("tri_light", self.tri_light),
@@ -146,7 +154,7 @@ class Scene:
 
     def nbytes(self) -> int:
         return sum(a.nbytes for a in (self.tri_v, self.tri_n, self.tri_mat, self.tri_light, self.tri_flags,
-                                      self.materials, self.lights))
+                                      self.materials, self.lights, self.light_ext))
 
 
 class SceneBuilder:
@@ -156,6 +164,7 @@ class SceneBuilder:
         self.v, self.n, self.mat, self.light, self.flags = [], [], [], [], []
         self.materials: list[np.ndarray] = []
         self.lights: list[np.ndarray] = []
+        self.light_ext: list[np.ndarray] = []
         self.shapes: list[tuple[str, int, int]] = []
         self._ntri = 0
 
@@ -182,8 +191,7 @@ class SceneBuilder:
     def add_quad_light(self, name: str, center, ex, ez, radiance, mat: int) -> int:
         """A quad emitter: light record plus its two (two-sided) triangles."""
         rec = quad_light(center, ex, ez, radiance)
-        self.lights.append(rec)
-        li = len(self.lights) - 1
+        li = self.add_light(rec)
         c = np.asarray(center, np.float32)
         ex = np.asarray(ex, np.float32)
         ez = np.asarray(ez, np.float32)
@@ -201,6 +209,51 @@ class SceneBuilder:
         self.add(name, tris, np.broadcast_to(nrm, (2, 3, 3)), mat, light=li)
         return li
 
+    def add_light(self, rec: np.ndarray, ext: np.ndarray | None = None) -> int:
+        """Appends a light record (and its extension, default: a plane); returns its index."""
+        self.lights.append(np.asarray(rec, np.float32))
+        self.light_ext.append(np.zeros(16, np.float32) if ext is None else np.asarray(ext, np.float32))
+        return len(self.lights) - 1
+
+    def add_triangle_light(self, name: str, v_world, obj_area: float, uvs, normal, radiance, mat: int,
+                           culled: bool = True) -> int:
+        """An emitting Milton `Triangle` (v1, v2, v3 in world space): one culled triangle and its
+        light record (type 1, uv frame from its three uvs; area = its object-space area)."""
+        v = np.asarray(v_world, np.float64).reshape(3, 3)
+        uv = np.asarray(uvs, np.float64).reshape(3, 2)
+        a, b = uv[1] - uv[0], uv[2] - uv[0]
+        cross = abs(a[0] * b[1] - a[1] * b[0])
+        if cross == 0:
+            raise ValueError("degenerate triangle uv frame")
+        rec = np.zeros(16, np.float32)
+        rec[0:3], rec[3:6], rec[6:9] = v[0], v[1] - v[0], v[2] - v[0]
+        rec[9:12] = np.asarray(normal, np.float64) / np.linalg.norm(normal)
+        rec[12] = obj_area
+        rec[13:16] = np.broadcast_to(np.asarray(radiance, np.float64), 3)
+        ext = np.zeros(16, np.float32)
+        ext[0] = 1
+        ext[1:3], ext[3:5], ext[5:7], ext[7] = uv[0], a, b, 1.0 / cross
+        li = self.add_light(rec, ext)
+        self.add(name, v[None], np.broadcast_to(rec[9:12], (1, 3, 3)), mat, light=li, culled=culled)
+        return li
+
+    def add_mesh_light(self, name: str, v_world, n_world, radiance, mat: int) -> int:
+        """An emitting Milton `Mesh`: its two-sided triangles and one light record (type 2) over
+        their run in the soup, area = the world-space area (Mesh::_getSurfaceArea)."""
+        v = np.asarray(v_world, np.float64).reshape(-1, 3, 3)
+        area = 0.5 * float(np.linalg.norm(np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]), axis=1).sum())
+        rec = np.zeros(16, np.float32)
+        rec[9:12] = (0.0, 1.0, 0.0)  # unused: a mesh light's normal is taken per sample
+        rec[12] = area
+        rec[13:16] = np.broadcast_to(np.asarray(radiance, np.float64), 3)
+        ext = np.zeros(16, np.float32)
+        ext[0] = 2
+        ext.view(np.uint32)[8] = self._ntri
+        ext.view(np.uint32)[9] = v.shape[0]
+        li = self.add_light(rec, ext)
+        self.add(name, v, n_world, mat, light=li)
+        return li
+
     def build(self, camera: np.ndarray, name: str = "scene") -> Scene:
         cat = lambda xs, shape, dt: np.concatenate(xs) if xs else np.zeros(shape, dt)  # noqa: E731
         return Scene(
@@ -209,4 +262,5 @@ class SceneBuilder:
             tri_flags=cat(self.flags, (0,), np.uint32),
             materials=np.stack(self.materials) if self.materials else np.zeros((0, 16), np.float32),
             lights=np.stack(self.lights) if self.lights else np.zeros((0, 16), np.float32),
-            camera=camera, name=name, shapes=list(self.shapes))
+            camera=camera, name=name, shapes=list(self.shapes),
+            light_ext=np.stack(self.light_ext) if self.light_ext else np.zeros((0, 16), np.float32))

@@ -29,9 +29,11 @@ which material are kept as the reference has them:
 * A nested "shapeSet" is parsed but its shapes never reach the scene: SceneNodeShape::flatten
   (SceneGraph.cpp:99-133) makes it the active set without adding it to its parent.
 
-What the GPU path cannot render is refused with a SceneFileError naming the element: analytic
-shapes other than planes and cubes (sphere, cylinder, cone, blob, point), emitters on anything
-but a unit plane, omni and environment emitters, thin-lens apertures, textures and bump maps,
+Emitters: a unit plane becomes a parallelogram light, a Triangle a triangle light with its uv
+frame and object-space area, a mesh one mesh light over its triangles (include/mgpu.h,
+``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
+element: analytic shapes other than planes and cubes (sphere, cylinder, cone, blob, point),
+emitting cubes, omni and environment emitters, thin-lens apertures, textures and bump maps,
 per-channel IOR or Phong exponents, instancing.  A "cube" becomes the 12 triangles of
 Milton's unit cube (Cube.cpp), which is the same surface but 12 primitive ids instead of one.
 """
@@ -711,14 +713,14 @@ class _Loader:
         _properties(req, v, props)
         if t == "plane" and "vertices" in props:
             d = np.array(props["vertices"], np.float64).reshape(4, 3)
-            self.begin(_Node("shape", _Shape("triangle", {"v": d[[0, 1, 2]]})))
+            self.begin(_Node("shape", _Shape("triangle", {"v": d[[0, 1, 2]], "uvs": (0, 0, 0, 1, 1, 1)})))
             self.end()
-            node = _Node("shape", _Shape("triangle", {"v": d[[0, 2, 3]]}))
+            node = _Node("shape", _Shape("triangle", {"v": d[[0, 2, 3]], "uvs": (0, 0, 1, 1, 1, 0)}))
         elif t == "plane":
             node = _Node("shape", _Shape("plane"))
         elif t == "triangle":
             verts = np.array(props.get("vertices", (0, 0, 0, 0, 0, 0.5, 0.5, 0, 0)), np.float64).reshape(3, 3)
-            node = _Node("shape", _Shape("triangle", {"v": verts}))
+            node = _Node("shape", _Shape("triangle", {"v": verts, "uvs": props.get("uvs", (0, 0, 1, 0, 0, 1))}))
         elif t == "cube":
             node = _Node("shape", _Shape("cube"))
         else:  # mesh
@@ -1000,24 +1002,42 @@ class _Flattener:
                 power = np.broadcast_to(np.asarray(props.get("power", (1.0, 1.0, 1.0)), np.float64), 3)
                 rec = S.quad_light(center, ex, ez, power / (area * math.pi))
                 rec[9:12] = nrm  # emitting side: the transformed +y (inverse transpose)
-                self.b.lights.append(rec)
-                li = len(self.b.lights) - 1
+                li = self.b.add_light(rec)
             else:
                 li = -1
             tris = np.array([corners[[0, 3, 2]], corners[[0, 2, 1]]], np.float64)
             self.b.add(name, tris, np.broadcast_to(nrm, (2, 3, 3)), mi, light=li)
             return
-        if emitter != "null":
-            raise SceneFileError(f"an emitting {sh.kind} is not supported by the GPU path (emitters must be "
-                                 "unit planes under a transform)")
+        power = np.broadcast_to(np.asarray(props.get("power", (1.0, 1.0, 1.0)), np.float64), 3)
         if sh.kind == "triangle":
-            v = _xf_points(m, sh.data["v"])
-            n_obj = np.cross(sh.data["v"][1] - sh.data["v"][0], sh.data["v"][2] - sh.data["v"][0])
+            vo = sh.data["v"]
+            v = _xf_points(m, vo)
+            n_obj = np.cross(vo[1] - vo[0], vo[2] - vo[0])
             nrm = _xf_normals(m, [n_obj / np.linalg.norm(n_obj)])[0]
-            if np.linalg.det(m[:3, :3]) < 0:
-                v = v[[0, 2, 1]]  # culling follows the object-space winding
-            self.b.add(name, v[None], np.broadcast_to(nrm, (1, 3, 3)), mi, culled=True)
-        elif sh.kind == "cube":
+            vi = v[[0, 2, 1]] if np.linalg.det(m[:3, :3]) < 0 else v  # culling follows the object-space winding
+            li = -1
+            if emitter == "oriented":
+                # Triangle::_getSurfaceArea is the object-space area (Triangle.cpp:356-362)
+                obj_area = 0.5 * float(np.linalg.norm(n_obj))
+                uv = np.asarray(sh.data["uvs"], np.float64).reshape(3, 2)
+                a, b = uv[1] - uv[0], uv[2] - uv[0]
+                cross = abs(a[0] * b[1] - a[1] * b[0])
+                if cross == 0:
+                    raise SceneFileError("an emitting triangle needs a non-degenerate uv frame")
+                rec = np.zeros(16, np.float32)
+                rec[0:3], rec[3:6], rec[6:9], rec[9:12] = v[0], v[1] - v[0], v[2] - v[0], nrm
+                rec[12] = obj_area
+                rec[13:16] = power / (obj_area * math.pi)
+                ext = np.zeros(16, np.float32)
+                ext[0] = 1
+                ext[1:3], ext[3:5], ext[5:7], ext[7] = uv[0], a, b, 1.0 / cross
+                li = self.b.add_light(rec, ext)
+            self.b.add(name, vi[None], np.broadcast_to(nrm, (1, 3, 3)), mi, light=li, culled=True)
+            return
+        if emitter != "null" and sh.kind != "mesh":
+            raise SceneFileError(f"an emitting {sh.kind} is not supported by the GPU path (emitters must be "
+                                 "planes, triangles or meshes)")
+        if sh.kind == "cube":
             tris, nrms = [], []
             for n_obj, q in _CUBE_FACES:
                 q = _xf_points(m, q)
@@ -1032,7 +1052,12 @@ class _Flattener:
             vw = _xf_points(m, verts)
             inv = np.linalg.inv(m)
             nw = normals @ inv[:3, :3]  # not normalised: interpolated, then normalised per hit
-            self.b.add(sh.data["path"], vw[faces], nw[nfaces], mi)
+            if emitter == "oriented":
+                tv = vw[faces]
+                area = 0.5 * float(np.linalg.norm(np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0]), axis=1).sum())
+                self.b.add_mesh_light(sh.data["path"], tv, nw[nfaces], power / (area * math.pi), mi)
+            else:
+                self.b.add(sh.data["path"], vw[faces], nw[nfaces], mi)
 
 
 def material_record(props: dict) -> np.ndarray:

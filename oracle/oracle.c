@@ -25,6 +25,8 @@
  *                          M/renderers/generators/JitteredSampleGenerator.cpp:19-39, M/core/Viewport.h:29-37
  *   estimator              M/renderers/renderers/PathTracer.cpp:28-116
  *   direct lighting        M/renderers/DirectIllumination.cpp:46-138, M/shapes/Plane.cpp:91-105
+ *   light sample points    M/shapes/Shape.cpp:52-64, M/shapes/Triangle.cpp:332-362,
+ *                          M/shapes/Mesh.cpp:419-465, M/shapes/MeshTriangle.cpp:299-333
  *   BSDFs                  M/materials/bsdfs/DiffuseBSDF.cpp:21-48,
  *                          M/materials/bsdfs/ModifiedPhongBSDF.cpp:48-181,
  *                          M/materials/bsdfs/DielectricBSDF.cpp:48-157, M/materials/bsdfs/Fresnel.h:45-90,
@@ -139,10 +141,16 @@ typedef struct {
   double kd[3], ks[3], n, ior, transparency;
 } orc_mat;
 
+/* Area light: Milton Plane (type 0), Triangle (1) or Mesh (2) emitter.  Triangle: center = v1,
+ * ex = v2 - v1, ez = v3 - v1, uv frame (uv0, a, b, 1/|a x b|).  Mesh: triangle run [first,
+ * first + count) of the soup. */
 typedef struct {
   v3 center, ex, ez, normal;
   double area;
   double Le[3];
+  int type;
+  double u0, v0, ax, ay, bx, by, inv_ab;
+  int64_t first, count;
 } orc_light;
 
 typedef struct {
@@ -618,7 +626,7 @@ static int kd_any(const orc_scene *s, const orc_tree *tr, v3 o, v3 d, double cli
  * light record (16 floats): center[3], ex[3], ez[3], normal[3], area, Le[3]   */
 static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n, const int32_t *mat,
                                     const int32_t *light, const uint32_t *flags, int nmat, const float *mats,
-                                    int nlight, const float *lights) {
+                                    int nlight, const float *lights, const float *light_ext) {
   orc_scene *s = (orc_scene *)calloc(1, sizeof(orc_scene));
   s->ntri = ntri; s->v = v; s->n = n; s->mat = mat; s->light = light; s->flags = flags;
   s->nmat = nmat;
@@ -641,6 +649,19 @@ static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n
     s->lights[i].normal = vnorm(V(l[9], l[10], l[11]));
     s->lights[i].area = l[12];
     for (int k = 0; k < 3; ++k) s->lights[i].Le[k] = l[13 + k];
+    if (light_ext) {
+      const float *x = light_ext + i * 16;
+      uint32_t first, count;
+      memcpy(&first, x + 8, 4);
+      memcpy(&count, x + 9, 4);
+      s->lights[i].type = (int)x[0];
+      s->lights[i].u0 = x[1]; s->lights[i].v0 = x[2];
+      s->lights[i].ax = x[3]; s->lights[i].ay = x[4];
+      s->lights[i].bx = x[5]; s->lights[i].by = x[6];
+      s->lights[i].inv_ab = x[7];
+      s->lights[i].first = first;
+      s->lights[i].count = count;
+    }
   }
   return s;
 }
@@ -951,6 +972,40 @@ static v3 shading_normal(const orc_scene *s, int64_t tri, v3 p) {
   return vnorm(n);
 }
 
+/* Shape::getPoint for light sample m at (u, v) (Shape.cpp:52-64): Plane::getPosition
+ * (Plane.cpp:91-93); Triangle::getPosition (Triangle.cpp:332-354), whose "barycentrics" are
+ * magnitudes of 2-D cross products in the triangle's uv frame; Mesh::getPosition / getPoint
+ * (Mesh.cpp:436-448) with MeshTriangle::getPosition (MeshTriangle.cpp:299-333): triangle
+ * min(floor(u n), n - 1), barycentrics (r1, v, r2) / (r1 + v + r2) with two more uniforms (the
+ * reference draws them from its global generator; here block 0x4000 + m of the path's stream),
+ * normal = the interpolated vertex normals (Mesh::_getGeometricNormal, Mesh.cpp:419-433). */
+static void light_point(const orc_render_ctx *c, const orc_path *ph, int depth, int m, const orc_light *L, double u,
+                        double v, v3 *pos, v3 *nrm) {
+  const orc_scene *s = c->s;
+  if (L->type == 1) {
+    double cx = u - L->u0, cy = v - L->v0;
+    double pb = fabs(cx * L->by - cy * L->bx) * L->inv_ab;
+    double pc = fabs(cx * L->ay - cy * L->ax) * L->inv_ab;
+    *pos = vadd(vadd(L->center, vmul(L->ex, pb)), vmul(L->ez, pc));
+    *nrm = L->normal;
+  } else if (L->type == 2) {
+    double u4[4];
+    orc_u4(&c->rng, ph->path, (uint32_t)depth, 0x4000u + (uint32_t)m, u4);
+    int64_t k = (int64_t)floor(u * (double)L->count);
+    if (k > L->count - 1) k = L->count - 1;
+    int64_t t = L->first + k;
+    double r1 = u4[0], r2 = u4[1];
+    double sum = r1 + v + r2;
+    double b0 = 1.0 / 3, b1 = 1.0 / 3, b2 = 1.0 / 3;
+    if (sum > 0) { b0 = r1 / sum; b1 = v / sum; b2 = r2 / sum; }
+    *pos = vadd(vadd(vmul(tri_vert(s, t, 0), b0), vmul(tri_vert(s, t, 1), b1)), vmul(tri_vert(s, t, 2), b2));
+    *nrm = vnorm(vadd(vadd(vmul(tri_nrm(s, t, 0), b0), vmul(tri_nrm(s, t, 1), b1)), vmul(tri_nrm(s, t, 2), b2)));
+  } else {
+    *pos = vadd(vadd(L->center, vmul(L->ex, u - 0.5)), vmul(L->ez, v - 0.5));
+    *nrm = L->normal;
+  }
+}
+
 static void direct_light(const orc_render_ctx *c, orc_path *ph, int depth, v3 p, const orc_bsdf *b, int light_self,
                          double out[3]) {
   const orc_scene *s = c->s;
@@ -969,19 +1024,20 @@ static void direct_light(const orc_render_ctx *c, orc_path *ph, int depth, v3 p,
         orc_u4(&c->rng, ph->path, (uint32_t)depth, 1u + (uint32_t)(m >> 1), u4);
         double ux = (sx + u4[2 * (m & 1)]) / side;
         double uy = (sy + u4[2 * (m & 1) + 1]) / side;
-        v3 lp = vadd(vadd(L->center, vmul(L->ex, ux - 0.5)), vmul(L->ez, uy - 0.5));
+        v3 lp, ln;
+        light_point(c, ph, depth, m, L, ux, uy, &lp, &ln);
         v3 wo = vsub(lp, p);
         double t = vlen(wo);
         wo = vmul(wo, 1.0 / t);
         double cwo = fabs(vdot(b->ns, wo));
-        double cwi = fabs(vdot(L->normal, vneg(wo)));
+        double cwi = fabs(vdot(ln, vneg(wo)));
         double fr[3];
         bsdf_eval(b, wo, fr);
         if (cwo > 0 && cwi > 0 && (fr[0] != 0 || fr[1] != 0 || fr[2] != 0)) {
           ph->rays_shadow++;
           /* Scene::intersects(ray, t - EPS) -> ShapeSet/kd intersects(ray, t - 2 EPS) */
           if (!kd_any(s, c->tr, p, wo, t - 2 * ORC_EPS, NULL)) {
-            double le = vdot(L->normal, vneg(wo)) > 0 ? 1.0 : 0.0;
+            double le = vdot(ln, vneg(wo)) > 0 ? 1.0 : 0.0;
             for (int k = 0; k < 3; ++k) dir[k] += (fr[k] * L->Le[k] * le * cwo * cwi) / (t * t);
           }
         }
@@ -1118,9 +1174,9 @@ static void *render_thread(void *arg) {
  * with its own counter-based random numbers, so the result does not depend on nthreads.     */
 int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat, const int32_t *light,
                const uint32_t *flags, int nmat, const float *mats, int nlight, const float *lights,
-               const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed, uint32_t stream,
-               double *film_sum, double *path_out, uint64_t *stats_out) {
-  orc_scene *s = scene_from_arrays(ntri, v, n, mat, light, flags, nmat, mats, nlight, lights);
+               const float *light_ext, const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed,
+               uint32_t stream, double *film_sum, double *path_out, uint64_t *stats_out) {
+  orc_scene *s = scene_from_arrays(ntri, v, n, mat, light, flags, nmat, mats, nlight, lights, light_ext);
   orc_render_ctx c;
   c.s = s;
   c.tr = tr;

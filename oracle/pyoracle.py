@@ -33,7 +33,8 @@ def load() -> C.CDLL:
     lib.orc_trace_closest.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, vp]
     lib.orc_trace_any.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp]
     lib.orc_render.restype = C.c_int
-    lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, u64, u32, vp, vp, vp]
+    lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, u64, u32, vp, vp,
+                               vp]
     lib.orc_philox4x32_10.argtypes = [vp, vp, vp]
     lib.orc_camera_dir.argtypes = [vp, C.c_double, C.c_double, vp]
     lib.orc_bsdf_sample.restype = C.c_int
@@ -129,9 +130,11 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
     paths = np.zeros((height * width * sample_count, 3), np.float64) if per_path else None
     st = np.zeros(4, np.uint64)
     lights = scene.lights if len(scene.lights) else np.zeros((1, 16), np.float32)
+    ext = getattr(scene, "light_ext", None)
+    ext = np.ascontiguousarray(ext, np.float32) if ext is not None and len(ext) else None
     lib.orc_render(scene.ntri, _p(scene.tri_v), _p(scene.tri_n), _p(scene.tri_mat), _p(scene.tri_light),
                    _p(scene.tri_flags), len(scene.materials), _p(scene.materials), len(scene.lights), _p(lights),
-                   tree.h, _p(scene.camera), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
+                   _p(ext), tree.h, _p(scene.camera), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
     mean = film[r0:r1] / max(sample_count, 1)
     if per_path:
         paths = paths.reshape(height, width, sample_count, 3)[r0:r1]

@@ -33,6 +33,7 @@ def hostcheck():
     lib.hc_bsdf_eval.argtypes = [vp, vp, vp, vp, vp]
     lib.hc_uniforms.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, vp]
     lib.hc_offset.argtypes = [vp, vp, vp]
+    lib.hc_light_point.argtypes = [vp, vp, vp, vp, vp, vp]
     return lib
 
 

@@ -1,5 +1,6 @@
-"""A Milton scene file (tests/scenes/box.js: unit-plane light, culled planes, a Phong cube, a
-dielectric OBJ mesh) loaded by milton_gb300.sceneloader renders on the GPU like the oracle."""
+"""Milton scene files loaded by milton_gb300.sceneloader render on the GPU like the oracle:
+tests/scenes/box.js (unit-plane light, culled planes, a Phong cube, a dielectric OBJ mesh) and
+tests/scenes/emitters.js (triangle, mesh and plane lights)."""
 from pathlib import Path
 
 import numpy as np
@@ -12,17 +13,20 @@ pytestmark = pytest.mark.gpu
 HERE = Path(__file__).resolve().parent
 
 
-def test_scene_file_renders_like_the_oracle(cuda, oracle):
-    sf = sceneloader.load(str(HERE / "scenes" / "box.js"))
+@pytest.mark.parametrize("name", ["box.js", "emitters.js"])
+def test_scene_file_renders_like_the_oracle(cuda, oracle, name):
+    # emitters.js: plane, triangle (two uv frames) and mesh lights, 4 light samples per vertex
+    sf = sceneloader.load(str(HERE / "scenes" / name))
     r = sceneloader.path_tracer(sf)
     st = r.settings()
     mean_g, paths_g, _ = gpu_render_paths(cuda, sf.scene, st)
     tree = oracle.Tree(sf.scene.tri_v)
-    mean_o, paths_o, _ = oracle.render(sf.scene, tree, st.width, st.height, st.spp, max_depth=st.max_depth,
-                                       rr_start=st.rr_start_depth, seed=st.seed, per_path=True)
+    mean_o, paths_o, _ = oracle.render(sf.scene, tree, st.width, st.height, st.spp, nds=st.no_direct_samples,
+                                       max_depth=st.max_depth, rr_start=st.rr_start_depth, seed=st.seed,
+                                       per_path=True)
     close = np.abs(paths_g - paths_o) <= 1e-4 + 2e-3 * np.maximum(np.abs(paths_g), np.abs(paths_o))
     agree = np.all(close, axis=-1).mean()
-    print(f"scene file: path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
+    print(f"{name}: path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
     assert agree >= 0.97
     assert mean_g.mean() > 0.01  # the light reaches the film
 

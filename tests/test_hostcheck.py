@@ -109,3 +109,43 @@ def test_offset_moves_off_the_surface(hostcheck):
         out = np.zeros(3, np.float32)
         hostcheck.hc_offset(p.ctypes.data, n.ctypes.data, out.ctypes.data)
         assert float((out.astype(np.float64) - p) @ n) > 0
+
+
+def test_light_point_types(hostcheck):
+    """light_point (shared by the GPU kernels) against the reference's formulas, restated here
+    in FP64: Plane::getPosition, Triangle::getPosition (uv frame, magnitudes of 2-D cross
+    products) and Mesh::getPosition (triangle floor(u n), barycentrics (r1, v, r2) / sum)."""
+    from pathlib import Path
+    from milton_gb300 import sceneloader as L
+    sf = L.load(str(Path(__file__).resolve().parent / "scenes" / "emitters.js"))
+    s = sf.scene
+    rng = np.random.default_rng(5)
+    tv = np.ascontiguousarray(s.tri_v, np.float32)
+    tn = np.ascontiguousarray(s.tri_n, np.float32)
+    for li in range(len(s.lights)):
+        rec, ext = s.lights[li], s.light_ext[li]
+        for _ in range(50):
+            uvr = rng.uniform(0, 1, 4).astype(np.float32)
+            out = np.zeros(6, np.float32)
+            hostcheck.hc_light_point(_p(rec), _p(ext), _p(uvr), _p(tv), _p(tn), _p(out))
+            u, v, r1, r2 = (float(x) for x in uvr)
+            kind = int(ext[0])
+            if kind == 0:
+                p = rec[0:3] + rec[3:6] * (u - 0.5) + rec[6:9] * (v - 0.5)
+                n = rec[9:12]
+            elif kind == 1:
+                c = np.array([u - ext[1], v - ext[2]], np.float64)
+                a, b = ext[3:5].astype(np.float64), ext[5:7].astype(np.float64)
+                pb = abs(c[0] * b[1] - c[1] * b[0]) * ext[7]
+                pc = abs(c[0] * a[1] - c[1] * a[0]) * ext[7]
+                p = rec[0:3] + rec[3:6] * pb + rec[6:9] * pc
+                n = rec[9:12]
+            else:
+                first, count = ext.view(np.uint32)[8:10]
+                t = first + min(int(np.floor(u * count)), count - 1)
+                bary = np.array([r1, v, r2]) / (r1 + v + r2)
+                p = bary @ s.tri_v[t].astype(np.float64)
+                n = bary @ s.tri_n[t].astype(np.float64)
+                n = n / np.linalg.norm(n)
+            assert np.allclose(out[:3], p, atol=1e-5), (li, kind)
+            assert np.allclose(out[3:], n / np.linalg.norm(n), atol=1e-5), (li, kind)

@@ -161,7 +161,7 @@ def test_camera_defaults_and_output_size():
 
 @pytest.mark.parametrize("body,extra,msg", [
     ('"sphere" : { "radius" : 1 }', "", "not a triangle shape"),
-    ('"material" : { "emitter" : { "type" : "oriented", "power" : 1 }, "triangle" : { } }', "", "emitting triangle"),
+    ('"material" : { "emitter" : { "type" : "oriented", "power" : 1 }, "cube" : { } }', "", "emitting cube"),
     ('"transform" : { "translate" : [0, 0, 0], "name" : "x", "plane" : { } }', "", "unknown key"),
     ('"triangle" : { }', '"camera" : { "type" : "thinlens" },', "thin-lens"),
     ('"triangle" : { }', '"renderer" : { "type" : "pathTracer" }, "renderer" : { "type" : "pathTracer" },',
@@ -201,3 +201,23 @@ def test_reference_cornell_box_file():
     assert np.allclose(rec[13:16], np.array([2e6, 2e6, 1.6e6]) / (140 * 125 * math.pi), rtol=1e-6)
     assert np.allclose(rec[9:12], [0, -1, 0], atol=1e-6)
     assert sf.renderer["type"] == "preview" and sf.renderer["noSuperSamples"] == 1024
+
+
+def test_triangle_and_mesh_emitters():
+    sf = L.load(str(HERE / "scenes" / "emitters.js"))
+    s = sf.scene
+    ext = s.light_ext
+    kinds = ext[:, 0].astype(int).tolist()
+    # in flatten order: the ceiling's two Triangles, the triangle shape, the mesh, the unit plane
+    assert kinds == [1, 1, 1, 2, 0]
+    # ceiling triangles: object-space area 0.18 each, uv frames of Milton's plane split
+    assert np.allclose(s.lights[0:2, 12], 0.18) and np.allclose(ext[0, 1:8], [0, 0, 0, 1, 1, 1, 1])
+    assert np.allclose(ext[1, 1:8], [0, 0, 1, 1, 1, 0, 1])
+    assert np.allclose(s.lights[0, 13:16], np.array([3, 3, 2.5]) / (0.18 * math.pi))
+    # the mesh light covers its 8 triangles, area = world-space area of the scaled octahedron
+    first, count = ext[3].view(np.uint32)[8:10]
+    assert count == 8 and np.all(s.tri_light[first:first + count] == 3)
+    oct_area = 8 * 0.5 * np.linalg.norm(np.cross([-1, 1, 0], [-1, 0, 1])) * 0.25 ** 2
+    assert s.lights[3, 12] == pytest.approx(oct_area, rel=1e-6)
+    # every emitting triangle points at its light record
+    assert sorted(set(s.tri_light.tolist()) - {-1}) == [0, 1, 2, 3, 4]
