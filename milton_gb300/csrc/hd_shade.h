@@ -72,14 +72,18 @@ MGPU_HD Light light_from(const float *l, const float *x) {
 // outside the triangle, as in the reference); Mesh::getPosition / MeshTriangle::getPosition
 // (Mesh.cpp:436-448, MeshTriangle.cpp:299-333): triangle floor(u count), barycentrics
 // (r1, v, r2) / (r1 + v + r2).  vert(i, k) / nrm(i, k) read vertex k of soup triangle i.
+// n is the emitter's normal at p (a mesh's interpolated vertex normals), g the normal of the
+// surface p lies on (unoriented), for moving the shadow ray's end off it.
 template <class Vert, class Nrm>
-MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, Vert vert, Nrm nrm, V3 &p, V3 &n) {
+MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, Vert vert, Nrm nrm, V3 &p, V3 &n,
+                         V3 &g) {
   if (L.type == kLightTriangle) {
     const float cx = u - L.u0, cy = v - L.v0;
     const float pb = fabsf(cx * L.by - cy * L.bx) * L.inv_ab;
     const float pc = fabsf(cx * L.ay - cy * L.ax) * L.inv_ab;
     p = L.center + L.ex * pb + L.ez * pc;
     n = L.normal;
+    g = L.normal;
   } else if (L.type == kLightMesh) {
     uint32_t k = (uint32_t)floorf(u * (float)L.count);
     if (k > L.count - 1u) k = L.count - 1u;
@@ -90,11 +94,14 @@ MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, V
       const float is = 1.0f / s;
       b0 = r1 * is; b1 = v * is; b2 = r2 * is;
     }
-    p = vert(t, 0) * b0 + vert(t, 1) * b1 + vert(t, 2) * b2;
+    const V3 a = vert(t, 0), b = vert(t, 1), c = vert(t, 2);
+    p = a * b0 + b * b1 + c * b2;
     n = normalize(nrm(t, 0) * b0 + nrm(t, 1) * b1 + nrm(t, 2) * b2);
+    g = normalize(cross(b - a, c - a));
   } else {
     p = L.center + L.ex * (u - 0.5f) + L.ez * (v - 0.5f);
     n = L.normal;
+    g = L.normal;
   }
 }
 

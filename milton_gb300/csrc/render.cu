@@ -39,7 +39,6 @@ constexpr int kCtrFetchExt = 2 * (kHardCap + 8);   // work counters of the persi
 constexpr int kCtrFetchSh = 3 * (kHardCap + 8);    // ... and of the persistent shadow kernel
 constexpr int kCtrTrunc = 4 * (kHardCap + 8);
 constexpr int kNumCounters = kCtrTrunc + 8;
-constexpr float kShadowMargin = 1e-4f;  // shadow rays stop this fraction short of the light
 constexpr int kBins = 4096;             // queue binning keys
 
 // One job chunk of a wave (device memory).
@@ -392,7 +391,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
             r1 = um.a;
             r2 = um.b;
           }
-          V3 lp, ln;
+          V3 lp, ln, lg;
           light_point(
               lt, ux, uy, r1, r2,
               [&](uint32_t t, int c) {
@@ -403,7 +402,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
                 const float4 q = __ldg(J.shade + 3 * (int64_t)t + c);
                 return v3(q.x, q.y, q.z);
               },
-              lp, ln);
+              lp, ln, lg);
           V3 wo = lp - P;
           float t = length(wo);
           wo = wo * (1.0f / t);
@@ -414,9 +413,16 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
             c = mul(thr, mul(fr, Le)) * (cwo * cwi / (t * t) * lt.area * inv_nds);
             if (nonzero(c)) {
               want = true;
+              // both ends of the shadow segment are moved off their surfaces toward each other
+              // (Wachter and Binder), so that neither the shading point's nor the light's own
+              // surface can occlude it, however grazing the direction
               V3 org = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
+              V3 tgt = offset_origin(lp, dot(lg, wo) < 0.0f ? lg : -lg);
+              V3 sdir = tgt - org;
+              const float sl = length(sdir);
+              sdir = sdir * (1.0f / sl);
               so4 = make_float4(org.x, org.y, org.z, __uint_as_float((uint32_t)(p * a.nl_stride + k)));
-              sd4 = make_float4(wo.x, wo.y, wo.z, t * (1.0f - kShadowMargin));
+              sd4 = make_float4(sdir.x, sdir.y, sdir.z, sl);
             }
           }
         }

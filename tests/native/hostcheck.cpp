@@ -110,11 +110,12 @@ void hc_offset(const float *p, const float *n, float *out) {
 void hc_light_point(const float *rec16, const float *ext16, const float *uvr, const float *tri_v, const float *tri_n,
                     float *out) {
   Light L = light_from(rec16, ext16);
-  V3 p, n;
+  V3 p, n, g;
   light_point(
       L, uvr[0], uvr[1], uvr[2], uvr[3],
       [&](uint32_t t, int c) { const float *q = tri_v + 9 * (size_t)t + 3 * c; return v3(q[0], q[1], q[2]); },
-      [&](uint32_t t, int c) { const float *q = tri_n + 9 * (size_t)t + 3 * c; return v3(q[0], q[1], q[2]); }, p, n);
+      [&](uint32_t t, int c) { const float *q = tri_n + 9 * (size_t)t + 3 * c; return v3(q[0], q[1], q[2]); }, p, n,
+      g);
   out[0] = p.x; out[1] = p.y; out[2] = p.z;
   out[3] = n.x; out[4] = n.y; out[5] = n.z;
 }
