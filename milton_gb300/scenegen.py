@@ -9,6 +9,11 @@
              materials 60% Lambertian / 30% modified Phong (n ~ U[10, 200], kd + ks <= 1) / 10%
              dielectric (IOR 1.5); 4 quad lights; 1024x1024, 64 spp, depth 8.
 * ``batch``  many independent scenes of uneven size built from the same recipes.
+* ``large``  a displaced-grid terrain (fBm heights; 2,800 x 2,800 cells = 15,680,000 triangles
+             by default: a 4096^2 vertex grid would be 33.5 M triangles, above the configuration's
+             stated ~20 M total) plus 2,000 copied UV spheres of 2,160 triangles resting on it
+             (4,320,000 triangles; modified Phong or dielectric), 16 quad lights in a 4 x 4 grid;
+             about 20 M triangles; rendered at 2048x2048, 128 spp, depth 16.
 
 Every generator is a pure function of its seed (numpy PCG64).
 """
@@ -229,3 +234,77 @@ def random_scene(seed: int, target_tris: int) -> Scene:
                          (0.0, 0.0, -2.0), 10.0, lm)
     cam = camera(eye=(0.0, 6.0, 15.0), focus=(0.0, 0.0, 0.0), height_angle=40.0, aspect=1.0)
     return b.build(cam, name=f"random{seed}")
+
+
+def _fbm(x, z, rng, octaves: int = 7):
+    """Fractional Brownian motion heights: a sum of octaves of randomly phased, randomly
+    oriented sinusoid pairs, amplitude halving and frequency doubling per octave."""
+    h = np.zeros(np.broadcast(x, z).shape, np.float64)
+    amp, freq = 1.0, 0.05
+    for _ in range(octaves):
+        for _ in range(3):
+            a = rng.uniform(0, 2 * np.pi)
+            ph = rng.uniform(0, 2 * np.pi, 2)
+            u = np.cos(a) * x + np.sin(a) * z
+            w = -np.sin(a) * x + np.cos(a) * z
+            h += amp * np.sin(freq * u * 2 * np.pi + ph[0]) * np.cos(freq * w * 2 * np.pi + ph[1]) / 3.0
+        amp *= 0.5
+        freq *= 2.0
+    return h
+
+
+def large(seed: int = 0, cells: int = 2800, n_objects: int = 2000, extent: float = 100.0, height: float = 6.0,
+          obj_nu: int = 40, obj_nv: int = 28, n_lights: int = 16) -> Scene:
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    # terrain: (cells + 1)^2 vertices over [-extent/2, extent/2]^2, two triangles per cell
+    g = np.linspace(-extent / 2, extent / 2, cells + 1)
+    X, Z = np.meshgrid(g, g, indexing="ij")
+    Y = height * _fbm(X, Z, rng)
+    P = np.stack([X, Y, Z], -1)
+    # vertex normals from central differences of the height field
+    dx = extent / cells
+    gy, gx = np.gradient(Y, dx, dx)
+    N = np.stack([-gy, np.ones_like(Y), -gx], -1)
+    N /= np.linalg.norm(N, axis=-1, keepdims=True)
+    i, j = np.meshgrid(np.arange(cells), np.arange(cells), indexing="ij")
+    a, bb, c, d = (i, j), (i + 1, j), (i + 1, j + 1), (i, j + 1)
+    t1 = np.stack([P[a], P[d], P[c]], -2)
+    n1 = np.stack([N[a], N[d], N[c]], -2)
+    t2 = np.stack([P[a], P[c], P[bb]], -2)
+    n2 = np.stack([N[a], N[c], N[bb]], -2)
+    tv = np.stack([t1, t2], 2).reshape(-1, 3, 3).astype(np.float32)
+    tn = np.stack([n1, n2], 2).reshape(-1, 3, 3).astype(np.float32)
+    del t1, t2, n1, n2, P, N
+    gm = b.material(diffuse(rng.uniform(0.3, 0.6, 3)))
+    b.add("terrain", tv, tn, gm)
+    del tv, tn
+    # 2,000 copied objects (glossy or dielectric spheres) resting on the terrain
+    def height_at(x, z):
+        fi = (x + extent / 2) / dx
+        fj = (z + extent / 2) / dx
+        i0 = np.clip(np.floor(fi).astype(int), 0, cells - 1)
+        j0 = np.clip(np.floor(fj).astype(int), 0, cells - 1)
+        return Y[i0:i0 + 2, j0:j0 + 2].max()
+    mats = [b.material(phong(rng.uniform(0.05, 0.4, 3), rng.uniform(0.2, 0.5, 3), rng.uniform(20, 300)))
+            for _ in range(16)] + [b.material(dielectric(1.5))]
+    placed = np.zeros((0, 3))
+    for k in range(n_objects):
+        for _ in range(1000):  # no two objects overlap
+            r = float(np.exp(rng.uniform(np.log(0.3), np.log(1.5))))
+            x, z = rng.uniform(-extent / 2 + 2, extent / 2 - 2, 2)
+            if not len(placed) or np.all((placed[:, 0] - x) ** 2 + (placed[:, 1] - z) ** 2 > (placed[:, 2] + r) ** 2):
+                break
+        placed = np.vstack([placed, (x, z, r)])
+        y = float(height_at(x, z)) + r
+        m = mats[-1] if rng.uniform() < 0.3 else mats[int(rng.integers(16))]
+        tris, nrm = _uv_sphere_fast((x, y, z), r, obj_nu, obj_nv)
+        b.add(f"object{k}", tris, nrm, m)
+    lm = b.material(diffuse(0.0))
+    side = int(round(np.sqrt(n_lights)))
+    for li in range(n_lights):
+        cx = (li % side + 0.5) / side * extent * 0.8 - extent * 0.4
+        cz = (li // side + 0.5) / side * extent * 0.8 - extent * 0.4
+        b.add_quad_light(f"light{li}", (cx, 40.0, cz), (4.0, 0.0, 0.0), (0.0, 0.0, -4.0), 40.0, lm)
+    cam = camera(eye=(0.0, 35.0, 75.0), focus=(0.0, 0.0, 0.0), height_angle=45.0, aspect=1.0)
+    return b.build(cam, name="large")
