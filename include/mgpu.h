@@ -109,7 +109,9 @@ typedef struct {
 /* Render parameters.  Defaults mirror Milton's PathTracer/DirectIllumination keys:
  * noDirectSamples 1, efficientDirect 1, no maximum depth, Russian roulette from depth 2
  * (PathTracer.cpp:88-89).  max_depth > 0 caps the number of path vertices.
- * camera: eye[3], look[3] (unit), up[3], heightAngle (degrees), aspectRatio (ThinLensCamera).
+ * camera: eye[3], look[3] (unit), up[3], heightAngle (degrees), aspectRatio, then the thin lens:
+ * aperture (metres; 0 = pinhole), focal length, focal distance, and two unused floats
+ * (ThinLensCamera, ThinLensCamera.cpp:62-175).
  * Sample passes [sample_begin, sample_begin + sample_count) of spp are rendered and added to
  * the film (progressive refinement = further calls with later passes).                    */
 typedef struct {
@@ -124,7 +126,7 @@ typedef struct {
   int32_t wave_paths;     /* paths in flight per wave; 0 = automatic */
   uint64_t seed;
   uint32_t stream_id;     /* decorrelates independent replicas / jobs */
-  float camera[11];
+  float camera[16];
 } mgpu_render_params;
 
 typedef struct {

@@ -51,6 +51,10 @@ int mgpu_renderer_get_value(mgpu_renderer *r, const char *key, char *buf, size_t
 int mgpu_renderer_set_scene(mgpu_renderer *r, const mgpu_scene_desc *desc);
 /* Renderer::setCamera: eye[3], look[3], up[3], heightAngle, aspectRatio */
 int mgpu_renderer_set_camera(mgpu_renderer *r, const float *camera11);
+/* ThinLensCamera's lens (ThinLensCamera.cpp:88-124): aperture in metres (0 = pinhole, the
+ * PinholeCamera), focal length = fstop x aperture, focal distance (autofocus resolved by the
+ * caller).  Default: pinhole.                                                              */
+int mgpu_renderer_set_lens(mgpu_renderer *r, float aperture, float focal_length, float focal_distance);
 /* PointSampleRenderer::setOutput: film size */
 int mgpu_renderer_set_output(mgpu_renderer *r, int32_t width, int32_t height);
 /* Renderer::init: builds the kd-tree and makes the scene resident on the current device */

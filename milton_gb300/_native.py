@@ -42,7 +42,7 @@ class RenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("sample_begin", C.c_int32),
                 ("sample_count", C.c_int32), ("no_direct_samples", C.c_int32), ("max_depth", C.c_int32),
                 ("rr_start_depth", C.c_int32), ("efficient_direct", C.c_int32), ("wave_paths", C.c_int32),
-                ("seed", C.c_uint64), ("stream_id", C.c_uint32), ("camera", C.c_float * 11)]
+                ("seed", C.c_uint64), ("stream_id", C.c_uint32), ("camera", C.c_float * 16)]
 
 
 class ServerParams(C.Structure):
@@ -131,6 +131,7 @@ SIGNATURES = [
     ("mgpu_renderer_get_value", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_size_t]),
     ("mgpu_renderer_set_scene", C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
     ("mgpu_renderer_set_camera", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("mgpu_renderer_set_lens", C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float]),
     ("mgpu_renderer_set_output", C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     ("mgpu_renderer_init", C.c_int, [C.c_void_p]),
     ("mgpu_renderer_render", C.c_int, [C.c_void_p]),

@@ -109,7 +109,7 @@ MGPU_HD F4u uniforms(const Rng &g, uint64_t path, uint32_t depth, uint32_t block
 
 // dimension map shared with the oracle
 constexpr uint32_t kDepthJitter = 0xFFFFu;   // path = pixel * side^2 + stratum: {jx, jy}
-constexpr uint32_t kDepthPathInit = 0xFFFEu; // path = global path id: {ior index}
+constexpr uint32_t kDepthPathInit = 0xFFFEu; // path = global path id: {ior index, lens e1, lens e2}
 // depth d, block 0: {bsdf0, bsdf1, bsdf2, rr};  depth d, block 1 + m/2: NEE sample m
 
 }  // namespace mgpu

@@ -109,11 +109,32 @@ MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, V
 struct Camera {
   V3 eye, u, v, n;
   float tan_w, tan_h;
+  float aperture, focal_len, focal_dist;  // thin lens (aperture 0 = pinhole)
 };
 
 MGPU_HD V3 camera_dir(const Camera &c, float x, float y) {
   float nx = 2.0f * x - 1.0f, ny = 1.0f - 2.0f * y;
   return normalize(c.u * (c.tan_w * nx) + c.v * (c.tan_h * ny) - c.n);
+}
+
+// ThinLensCamera::getWorldRay (ThinLensCamera.cpp:131-175): the pinhole direction through the
+// film point; with an aperture, the ray is refocused through the point where it meets the
+// focal plane, from an origin shifted by r = cofRadius sin(e1) at angle e2 on the lens
+// (e1 = u1 pi/2, e2 = u2 2 pi: the reference's radius distribution, not a uniform disc).
+MGPU_HD void camera_ray(const Camera &c, float x, float y, float u1, float u2, V3 &o, V3 &d) {
+  d = camera_dir(c, x, y);
+  o = c.eye;
+  if (c.aperture > 0.0f) {
+    const float t = c.focal_dist / -dot(d, c.n);
+    if (t == c.focal_len) return;
+    const V3 focus = c.eye + d * t;
+    const float l_image = c.focal_len * t / (t - c.focal_len);
+    const float cof = c.aperture * (l_image - c.focal_dist) / l_image;
+    const float r = cof * sinf(u1 * (0.5f * kPi));
+    const float e2 = u2 * (2.0f * kPi);
+    o = c.eye + c.u * (r * cosf(e2)) + c.v * (r * sinf(e2));
+    d = normalize(focus - o);
+  }
 }
 
 // Vector::getOrthonormalBasis (Vector.inl:527-538)

@@ -18,7 +18,7 @@ struct mgpu_renderer {
   std::vector<uint32_t> flags;
   bool has_scene = false, has_n = false, has_light = false, has_flags = false;
   int32_t nmat = 0, nlight = 0;
-  float camera[11] = {0, 0, 0, 0, 0, -1, 0, 1, 0, 45, 1};
+  float camera[16] = {0, 0, 0, 0, 0, -1, 0, 1, 0, 45, 1, 0, 0, 1, 0, 0};
   int32_t width = 0, height = 0;
   mgpu_accel *accel = nullptr;
   mgpu_scene *scene = nullptr;
@@ -119,7 +119,17 @@ int mgpu_renderer_set_scene(mgpu_renderer *r, const mgpu_scene_desc *d) {
 
 int mgpu_renderer_set_camera(mgpu_renderer *r, const float *c) {
   if (!r || !c) return bad("mgpu_renderer_set_camera: null argument");
-  memcpy(r->camera, c, sizeof(r->camera));
+  memcpy(r->camera, c, 11 * sizeof(float));  // the lens stays as mgpu_renderer_set_lens left it
+  return MGPU_OK;
+}
+
+int mgpu_renderer_set_lens(mgpu_renderer *r, float aperture, float focal_length, float focal_distance) {
+  if (!r) return bad("mgpu_renderer_set_lens: null renderer");
+  if (!(aperture >= 0.0f) || (aperture > 0.0f && !(focal_distance > 0.0f && focal_length > 0.0f)))
+    return bad("mgpu_renderer_set_lens: aperture must be >= 0, focal length and distance > 0");
+  r->camera[11] = aperture;
+  r->camera[12] = focal_length;
+  r->camera[13] = focal_distance;
   return MGPU_OK;
 }
 

@@ -207,8 +207,9 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
         F4u ui = uniforms(J.rng, pid, kDepthPathInit, 0);
         uint32_t ior = min((uint32_t)(ui.a * 3.0f), 2u);
         flags = ior;
-        V3 d = camera_dir(J.cam, px, py);
-        o4 = make_float4(J.cam.eye.x, J.cam.eye.y, J.cam.eye.z, __int_as_float((int)p));
+        V3 o, d;
+        camera_ray(J.cam, px, py, ui.b, ui.c, o, d);
+        o4 = make_float4(o.x, o.y, o.z, __int_as_float((int)p));
         d4 = make_float4(d.x, d.y, d.z, __int_as_float(j));
       }
       a.path_L[p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(flags));
@@ -822,6 +823,9 @@ static Camera make_camera(const float *c) {
   k.n = v3((float)n[0], (float)n[1], (float)n[2]);
   k.tan_w = (float)tw;
   k.tan_h = (float)th;
+  k.aperture = c[11];
+  k.focal_len = c[12];
+  k.focal_dist = c[13];
   return k;
 }
 
@@ -843,6 +847,10 @@ static int validate(const Job &j) {
     return fail(MGPU_E_INVALID, "mgpu_render: bad parameters");
   if ((int64_t)rp->sample_begin + rp->sample_count > (int64_t)1 << 30)
     return fail(MGPU_E_INVALID, "mgpu_render: sample range too large");
+  if (!(rp->camera[11] >= 0.0f) ||
+      (rp->camera[11] > 0.0f && !(rp->camera[12] > 0.0f && rp->camera[13] > 0.0f)))
+    return fail(MGPU_E_INVALID, "mgpu_render: a thin lens needs focal length and focal distance > 0 "
+                                "(resolve autofocus before rendering)");
   int nds_side = std::max(1, (int)sqrt((double)rp->no_direct_samples));
   if ((int64_t)j.scene->nlight * nds_side * nds_side > 4096)
     return fail(MGPU_E_INVALID, "mgpu_render: too many light samples per vertex");

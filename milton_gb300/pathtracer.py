@@ -196,6 +196,37 @@ def film_error(films, stream=None) -> np.ndarray:
     return out[:len(films)]
 
 
+def resolve_autofocus(camera: np.ndarray, dscene: "DeviceScene", stream=None) -> np.ndarray:
+    """ThinLensCamera's autofocus (ThinLensCamera.cpp:97-121).  A camera whose focal distance
+    is negative asks for it: the ray through focal point (camera[14], camera[15]) -- taken, as
+    in the reference, at (p - 0.5) in film coordinates, half the offset a pixel ray uses -- is
+    traced on the device, and its hit distance becomes the focal distance; on a miss the
+    fallback |camera[13]| (the focalDistance key, default 1) is kept.  Returns the camera."""
+    cam = np.array(camera, np.float32).reshape(-1)
+    if cam.shape[0] < 16 or not (cam[11] > 0 and cam[13] < 0):
+        return cam
+    eye, look, up = (cam[0:3].astype(np.float64), cam[3:6].astype(np.float64), cam[6:9].astype(np.float64))
+    n = -look
+    u = np.cross(up, n)
+    n /= np.linalg.norm(n)
+    u /= np.linalg.norm(u)
+    v = np.cross(n, u)
+    th = np.tan(np.radians(float(cam[9])) / 2)
+    tw = float(cam[10]) * th
+    fx = np.clip(cam[14], 0, 1) - 0.5
+    fy = 0.5 - np.clip(cam[15], 0, 1)
+    d = u * (tw * fx) + v * (th * fy) - n
+    d /= np.linalg.norm(d)
+    import torch
+    rays = torch.tensor([[*eye, 0.0, *d, float("inf")]], dtype=torch.float32, device="cuda")
+    hits = trace_closest(dscene, rays, stream=stream)
+    torch.cuda.synchronize()
+    t = float(hits[0, 0].item())
+    cam[13] = t if np.isfinite(t) and t > 0 else -cam[13]
+    cam[14] = cam[15] = 0.0
+    return cam
+
+
 @dataclass
 class RenderSettings:
     width: int
@@ -220,8 +251,9 @@ class RenderSettings:
         p.max_depth, p.rr_start_depth = self.max_depth, self.rr_start_depth
         p.efficient_direct, p.wave_paths = self.efficient_direct, self.wave_paths
         p.seed, p.stream_id = self.seed, self.stream_id
-        for i in range(11):
-            p.camera[i] = float(camera[i])
+        cam = np.asarray(camera, np.float32).reshape(-1)
+        for i in range(16):
+            p.camera[i] = float(cam[i]) if i < cam.shape[0] else 0.0
         return p
 
 
@@ -370,6 +402,7 @@ class PathTracer:
         self._accel = None
         self._dscene = None
         self._film = None
+        self._camera = None
 
     # PropertyMap::getValue(key, default)
     def get(self, key, default):
@@ -401,12 +434,13 @@ class PathTracer:
         self._accel = Accel(self.scene, self.kd_settings())
         self._dscene = DeviceScene(self.scene, self._accel)
         self._film = Film(self.width, self.height)
+        self._camera = resolve_autofocus(self.scene.camera, self._dscene)
 
     def render(self, stream=None):
         if self._dscene is None:
             raise RuntimeError("PathTracer.render: init() has not been called")
         self._film.clear(stream)
-        render(self._dscene, self.settings(), self._film, stream=stream)
+        render(self._dscene, self.settings(), self._film, camera=self._camera, stream=stream)
 
     def output(self) -> np.ndarray:
         return self._film.mean()

@@ -36,6 +36,7 @@ class DynamicRenderer:
         N.check(self.lib.mgpu_renderer_set_scene(self.handle, C.byref(d)))
         cam = np.ascontiguousarray(scene.camera, np.float32)
         N.check(self.lib.mgpu_renderer_set_camera(self.handle, cam.ctypes.data))
+        N.check(self.lib.mgpu_renderer_set_lens(self.handle, float(cam[11]), float(cam[12]), float(cam[13])))
 
     def set_output(self, width: int, height: int) -> None:
         self.width, self.height = width, height

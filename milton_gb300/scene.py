@@ -13,7 +13,8 @@ A `Scene` holds exactly what crosses the C ABI (``mgpu_scene_desc``):
 * ``lights``    (L, 16)   float32  center[3], ex[3], ez[3], normal[3], area, Le[3]
 * ``light_ext`` (L, 16)   float32  type (0 plane, 1 Triangle, 2 Mesh) and its parameters
                                    (include/mgpu.h); all zeros = planes
-* ``camera``    (11,)     float32  eye[3], look[3], up[3], heightAngle (deg), aspectRatio
+* ``camera``    (16,)     float32  eye[3], look[3], up[3], heightAngle (deg), aspectRatio, aperture (m),
+                                   focal length, focal distance, 0, 0 (aperture 0 = pinhole)
 
 Materials use Milton's keys and defaults (Material.cpp:67-92, DiffuseBSDF.cpp:44-46,
 ModifiedPhongBSDF.cpp:48-81, DielectricBSDF.cpp:48-53): diffuse ``kd`` (0.5), Phong ``kd``/
@@ -94,19 +95,22 @@ def light_power(radiance, area) -> float:
     return float(radiance) * np.pi * float(area)
 
 
-def camera(eye, focus=None, look=None, up=(0, 1, 0), height_angle=45.0, aspect=1.0) -> np.ndarray:
-    """ThinLensCamera keys: eye, focus or look, up, heightAngle, aspectRatio."""
+def camera(eye, focus=None, look=None, up=(0, 1, 0), height_angle=45.0, aspect=1.0, aperture=0.0,
+           focal_length=0.0, focal_distance=1.0) -> np.ndarray:
+    """ThinLensCamera keys: eye, focus or look, up, heightAngle, aspectRatio; aperture in metres
+    (0 = pinhole), focal length (fstop x aperture) and focal distance for the thin lens."""
     eye = np.asarray(eye, np.float64)
     if look is None:
         look = np.asarray(focus if focus is not None else (0, 0, 0), np.float64) - eye
     look = np.asarray(look, np.float64)
     look = look / np.linalg.norm(look)
-    c = np.zeros(11, np.float32)
+    c = np.zeros(16, np.float32)
     c[0:3] = eye
     c[3:6] = look
     c[6:9] = up
     c[9] = height_angle
     c[10] = aspect
+    c[11], c[12], c[13] = aperture, focal_length, focal_distance
     return c
 
 
@@ -137,7 +141,11 @@ class Scene:
         self.light_ext = np.ascontiguousarray(self.light_ext, np.float32).reshape(-1, 16)
         if len(self.light_ext) != len(self.lights):
             raise ValueError("light_ext needs one row per light")
-        self.camera = np.ascontiguousarray(self.camera, np.float32).reshape(11)
+        cam = np.ascontiguousarray(self.camera, np.float32).reshape(-1)
+        if cam.shape[0] not in (11, 16):
+            raise ValueError("camera needs 11 (pinhole) or 16 (thin lens) floats")
+        self.camera = np.zeros(16, np.float32)
+        self.camera[:cam.shape[0]] = cam
         T = self.tri_v.shape[0]
         for name, arr in (("tri_n", self.tri_n), ("tri_mat", self.tri_mat), ("tri_light", self.tri_light),
                           ("tri_flags", self.tri_flags)):

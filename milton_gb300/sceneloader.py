@@ -33,8 +33,9 @@ Emitters: a unit plane becomes a parallelogram light, a Triangle a triangle ligh
 frame and object-space area, a mesh one mesh light over its triangles (include/mgpu.h,
 ``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
 element: analytic shapes other than planes and cubes (sphere, cylinder, cone, blob, point),
-emitting cubes, omni and environment emitters, thin-lens apertures, textures and bump maps,
-per-channel IOR or Phong exponents, instancing.  A "cube" becomes the 12 triangles of
+emitting cubes, omni and environment emitters, textures and bump maps, per-channel IOR or
+Phong exponents, instancing.  A thin-lens camera keeps its aperture, f-stop and focal distance;
+its autofocus is resolved against the resident scene (pathtracer.resolve_autofocus).  A "cube" becomes the 12 triangles of
 Milton's unit cube (Cube.cpp), which is the same surface but 12 primitive ids instead of one.
 """
 from __future__ import annotations
@@ -1106,9 +1107,6 @@ def material_record(props: dict) -> np.ndarray:
 def camera_record(props: dict, width: int, height: int) -> np.ndarray:
     """ThinLensCamera::init (ThinLensCamera.cpp:62-86, 241-259): defaults eye (2, 2, 2), look
     toward focus (default origin), up = the default camera's v axis."""
-    # PinholeCamera::init forces aperture 0 (PinholeCamera.cpp); a thin lens defaults to 35 mm
-    if props.get("type") == "thinlens" and props.get("aperture", 35.0) != 0:
-        raise SceneFileError("thin-lens depth of field is not supported by the GPU path")
     eye = np.asarray(props.get("eye", (2.0, 2.0, 2.0)), np.float64)
     focus = np.asarray(props.get("focus", (0.0, 0.0, 0.0)), np.float64)
     if "look" in props:
@@ -1123,12 +1121,27 @@ def camera_record(props: dict, width: int, height: int) -> np.ndarray:
     ln = look / np.linalg.norm(look)
     if abs(abs(float(ln @ (up / np.linalg.norm(up)))) - 1.0) < 1e-7:
         up = np.array([0.0, 1.0, 0.0]) if not np.array_equal(up, [0.0, 1.0, 0.0]) else np.array([0.0, 0.0, 1.0])
-    cam = np.zeros(11, np.float32)
+    cam = np.zeros(16, np.float32)
     cam[0:3] = eye
     cam[3:6] = ln
     cam[6:9] = up
     cam[9] = props.get("heightAngle", 45.0)
     cam[10] = props.get("aspectRatio", 1.0)
+    cam[13] = 1.0
+    # PinholeCamera::init forces aperture 0 (PinholeCamera.cpp); a thin lens defaults to a 35 mm
+    # aperture and f/14, focal length = fstop x aperture (ThinLensCamera.cpp:88-95)
+    if props.get("type") == "thinlens":
+        aperture = float(props.get("aperture", 35.0)) / 1000.0
+        cam[11] = aperture
+        cam[12] = float(props.get("fstop", 14.0)) * aperture
+        if "focalPoint" in props or "focalDistance" not in props:
+            # autofocus on the scene (ThinLensCamera.cpp:97-121): resolved once the scene is
+            # resident (pathtracer.resolve_autofocus); -fallback marks it, the point follows
+            fp = props.get("focalPoint", (0.5, 0.5))
+            cam[13] = -float(props.get("focalDistance", 1.0))
+            cam[14], cam[15] = fp[0], fp[1]
+        else:
+            cam[13] = float(props["focalDistance"])
     return cam
 
 

@@ -20,7 +20,7 @@
  *                          M/shapes/Intersectable.cpp:20-25 (any-hit window)
  *   shading point          M/core/SurfacePoint.cpp:49-65, M/shapes/Mesh.cpp:419-433,
  *                          M/shapes/MeshTriangle.cpp:344-361, M/shapes/Transformable.inl:37-48
- *   camera                 M/cameras/ThinLensCamera.cpp:131-175 (pinhole branch), :181-259
+ *   camera                 M/cameras/ThinLensCamera.cpp:131-175 (getWorldRay, thin lens), :181-259
  *   super-sampling         M/renderers/generators/SuperSampleGenerator.cpp:23-91,
  *                          M/renderers/generators/JitteredSampleGenerator.cpp:19-39, M/core/Viewport.h:29-37
  *   estimator              M/renderers/renderers/PathTracer.cpp:28-116
@@ -125,7 +125,7 @@ static inline void orc_u4(const orc_rng *g, uint64_t path, uint32_t depth, uint3
 
 /* dimension map (identical on the GPU):
  *   depth 0xFFFF, block 0, path = pixel * side^2 + stratum : {jitter x, jitter y, -, -}
- *   depth 0xFFFE, block 0, path = global path id           : {ior index, -, -, -}
+ *   depth 0xFFFE, block 0, path = global path id           : {ior index, lens e1, lens e2, -}
  *   depth d,      block 0                                  : {bsdf0, bsdf1, bsdf2, russian roulette}
  *   depth d,      block 1 + m/2                            : NEE sample m, lanes 2(m%2), 2(m%2)+1  */
 #define ORC_DEPTH_JITTER 0xFFFFu
@@ -734,11 +734,11 @@ void orc_trace_any(const orc_tree *tr, int64_t ntri, const float *v, const uint3
 }
 
 /* ------------------------------------------------------------------------- */
-/* camera (pinhole branch of ThinLensCamera)                                   */
-typedef struct { v3 eye, u, v, n; double tan_w, tan_h; } orc_cam;
+/* camera (ThinLensCamera)                                                     */
+typedef struct { v3 eye, u, v, n; double tan_w, tan_h, aperture, focal_len, focal_dist; } orc_cam;
 
 static orc_cam cam_from(const float *c) {
-  /* c: eye[3], look[3], up[3], heightAngle (deg), aspect */
+  /* c: eye[3], look[3], up[3], heightAngle (deg), aspect, aperture, focal length, focal distance */
   orc_cam k;
   k.eye = V(c[0], c[1], c[2]);
   v3 look = V(c[3], c[4], c[5]);
@@ -753,6 +753,9 @@ static orc_cam cam_from(const float *c) {
   double va = hang * (ORC_PI / 180.0);
   k.tan_h = tan(va / 2);
   k.tan_w = aspect * k.tan_h;
+  k.aperture = c[11];
+  k.focal_len = c[12];
+  k.focal_dist = c[13];
   return k;
 }
 
@@ -760,6 +763,25 @@ static inline v3 cam_dir(const orc_cam *k, double x, double y) {
   double nx = 2 * x - 1, ny = 1 - 2 * y;
   v3 d = vadd(vadd(vmul(k->u, k->tan_w * nx), vmul(k->v, k->tan_h * ny)), vneg(k->n));
   return vnorm(d);
+}
+
+/* ThinLensCamera::getWorldRay, M/cameras/ThinLensCamera.cpp:131-175: with an aperture the ray
+ * is refocused through its focal-plane point from a lens point at radius cofRadius sin(e1),
+ * angle e2, e1 = U(0, pi/2), e2 = U(0, 2 pi) (here u1, u2: the path-init draw's lanes 1, 2). */
+static inline void cam_ray(const orc_cam *k, double x, double y, double u1, double u2, v3 *o, v3 *d) {
+  *d = cam_dir(k, x, y);
+  *o = k->eye;
+  if (k->aperture > 0) {
+    double t = -k->focal_dist / vdot(*d, k->n);
+    if (t == k->focal_len) return;
+    v3 focus = vadd(k->eye, vmul(*d, t));
+    double l_image = k->focal_len * t / (t - k->focal_len);
+    double cof = k->aperture * (l_image - k->focal_dist) / l_image;
+    double r = cof * sin(u1 * (ORC_PI / 2));
+    double e2 = u2 * (2 * ORC_PI);
+    *o = vadd(vadd(k->eye, vmul(k->u, r * cos(e2))), vmul(k->v, r * sin(e2)));
+    *d = vnorm(vsub(focus, *o));
+  }
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1137,9 +1159,10 @@ static void render_row(orc_job *j, int y) {
       orc_u4(&c->rng, ph.path, ORC_DEPTH_PATHINIT, 0u, ui);
       ph.ior_index = (unsigned)floor(ui[0] * 3.0);
       if (ph.ior_index > 2) ph.ior_index = 2;
-      v3 d = cam_dir(&c->cam, px, py);
+      v3 o, d;
+      cam_ray(&c->cam, px, py, ui[1], ui[2], &o, &d);
       double L[3];
-      evaluate(c, &ph, c->cam.eye, d, 0, L);
+      evaluate(c, &ph, o, d, 0, L);
       for (int k3 = 0; k3 < 3; ++k3) acc[k3] += L[k3];
       if (j->path_out) {
         double *po = j->path_out + (pix * (uint64_t)c->p.sample_count + (uint64_t)si) * 3;
@@ -1216,6 +1239,16 @@ int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat,
 }
 
 /* per-sample helpers exposed for unit tests of the restated pieces */
+/* camera ray with the thin lens: camera = 16 floats, (u1, u2) the lens lanes */
+void orc_camera_ray(const float *camera, double x, double y, double u1, double u2, double o_out[3],
+                    double d_out[3]) {
+  orc_cam k = cam_from(camera);
+  v3 o, d;
+  cam_ray(&k, x, y, u1, u2, &o, &d);
+  o_out[0] = o.x; o_out[1] = o.y; o_out[2] = o.z;
+  d_out[0] = d.x; d_out[1] = d.y; d_out[2] = d.z;
+}
+
 void orc_camera_dir(const float *camera, double x, double y, double out[3]) {
   orc_cam k = cam_from(camera);
   v3 d = cam_dir(&k, x, y);

@@ -37,6 +37,7 @@ def load() -> C.CDLL:
                                vp]
     lib.orc_philox4x32_10.argtypes = [vp, vp, vp]
     lib.orc_camera_dir.argtypes = [vp, C.c_double, C.c_double, vp]
+    lib.orc_camera_ray.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, vp, vp]
     lib.orc_bsdf_sample.restype = C.c_int
     lib.orc_bsdf_sample.argtypes = [vp, vp, vp, C.c_int, vp, vp, vp]
     lib.orc_bsdf_eval.argtypes = [vp, vp, vp, vp, vp]
@@ -130,11 +131,13 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
     paths = np.zeros((height * width * sample_count, 3), np.float64) if per_path else None
     st = np.zeros(4, np.uint64)
     lights = scene.lights if len(scene.lights) else np.zeros((1, 16), np.float32)
+    cam = np.zeros(16, np.float32)
+    cam[:np.asarray(scene.camera).reshape(-1).shape[0]] = np.asarray(scene.camera, np.float32).reshape(-1)
     ext = getattr(scene, "light_ext", None)
     ext = np.ascontiguousarray(ext, np.float32) if ext is not None and len(ext) else None
     lib.orc_render(scene.ntri, _p(scene.tri_v), _p(scene.tri_n), _p(scene.tri_mat), _p(scene.tri_light),
                    _p(scene.tri_flags), len(scene.materials), _p(scene.materials), len(scene.lights), _p(lights),
-                   _p(ext), tree.h, _p(scene.camera), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
+                   _p(ext), tree.h, _p(cam), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
     mean = film[r0:r1] / max(sample_count, 1)
     if per_path:
         paths = paths.reshape(height, width, sample_count, 3)[r0:r1]
@@ -157,9 +160,23 @@ def uniforms(seed, stream, path, depth, block) -> np.ndarray:
     return out
 
 
+def camera_ray(camera, x, y, u1, u2):
+    """Thin-lens camera ray (origin, direction) through film point (x, y), lens lanes u1, u2."""
+    cam = np.zeros(16, np.float32)
+    c = np.asarray(camera, np.float32).reshape(-1)
+    cam[:c.shape[0]] = c
+    o = np.zeros(3, np.float64)
+    d = np.zeros(3, np.float64)
+    load().orc_camera_ray(_p(cam), x, y, u1, u2, _p(o), _p(d))
+    return o, d
+
+
 def camera_dir(camera, x, y) -> np.ndarray:
+    """Pinhole direction through film point (x, y) (the thin lens, if any, is not applied)."""
     out = np.zeros(3, np.float64)
-    cam = np.ascontiguousarray(camera, np.float32)
+    cam = np.zeros(16, np.float32)
+    c = np.asarray(camera, np.float32).reshape(-1)
+    cam[:c.shape[0]] = c
     load().orc_camera_dir(_p(cam), x, y, _p(out))
     return out
 

@@ -34,6 +34,7 @@ def hostcheck():
     lib.hc_uniforms.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, vp]
     lib.hc_offset.argtypes = [vp, vp, vp]
     lib.hc_light_point.argtypes = [vp, vp, vp, vp, vp, vp]
+    lib.hc_camera_ray.argtypes = [vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
     return lib
 
 

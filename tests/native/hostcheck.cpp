@@ -2,6 +2,7 @@
 // (milton_gb300/csrc/hd_*.h) compiled for the CPU, so that the FP32 arithmetic the kernels run
 // can be checked against the oracle without a GPU.  Test infrastructure only; it is not part of
 // libmgpu.so and nothing in the product calls it.
+#include <cmath>
 #include <string.h>
 
 #include "../../milton_gb300/csrc/hd_shade.h"
@@ -103,6 +104,31 @@ void hc_uniforms(uint64_t seed, uint32_t stream, uint64_t path, uint32_t depth, 
 void hc_offset(const float *p, const float *n, float *out) {
   V3 o = offset_origin(v3(p[0], p[1], p[2]), v3(n[0], n[1], n[2]));
   out[0] = o.x; out[1] = o.y; out[2] = o.z;
+}
+
+// camera_ray on the host: camera16 as the render parameters carry it; out: o[3], d[3]
+void hc_camera_ray(const float *c, float x, float y, float u1, float u2, float *out) {
+  // setOrientation / _computeMatrix as make_camera does on the host side of the library
+  double n[3] = {-c[3], -c[4], -c[5]}, up[3] = {c[6], c[7], c[8]};
+  double u[3] = {up[1] * n[2] - up[2] * n[1], up[2] * n[0] - up[0] * n[2], up[0] * n[1] - up[1] * n[0]};
+  double ln = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), lu = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  for (int k = 0; k < 3; ++k) { n[k] /= ln; u[k] /= lu; }
+  double v[3] = {n[1] * u[2] - n[2] * u[1], n[2] * u[0] - n[0] * u[2], n[0] * u[1] - n[1] * u[0]};
+  double th = tan(c[9] * (3.14159265358979323846 / 180.0) / 2);
+  Camera k;
+  k.eye = v3(c[0], c[1], c[2]);
+  k.u = v3((float)u[0], (float)u[1], (float)u[2]);
+  k.v = v3((float)v[0], (float)v[1], (float)v[2]);
+  k.n = v3((float)n[0], (float)n[1], (float)n[2]);
+  k.tan_h = (float)th;
+  k.tan_w = (float)(c[10] * th);
+  k.aperture = c[11];
+  k.focal_len = c[12];
+  k.focal_dist = c[13];
+  V3 o, d;
+  camera_ray(k, x, y, u1, u2, o, d);
+  out[0] = o.x; out[1] = o.y; out[2] = o.z;
+  out[3] = d.x; out[4] = d.y; out[5] = d.z;
 }
 
 // light_point on the host: rec16 + ext16 light record, (u, v, r1, r2); tri_v / tri_n the soup

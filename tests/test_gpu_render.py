@@ -140,3 +140,38 @@ def test_renderer_plugin_object(cuda):
     pt.render(ds, pt.RenderSettings(32, 32, 4, max_depth=5, rr_start_depth=3, seed=9), f)
     assert np.array_equal(out, f.mean())
     r.close()
+
+
+def test_thin_lens_per_path(cuda, oracle):
+    # ThinLensCamera::getWorldRay with an aperture: same lens samples, same paths as the oracle
+    from milton_gb300.scene import camera
+    s = scenegen.plain(0)
+    c = s.camera
+    s.camera = camera(eye=c[0:3], look=c[3:6], up=c[6:9], height_angle=float(c[9]), aspect=float(c[10]),
+                      aperture=0.08, focal_length=0.6, focal_distance=2.5)
+    W = H = 48
+    st = pt.RenderSettings(W, H, 8, max_depth=5, rr_start_depth=3, seed=7)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st)
+    tree = oracle.Tree(s.tri_v)
+    mean_o, paths_o, _ = oracle.render(s, tree, W, H, 8, max_depth=5, rr_start=3, seed=7, per_path=True)
+    agree = _path_agreement(paths_g, paths_o)
+    print(f"thin lens: path agreement {agree:.5f}")
+    assert agree >= 0.98
+
+
+def test_autofocus_and_unresolved_lens(cuda, oracle):
+    s = scenegen.plain(0)
+    acc = pt.Accel(s)
+    ds = pt.DeviceScene(s, acc)
+    cam = s.camera.copy()
+    cam[11], cam[12], cam[13], cam[14], cam[15] = 0.05, 0.6, -1.0, 0.5, 0.5
+    f = pt.Film(16, 16)
+    with pytest.raises(pt.N.MgpuError, match="thin lens"):
+        pt.render(ds, pt.RenderSettings(16, 16, 1), f, camera=cam)
+    c2 = pt.resolve_autofocus(cam, ds)
+    # the centre ray's hit distance, from the oracle's closest hit
+    d = oracle.camera_dir(s.camera, 0.5, 0.5)
+    t, _, _, _ = oracle.trace_closest(None, s.tri_v, s.tri_flags,
+                                      np.array([[*s.camera[:3], 0, *d, np.inf]], np.float32))
+    assert c2[13] == pytest.approx(t[0], rel=1e-5)
+    pt.render(ds, pt.RenderSettings(16, 16, 1), f, camera=c2)

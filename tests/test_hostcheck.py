@@ -149,3 +149,28 @@ def test_light_point_types(hostcheck):
                 n = n / np.linalg.norm(n)
             assert np.allclose(out[:3], p, atol=1e-5), (li, kind)
             assert np.allclose(out[3:], n / np.linalg.norm(n), atol=1e-5), (li, kind)
+
+
+def test_thin_lens_camera_rays(hostcheck, oracle):
+    """camera_ray (kernels, FP32) against the oracle's ThinLensCamera::getWorldRay (FP64)."""
+    from milton_gb300.scene import camera
+    rng = np.random.default_rng(9)
+    for aperture, fl, fd in ((0.0, 0.0, 1.0), (0.05, 0.7, 3.0), (0.2, 0.5, 1.2)):
+        cam = camera(eye=(0.3, 1.1, 3.5), focus=(0.0, 0.8, 0.0), height_angle=40.0, aspect=1.25, aperture=aperture,
+                     focal_length=fl, focal_distance=fd)
+        for _ in range(200):
+            x, y, u1, u2 = rng.uniform(0, 1, 4)
+            out = np.zeros(6, np.float32)
+            hostcheck.hc_camera_ray(_p(cam), x, y, u1, u2, _p(out))
+            o, d = oracle.camera_ray(cam, x, y, u1, u2)
+            assert np.allclose(out[:3], o, atol=2e-6) and np.allclose(out[3:], d, atol=2e-6)
+            if aperture == 0.0:
+                assert np.allclose(out[:3], cam[:3])
+    # rays of one film point converge on the focal plane (distance fd along the view axis)
+    cam = camera(eye=(0, 0, 0), look=(0, 0, -1), aperture=0.1, focal_length=0.5, focal_distance=2.0)
+    pts = []
+    for u1, u2 in rng.uniform(0, 1, (16, 2)):
+        o, d = oracle.camera_ray(cam, 0.3, 0.6, u1, u2)
+        t = (-2.0 - o[2]) / d[2]
+        pts.append(o + t * d)
+    assert np.ptp(np.array(pts), axis=0).max() < 1e-9

@@ -163,7 +163,6 @@ def test_camera_defaults_and_output_size():
     ('"sphere" : { "radius" : 1 }', "", "not a triangle shape"),
     ('"material" : { "emitter" : { "type" : "oriented", "power" : 1 }, "cube" : { } }', "", "emitting cube"),
     ('"transform" : { "translate" : [0, 0, 0], "name" : "x", "plane" : { } }', "", "unknown key"),
-    ('"triangle" : { }', '"camera" : { "type" : "thinlens" },', "thin-lens"),
     ('"triangle" : { }', '"renderer" : { "type" : "pathTracer" }, "renderer" : { "type" : "pathTracer" },',
      "multiple renderer definitions"),
     ('"material" : { "bsdf" : { "type" : "diffuse", "kd" : 2 } }', "", "clampedSpectrum"),
@@ -221,3 +220,17 @@ def test_triangle_and_mesh_emitters():
     assert s.lights[3, 12] == pytest.approx(oct_area, rel=1e-6)
     # every emitting triangle points at its light record
     assert sorted(set(s.tri_light.tolist()) - {-1}) == [0, 1, 2, 3, 4]
+
+
+def test_thin_lens_camera_record():
+    sf = L.loads(_scene('"triangle" : { }', '"camera" : { "type" : "thinlens", "eye" : [0, 0, 5], '
+                                            '"aperture" : 50, "fstop" : 10, "focalDistance" : 4.5 },'))
+    cam = sf.scene.camera
+    assert cam[11] == pytest.approx(0.05) and cam[12] == pytest.approx(0.5) and cam[13] == pytest.approx(4.5)
+    # no focalDistance: autofocus on the scene centre, fallback 1 (resolved once resident)
+    cam = L.loads(_scene('"triangle" : { }', '"camera" : { "type" : "thinlens" },')).scene.camera
+    assert cam[11] == pytest.approx(0.035) and cam[12] == pytest.approx(0.49)
+    assert cam[13] == -1.0 and tuple(cam[14:16]) == (0.5, 0.5)
+    # a pinhole camera ignores its aperture key
+    cam = L.loads(_scene('"triangle" : { }', '"camera" : { "type" : "pinhole", "aperture" : 100 },')).scene.camera
+    assert cam[11] == 0.0
