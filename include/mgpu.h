@@ -190,6 +190,10 @@ int mgpu_film_read_raw(mgpu_film *film, float *out8, void *stream);
  * luminance against the converged image; +inf if no pixel has 2 samples.  Deterministic.
  * Progressive refinement's stopping test; no counterpart in the reference.                */
 int mgpu_film_error(mgpu_film *const *films, int32_t n, double *out_rmse, void *stream);
+/* Reinhard tone map of the film's per-pixel means to 8-bit sRGB (width*height*4 bytes, RGBA,
+ * row-major from the top), computed on the device in FP64 (ReinhardToneMap::map,
+ * M/renderers/tonemaps/ReinhardToneMap.cpp:25-94; synchronises).                            */
+int mgpu_film_tonemap(mgpu_film *film, uint8_t *out_rgba, void *stream);
 
 /* PathTracer::render over the requested sample passes (PathTracer.cpp:28-116 per path). */
 int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream);

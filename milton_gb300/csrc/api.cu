@@ -150,6 +150,87 @@ __global__ void k_film_error_final(const double2 *partial, int32_t n, double *ou
   out[f] = c > 0.0 ? sqrt(a / c) : INFINITY;
 }
 
+// Reinhard tone map (ReinhardToneMap::map, M/renderers/tonemaps/ReinhardToneMap.cpp:25-94) of the
+// film's per-pixel means, in FP64: key = exp(mean log(1e-7 + Y)), white = 1 / max(Y)^2 (the
+// unscaled maximum, as the reference has it), Y' = L (1 + L white) / (1 + L) with L = 0.18 Y /
+// key, chromaticity kept, gamma 2.22, clamp to [0, 255] and truncate (a NaN, as from an
+// all-black pixel, becomes 0).  sRGB <-> XYZ matrices as ColorUtils.cpp:115-133 (the standard
+// D65 pair).
+__device__ const double kRgbToXyz[9] = {0.41245322014416, 0.35757958129350, 0.18042258997054,
+                                        0.21267112134122, 0.71515920531078, 0.07216877677613,
+                                        0.01933381646199, 0.11919354020663, 0.95022692228971};
+__device__ const double kXyzToRgb[9] = {3.240479, -1.537150, -0.498535, -0.969256, 1.875992,
+                                        0.041556, 0.055648, -0.204043, 1.057311};
+
+__device__ __forceinline__ void film_xyz(const float4 S, const float4 C, double &X, double &Y, double &Z) {
+  const double n = S.w;
+  double r = 0.0, g = 0.0, b = 0.0;
+  if (n > 0.0) {
+    r = ((double)S.x - C.x) / n;
+    g = ((double)S.y - C.y) / n;
+    b = ((double)S.z - C.z) / n;
+  }
+  X = kRgbToXyz[0] * r + kRgbToXyz[1] * g + kRgbToXyz[2] * b;
+  Y = kRgbToXyz[3] * r + kRgbToXyz[4] * g + kRgbToXyz[5] * b;
+  Z = kRgbToXyz[6] * r + kRgbToXyz[7] * g + kRgbToXyz[8] * b;
+}
+
+__global__ void __launch_bounds__(kErrThreads) k_tonemap_reduce(FilmRef f, double2 *partial) {
+  double lsum = 0.0, ymax = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kErrThreads + threadIdx.x; i < f.npix; i += (int64_t)kErrBlocks * kErrThreads) {
+    double X, Y, Z;
+    film_xyz(f.sum[i], f.c[i], X, Y, Z);
+    lsum += log(1e-7 + Y);
+    ymax = fmax(ymax, Y);
+  }
+  __shared__ double sa[kErrThreads], sm[kErrThreads];
+  sa[threadIdx.x] = lsum;
+  sm[threadIdx.x] = ymax;
+  __syncthreads();
+  for (int w = kErrThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sa[threadIdx.x] += sa[threadIdx.x + w];
+      sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(sa[0], sm[0]);
+}
+
+__global__ void k_tonemap_map(FilmRef f, const double2 *partial, uchar4 *out) {
+  __shared__ double s_scale, s_white;
+  if (threadIdx.x == 0) {
+    double a = 0.0, m = 0.0;
+    for (int b = 0; b < kErrBlocks; ++b) {
+      a += partial[b].x;
+      m = fmax(m, partial[b].y);
+    }
+    const double key = exp(a / (double)f.npix);
+    s_scale = key <= 0.0 ? 0.0 : 0.18 / key;
+    s_white = m <= 0.0 ? 0.0 : 1.0 / (m * m);
+  }
+  __syncthreads();
+  const double scale = s_scale, white = s_white, corr = 1.0 / 2.22;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < f.npix; i += (int64_t)gridDim.x * blockDim.x) {
+    double X, Y, Z;
+    film_xyz(f.sum[i], f.c[i], X, Y, Z);
+    const double s = X + Y + Z;
+    const double cx = X / s, cy = Y / s;  // xyY chromaticity (NaN for a black pixel)
+    const double lum = scale * Y;
+    const double Yd = lum * (1.0 + lum * white) / (1.0 + lum);
+    const double Xd = Yd * cx / cy, Zd = Yd * (1.0 - cx - cy) / cy;
+    double rgb[3];
+    for (int k = 0; k < 3; ++k)
+      rgb[k] = 255.0 * pow(kXyzToRgb[3 * k] * Xd + kXyzToRgb[3 * k + 1] * Yd + kXyzToRgb[3 * k + 2] * Zd, corr);
+    unsigned char o[3];
+    for (int k = 0; k < 3; ++k) {
+      const double v = rgb[k];
+      o[k] = v >= 255.0 ? 255 : (v <= 0.0 ? 0 : (v == v ? (unsigned char)v : 0));
+    }
+    out[i] = make_uchar4(o[0], o[1], o[2], 255);
+  }
+}
+
 // per-thread device scratch of the error estimate (grown as needed, per device)
 struct ErrScratch {
   int device = -1;
@@ -436,6 +517,27 @@ int mgpu_film_read(mgpu_film *f, double *out_mean, void *stream) {
       out_mean[3 * i + 0] = out_mean[3 * i + 1] = out_mean[3 * i + 2] = 0.0;
     }
   }
+  return MGPU_OK;
+}
+
+int mgpu_film_tonemap(mgpu_film *f, uint8_t *out_rgba, void *stream) {
+  if (!f || !out_rgba) return fail(MGPU_E_INVALID, "mgpu_film_tonemap: null argument");
+  const int64_t npix = (int64_t)f->width * f->height;
+  FilmRef ref{f->d_sum, f->d_c, npix};
+  void *d = nullptr;
+  const size_t b_part = align_up(kErrBlocks * sizeof(double2), 256);
+  MGPU_CUDA(cudaMalloc(&d, b_part + (size_t)npix * sizeof(uchar4)));
+  double2 *part = (double2 *)d;
+  uchar4 *img = (uchar4 *)((char *)d + b_part);
+  cudaStream_t st = as_stream(stream);
+  k_tonemap_reduce<<<kErrBlocks, kErrThreads, 0, st>>>(ref, part);
+  k_tonemap_map<<<device_sm_count() * 4, 256, 0, st>>>(ref, part, img);
+  g_launches.fetch_add(2);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out_rgba, img, (size_t)npix * sizeof(uchar4), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "mgpu_film_tonemap");
   return MGPU_OK;
 }
 

@@ -157,6 +157,12 @@ class Film:
         N.check(self._lib.mgpu_film_read_raw(self.handle, N.ptr(out), _stream_handle(stream)))
         return out
 
+    def tonemap(self, stream=None) -> np.ndarray:
+        """mgpu_film_tonemap: Milton's Reinhard tone map of the per-pixel means, (H, W, 4) uint8."""
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        N.check(self._lib.mgpu_film_tonemap(self.handle, N.ptr(out), _stream_handle(stream)))
+        return out
+
     def rmse_estimate(self, stream=None) -> float:
         """Estimated RMSE of the per-pixel mean luminance: sqrt(mean over pixels of the sample
         variance / n), from the film's second moment."""
@@ -444,6 +450,11 @@ class PathTracer:
 
     def output(self) -> np.ndarray:
         return self._film.mean()
+
+    def write_png(self, path: str) -> None:
+        """The output through Milton's Reinhard tone map (on the device), as an 8-bit PNG."""
+        from .imageio import write_png
+        write_png(path, self._film.tonemap())
 
     @property
     def accel(self) -> Accel:

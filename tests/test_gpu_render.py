@@ -175,3 +175,20 @@ def test_autofocus_and_unresolved_lens(cuda, oracle):
                                       np.array([[*s.camera[:3], 0, *d, np.inf]], np.float32))
     assert c2[13] == pytest.approx(t[0], rel=1e-5)
     pt.render(ds, pt.RenderSettings(16, 16, 1), f, camera=c2)
+
+
+def test_device_tonemap_matches_host_model(cuda, tmp_path):
+    from milton_gb300 import imageio
+    from oracle import tonemap
+    s = scenegen.plain(0)
+    acc = pt.Accel(s)
+    ds = pt.DeviceScene(s, acc)
+    f = pt.Film(64, 48)
+    pt.render(ds, pt.RenderSettings(64, 48, 16, max_depth=5, rr_start_depth=3, seed=2), f)
+    dev = f.tonemap()
+    host = tonemap.reinhard(f.mean())
+    diff = np.abs(dev.astype(int) - host.astype(int))
+    assert diff.max() <= 1 and (diff == 0).mean() >= 0.99
+    p = tmp_path / "plain.png"
+    imageio.write_png(str(p), dev)
+    assert np.array_equal(imageio.read_png(str(p)), dev)
