@@ -179,8 +179,23 @@ typedef struct mgpu_film mgpu_film;
 int mgpu_film_create(int32_t width, int32_t height, void *stream, mgpu_film **out);
 int mgpu_film_clear(mgpu_film *film, void *stream);
 int mgpu_film_destroy(mgpu_film *film);
-/* Per-pixel mean in FP64: out = host array of width*height*3 doubles (synchronises). */
+/* The film's output in FP64: out = host array of width*height*3 doubles (synchronises): the
+ * per-pixel mean, or with a reconstruction filter set, sum(w L) / sum(w) over the samples
+ * splatted onto each pixel.                                                                */
 int mgpu_film_read(mgpu_film *film, double *out_mean, void *stream);
+/* Reconstruction filter of ReconstructionRenderOutput (ReconstructionRenderOutput.cpp:30-83):
+ * every sample is splatted onto the pixels within (ceil(support) | 1) / 2 of its own with
+ * weight filter(pixel - position) when > 0 (the per-pixel mean is kept as well).  type:
+ * MGPU_FILTER_NONE, _BOX, _TRIANGLE, _GAUSSIAN (p1 = sigma), _MITCHELL (p1 = B, p2 = C),
+ * _LANCZOS_SINC (p1 = tau) (M/filters/KernelFilter.cpp:18-40).  The splat sums are 2^-24
+ * fixed point, so results do not depend on the order of the atomic additions.  Clears them. */
+int mgpu_film_set_filter(mgpu_film *film, int32_t type, float support, float p1, float p2, void *stream);
+#define MGPU_FILTER_NONE 0
+#define MGPU_FILTER_BOX 1
+#define MGPU_FILTER_TRIANGLE 2
+#define MGPU_FILTER_GAUSSIAN 3
+#define MGPU_FILTER_MITCHELL 4
+#define MGPU_FILTER_LANCZOS_SINC 5
 /* Raw device film: 2 float4 per pixel (sum.rgb + count, compensation.rgb + luminance sum of
  * squares) -> host floats.                                                                  */
 int mgpu_film_read_raw(mgpu_film *film, float *out8, void *stream);
@@ -190,7 +205,7 @@ int mgpu_film_read_raw(mgpu_film *film, float *out8, void *stream);
  * luminance against the converged image; +inf if no pixel has 2 samples.  Deterministic.
  * Progressive refinement's stopping test; no counterpart in the reference.                */
 int mgpu_film_error(mgpu_film *const *films, int32_t n, double *out_rmse, void *stream);
-/* Reinhard tone map of the film's per-pixel means to 8-bit sRGB (width*height*4 bytes, RGBA,
+/* Reinhard tone map of the film's output (as mgpu_film_read) to 8-bit sRGB (width*height*4 bytes, RGBA,
  * row-major from the top), computed on the device in FP64 (ReinhardToneMap::map,
  * M/renderers/tonemaps/ReinhardToneMap.cpp:25-94; synchronises).                            */
 int mgpu_film_tonemap(mgpu_film *film, uint8_t *out_rgba, void *stream);

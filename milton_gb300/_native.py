@@ -96,6 +96,7 @@ SIGNATURES = [
     ("mgpu_film_read_raw", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mgpu_film_error", C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_void_p]),
     ("mgpu_film_tonemap", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mgpu_film_set_filter", C.c_int, [C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float, C.c_void_p]),
     ("mgpu_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_render_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p]),
     ("mgpu_batch_create", C.c_int, [C.POINTER(C.c_void_p)]),

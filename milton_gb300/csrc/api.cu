@@ -162,24 +162,40 @@ __device__ const double kRgbToXyz[9] = {0.41245322014416, 0.35757958129350, 0.18
 __device__ const double kXyzToRgb[9] = {3.240479, -1.537150, -0.498535, -0.969256, 1.875992,
                                         0.041556, 0.055648, -0.204043, 1.057311};
 
-__device__ __forceinline__ void film_xyz(const float4 S, const float4 C, double &X, double &Y, double &Z) {
-  const double n = S.w;
+struct ToneSrc {
+  FilmRef f;
+  const unsigned long long *fx;  // filtered sums, or null for the per-pixel mean
+};
+
+__device__ __forceinline__ void film_xyz(const ToneSrc &t, int64_t i, double &X, double &Y, double &Z) {
   double r = 0.0, g = 0.0, b = 0.0;
-  if (n > 0.0) {
-    r = ((double)S.x - C.x) / n;
-    g = ((double)S.y - C.y) / n;
-    b = ((double)S.z - C.z) / n;
+  if (t.fx) {
+    const double w = (double)t.fx[4 * i + 3];
+    if (w > 0.0) {
+      r = (double)t.fx[4 * i] / w;
+      g = (double)t.fx[4 * i + 1] / w;
+      b = (double)t.fx[4 * i + 2] / w;
+    }
+  } else {
+    const float4 S = t.f.sum[i], C = t.f.c[i];
+    const double n = S.w;
+    if (n > 0.0) {
+      r = ((double)S.x - C.x) / n;
+      g = ((double)S.y - C.y) / n;
+      b = ((double)S.z - C.z) / n;
+    }
   }
   X = kRgbToXyz[0] * r + kRgbToXyz[1] * g + kRgbToXyz[2] * b;
   Y = kRgbToXyz[3] * r + kRgbToXyz[4] * g + kRgbToXyz[5] * b;
   Z = kRgbToXyz[6] * r + kRgbToXyz[7] * g + kRgbToXyz[8] * b;
 }
 
-__global__ void __launch_bounds__(kErrThreads) k_tonemap_reduce(FilmRef f, double2 *partial) {
+__global__ void __launch_bounds__(kErrThreads) k_tonemap_reduce(ToneSrc t, double2 *partial) {
   double lsum = 0.0, ymax = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * kErrThreads + threadIdx.x; i < f.npix; i += (int64_t)kErrBlocks * kErrThreads) {
+  for (int64_t i = (int64_t)blockIdx.x * kErrThreads + threadIdx.x; i < t.f.npix;
+       i += (int64_t)kErrBlocks * kErrThreads) {
     double X, Y, Z;
-    film_xyz(f.sum[i], f.c[i], X, Y, Z);
+    film_xyz(t, i, X, Y, Z);
     lsum += log(1e-7 + Y);
     ymax = fmax(ymax, Y);
   }
@@ -197,7 +213,8 @@ __global__ void __launch_bounds__(kErrThreads) k_tonemap_reduce(FilmRef f, doubl
   if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(sa[0], sm[0]);
 }
 
-__global__ void k_tonemap_map(FilmRef f, const double2 *partial, uchar4 *out) {
+__global__ void k_tonemap_map(ToneSrc t, const double2 *partial, uchar4 *out) {
+  const FilmRef &f = t.f;
   __shared__ double s_scale, s_white;
   if (threadIdx.x == 0) {
     double a = 0.0, m = 0.0;
@@ -213,7 +230,7 @@ __global__ void k_tonemap_map(FilmRef f, const double2 *partial, uchar4 *out) {
   const double scale = s_scale, white = s_white, corr = 1.0 / 2.22;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < f.npix; i += (int64_t)gridDim.x * blockDim.x) {
     double X, Y, Z;
-    film_xyz(f.sum[i], f.c[i], X, Y, Z);
+    film_xyz(t, i, X, Y, Z);
     const double s = X + Y + Z;
     const double cx = X / s, cy = Y / s;  // xyY chromaticity (NaN for a black pixel)
     const double lum = scale * Y;
@@ -478,12 +495,33 @@ int mgpu_film_create(int32_t width, int32_t height, void *stream, mgpu_film **ou
 int mgpu_film_clear(mgpu_film *f, void *stream) {
   if (!f) return fail(MGPU_E_INVALID, "mgpu_film_clear: null film");
   MGPU_CUDA(cudaMemsetAsync(f->d_sum, 0, 2 * (size_t)f->width * f->height * sizeof(float4), as_stream(stream)));
+  if (f->d_fx)
+    MGPU_CUDA(cudaMemsetAsync(f->d_fx, 0, 4 * (size_t)f->width * f->height * sizeof(unsigned long long),
+                              as_stream(stream)));
+  return MGPU_OK;
+}
+
+int mgpu_film_set_filter(mgpu_film *f, int32_t type, float support, float p1, float p2, void *stream) {
+  if (!f) return fail(MGPU_E_INVALID, "mgpu_film_set_filter: null film");
+  if (type < kFilterNone || type > kFilterLanczos || (type != kFilterNone && !(support > 0.0f && support <= 64.0f)) ||
+      (type == kFilterGaussian && !(p1 > 0.0f)) || (type == kFilterLanczos && !(p1 > 0.0f)))
+    return fail(MGPU_E_INVALID, "mgpu_film_set_filter: bad filter type or parameters");
+  if (f->d_fx) {
+    cudaFree(f->d_fx);
+    f->d_fx = nullptr;
+  }
+  f->filter = FilmFilter{type, type == kFilterNone ? 0 : (int)(((unsigned)ceilf(support) | 1u) >> 1), support, p1, p2};
+  if (type == kFilterNone) return MGPU_OK;
+  const size_t bytes = 4 * (size_t)f->width * f->height * sizeof(unsigned long long);
+  MGPU_CUDA(cudaMalloc(&f->d_fx, bytes));
+  MGPU_CUDA(cudaMemsetAsync(f->d_fx, 0, bytes, as_stream(stream)));
   return MGPU_OK;
 }
 
 int mgpu_film_destroy(mgpu_film *f) {
   if (!f) return MGPU_OK;
   cudaError_t e = cudaFree(f->d_sum);
+  if (f->d_fx) cudaFree(f->d_fx);
   delete f;
   if (e != cudaSuccess) return cuda_fail(e, "mgpu_film_destroy: cudaFree");
   return MGPU_OK;
@@ -503,6 +541,18 @@ int mgpu_film_read_raw(mgpu_film *f, float *out8, void *stream) {
 int mgpu_film_read(mgpu_film *f, double *out_mean, void *stream) {
   if (!f || !out_mean) return fail(MGPU_E_INVALID, "mgpu_film_read: null argument");
   size_t n = (size_t)f->width * f->height;
+  if (f->d_fx) {
+    // reconstruction filter: per pixel sum(w L) / sum(w) (ProgressiveFilterValue, weights > 0)
+    std::vector<unsigned long long> fx(4 * n);
+    cudaStream_t st = as_stream(stream);
+    MGPU_CUDA(cudaMemcpyAsync(fx.data(), f->d_fx, fx.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    MGPU_CUDA(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < n; ++i) {
+      const double w = (double)fx[4 * i + 3];
+      for (int k = 0; k < 3; ++k) out_mean[3 * i + k] = w > 0 ? (double)fx[4 * i + k] / w : 0.0;
+    }
+    return MGPU_OK;
+  }
   std::vector<float4> raw(2 * n);
   int rc = mgpu_film_read_raw(f, (float *)raw.data(), stream);
   if (rc != MGPU_OK) return rc;
@@ -523,7 +573,7 @@ int mgpu_film_read(mgpu_film *f, double *out_mean, void *stream) {
 int mgpu_film_tonemap(mgpu_film *f, uint8_t *out_rgba, void *stream) {
   if (!f || !out_rgba) return fail(MGPU_E_INVALID, "mgpu_film_tonemap: null argument");
   const int64_t npix = (int64_t)f->width * f->height;
-  FilmRef ref{f->d_sum, f->d_c, npix};
+  ToneSrc ref{FilmRef{f->d_sum, f->d_c, npix}, f->d_fx};
   void *d = nullptr;
   const size_t b_part = align_up(kErrBlocks * sizeof(double2), 256);
   MGPU_CUDA(cudaMalloc(&d, b_part + (size_t)npix * sizeof(uchar4)));

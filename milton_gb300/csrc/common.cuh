@@ -68,5 +68,9 @@ struct mgpu_film {
   int device = 0;
   int32_t width = 0, height = 0;
   float4 *d_sum = nullptr;  // rgb sum + sample count
-  float4 *d_c = nullptr;    // Kahan compensation
+  float4 *d_c = nullptr;    // Kahan compensation + sum of squared luminance
+  // reconstruction filter (type kFilterNone = per-pixel mean): splatted sums w L (rgb) and w per
+  // pixel in 2^-24 fixed point, so that the atomic additions are order-independent
+  mgpu::FilmFilter filter{mgpu::kFilterNone, 0, 0.0f, 0.0f, 0.0f};
+  unsigned long long *d_fx = nullptr;
 };

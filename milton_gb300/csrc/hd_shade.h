@@ -137,6 +137,56 @@ MGPU_HD void camera_ray(const Camera &c, float x, float y, float u1, float u2, V
   }
 }
 
+// Reconstruction filters of ReconstructionRenderOutput (M/filters/BoxFilter.cpp,
+// TriangleFilter.cpp, GaussianFilter.cpp, MitchellFilter.cpp, LanczosSincFilter.cpp), evaluated
+// at the offset from a sample's film position to a pixel's integer coordinates, as
+// ReconstructionRenderOutput::addSample does (ReconstructionRenderOutput.cpp:30-83), quirks
+// included (the triangle filter is not mirrored for negative offsets; Mitchell's outer branch
+// has no 1/6 and no cut-off).  half = (ceil(support) | 1) >> 1 (KernelFilter.h:28).
+constexpr int kFilterNone = 0, kFilterBox = 1, kFilterTriangle = 2, kFilterGaussian = 3, kFilterMitchell = 4,
+              kFilterLanczos = 5;
+
+struct FilmFilter {
+  int type, half;
+  float support, p1, p2;  // gaussian: sigma; mitchell: B, C; lanczosSinc: tau
+};
+
+MGPU_HD float mitchell_1d(float x, float support, float B, float C) {
+  x = fabsf(2.0f * x / support);
+  if (x > 1.0f)
+    return (((-B / 6.0f - C) * x + (B + 5.0f * C)) * x + (-2.0f * B - 8.0f * C)) * x + (4.0f / 3.0f * B + 4.0f * C);
+  return x * x * ((2.0f - 1.5f * B - C) * x + (-3.0f + 2.0f * B + C)) + (1.0f - B / 3.0f);
+}
+
+MGPU_HD float lanczos_1d(float x, float support, float tau) {
+  x = fabsf(x / support);
+  if (x < kEps) return 1.0f;
+  if (x > 1.0f) return 0.0f;
+  x *= kPi;
+  return sinf(x * tau) / (x * tau) * (sinf(x) / x);
+}
+
+MGPU_HD float filter_eval(const FilmFilter &f, float dx, float dy) {
+  switch (f.type) {
+    case kFilterBox:
+      return 2.0f * sqrtf(dx * dx + dy * dy) < f.support ? 1.0f : 0.0f;
+    case kFilterTriangle: {
+      const float r = f.support / 2.0f;
+      return fmaxf(0.0f, 1.0f - dx / r) * fmaxf(0.0f, 1.0f - dy / r);
+    }
+    case kFilterGaussian: {
+      const float coeff = -0.5f / (f.p1 * f.p1);
+      return fmaxf(0.0f, (1.0f / (sqrtf(2.0f * kPi) * f.p1)) * expf(coeff * (dx * dx + dy * dy)));
+    }
+    case kFilterMitchell:
+      return mitchell_1d(dx, f.support, f.p1, f.p2) * mitchell_1d(dy, f.support, f.p1, f.p2);
+    case kFilterLanczos:
+      return lanczos_1d(dx, f.support, f.p1) * lanczos_1d(dy, f.support, f.p1);
+    default:
+      return 0.0f;
+  }
+}
+
 // Vector::getOrthonormalBasis (Vector.inl:527-538)
 MGPU_HD void onb(V3 n, V3 &U, V3 &W) {
   V3 up = v3(0.0f, 1.0f, 0.0f);

@@ -57,6 +57,8 @@ struct JobArgs {
   int64_t path_base;              // first wave path of the chunk
   int64_t slot_base;              // first accumulate slot of the chunk in the wave
   float4 *film_sum, *film_c;
+  FilmFilter filt;                 // reconstruction filter of the film (kFilterNone: mean only)
+  unsigned long long *film_fx;     // its fixed-point splat sums (4 per pixel)
   float4 *path_out;               // optional per-path radiance
 };
 
@@ -559,6 +561,33 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint32_t *__restrict_
 
 // accumulate: per pixel, Kahan-add the wave's samples into the compensated FP32 film
 // (ProgressiveFilterValue::addSample, ProgressiveFilterValue.h:33-36, box weight 1)
+// Reconstruction splat of one sample (ReconstructionRenderOutput::addSample,
+// ReconstructionRenderOutput.cpp:30-83): the sample's film position is regenerated from its
+// jitter (as k_generate draws it) and its radiance is added, weighted, to every pixel within the
+// filter's half width whose weight is positive.  Fixed point 2^-24 makes the sums independent of
+// the order of the atomic additions; non-finite or oversized contributions are dropped.
+__device__ void splat(const JobArgs &J, int x, int y, int s, V3 L) {
+  const int k = s % J.s2;
+  const uint64_t pix = (uint64_t)y * J.W + x;
+  const F4u jt = uniforms(J.rng, pix * (uint64_t)J.s2 + (uint64_t)k, kDepthJitter, 0);
+  const float px = ((float)x + ((float)(k % J.side) + jt.a) / (float)J.side) / (float)J.W;
+  const float py = ((float)y + ((float)(k / J.side) + jt.b) / (float)J.side) / (float)J.H;
+  const float cx = px * (float)J.W, cy = py * (float)J.H;
+  const int h = J.filt.half;
+  const int y0 = max(0, y - h), y1 = min(J.H - 1, y + h), x0 = max(0, x - h), x1 = min(J.W - 1, x + h);
+  const float scale = 16777216.0f;  // 2^24
+  for (int yy = y0; yy <= y1; ++yy)
+    for (int xx = x0; xx <= x1; ++xx) {
+      const float w = filter_eval(J.filt, (float)xx - cx, (float)yy - cy);
+      if (!(w > 0.0f)) continue;
+      const float v[4] = {w * L.x * scale, w * L.y * scale, w * L.z * scale, w * scale};
+      if (!(v[0] < 1e18f && v[1] < 1e18f && v[2] < 1e18f && v[3] < 1e18f)) continue;
+      unsigned long long *dst = J.film_fx + 4 * ((int64_t)yy * J.W + xx);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) atomicAdd(dst + c, (unsigned long long)llrintf(v[c]));
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     unsigned long long ext = 0, bounces = 0, sh = 0;
@@ -597,6 +626,7 @@ __global__ void __launch_bounds__(kBlock) k_accumulate(RenderArgs a) {
       // second moment of the per-sample luminance (variance / error estimates), unfused
       const float lum = __fmul_rn(__fadd_rn(__fadd_rn(L.x, L.y), L.z), 1.0f / 3.0f);
       C.w = __fadd_rn(C.w, __fmul_rn(lum, lum));
+      if (J.film_fx) splat(J, x, y, J.s0 + si, L);
     }
     S.w += (float)J.ns;
     J.film_sum[pix] = S;
@@ -888,6 +918,8 @@ static JobArgs job_args(const Job &j) {
   J.sample_count = rp->sample_count;
   J.film_sum = j.film->d_sum;
   J.film_c = j.film->d_c;
+  J.filt = j.film->filter;
+  J.film_fx = j.film->d_fx;
   J.path_out = (float4 *)j.path_out;
   int nlp = 1;
   while (nlp < std::min(sc->nlight, 16)) nlp <<= 1;

@@ -147,6 +147,8 @@ class Film:
     def clear(self, stream=None):
         N.check(self._lib.mgpu_film_clear(self.handle, _stream_handle(stream)))
 
+    filter = ("none", 0.0, {})
+
     def mean(self, stream=None) -> np.ndarray:
         out = np.zeros((self.height, self.width, 3), np.float64)
         N.check(self._lib.mgpu_film_read(self.handle, N.ptr(out), _stream_handle(stream)))
@@ -156,6 +158,24 @@ class Film:
         out = np.zeros((2, self.height, self.width, 4), np.float32)
         N.check(self._lib.mgpu_film_read_raw(self.handle, N.ptr(out), _stream_handle(stream)))
         return out
+
+    def set_filter(self, kind: str = "none", support: float = 2.0, stream=None, **params) -> None:
+        """Reconstruction filter of the film's output (mgpu_film_set_filter): "none", "box",
+        "triangle", "gaussian" (sigma), "mitchell" (B, C), "lanczosSinc" (tau), with Milton's
+        defaults (M/filters/KernelFilter.cpp:18-40)."""
+        kinds = {"none": 0, "box": 1, "triangle": 2, "gaussian": 3, "mitchell": 4, "lanczosSinc": 5}
+        if kind not in kinds:
+            raise ValueError(f"unknown filter {kind!r}")
+        p1, p2 = 0.0, 0.0
+        if kind == "gaussian":
+            p1 = params.get("sigma", 1.0)
+        elif kind == "mitchell":
+            p1, p2 = params.get("B", 1.0 / 3.0), params.get("C", 1.0 / 3.0)
+        elif kind == "lanczosSinc":
+            p1 = params.get("tau", 3.0)
+        N.check(self._lib.mgpu_film_set_filter(self.handle, kinds[kind], float(support), float(p1), float(p2),
+                                               _stream_handle(stream)))
+        self.filter = (kind, float(support), dict(params))
 
     def tonemap(self, stream=None) -> np.ndarray:
         """mgpu_film_tonemap: Milton's Reinhard tone map of the per-pixel means, (H, W, 4) uint8."""
@@ -404,6 +424,10 @@ class PathTracer:
     width: int = 0
     height: int = 0
 
+    # reconstruction filter of the output (kind, support, params), e.g. from a scene file's
+    # "output" block; None = per-pixel mean
+    output_filter: tuple | None = None
+
     def __post_init__(self):
         self._accel = None
         self._dscene = None
@@ -440,6 +464,9 @@ class PathTracer:
         self._accel = Accel(self.scene, self.kd_settings())
         self._dscene = DeviceScene(self.scene, self._accel)
         self._film = Film(self.width, self.height)
+        if self.output_filter is not None:
+            kind, support, params = self.output_filter
+            self._film.set_filter(kind, support, **params)
         self._camera = resolve_autofocus(self.scene.camera, self._dscene)
 
     def render(self, stream=None):

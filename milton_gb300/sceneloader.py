@@ -517,6 +517,14 @@ class _Loader:
                 raise SceneFileError("invalid output type")
             req["tonemap"] = "string"
             self.output = {"type": kind}
+            # the reconstruction filter: an explicit "filter" object, or DefaultRenderOutput's
+            # Lanczos-sinc of support 2 (DefaultRenderOutput.cpp:20); "naive" has none
+            if kind != "naive":
+                fv = v.find("filter")
+                if fv is not _MISSING:
+                    self.output["filter"] = parse_filter(fv)
+                elif kind == "default":
+                    self.output["filter"] = ("lanczosSinc", 2.0, {"tau": 3.0})
         props = {}
         _properties(req, v, props)
         self.output_props.update(props)
@@ -748,6 +756,37 @@ class _Loader:
 # meshes (MeshLoader.cpp:21-42; OBJ: MeshLoaderOBJ.cpp with obj-parser-0.1 triangulating
 # faces as fans; PLY: MeshLoaderPLY.cpp reads float32 vertex x/y/z and fan-triangulates
 # face vertex_indices lists)
+
+def parse_filter(v) -> tuple:
+    """MiltonJSONSceneLoader::_parse_filter (:1340-1382) -> (kind, support, params) with
+    KernelFilter::create's defaults (support 2, sigma 1, B = C = 1/3, tau 3)."""
+    if isinstance(v, str):
+        v = JObj([("type", v)])
+    if not isinstance(v, JObj):
+        raise SceneFileError(f"filter must be of type 'object', found '{_tname(v)}'")
+    t = v.find("type")
+    if t is _MISSING:
+        raise SceneFileError("unable to infer filter type")
+    req = {"support": "uint"}
+    if t == "gaussian":
+        req["sigma"] = "real_t"
+    elif t == "mitchell":
+        req.update(B="real_t", C="real_t")
+    elif t == "lanczosSinc":
+        req["tau"] = "real_t"
+    elif t not in ("box", "triangle"):
+        raise SceneFileError("invalid filter type")
+    props = {}
+    _properties(req, v, props)
+    params = {}
+    if t == "gaussian":
+        params["sigma"] = float(props.get("sigma", 1.0))
+    elif t == "mitchell":
+        params.update(B=float(props.get("B", 1.0 / 3.0)), C=float(props.get("C", 1.0 / 3.0)))
+    elif t == "lanczosSinc":
+        params["tau"] = float(props.get("tau", 3.0))
+    return (t, float(props.get("support", 2)), params)
+
 
 def load_mesh(path: str):
     """(vertices (V, 3) float64, triangles (T, 3) int, normals (N, 3) or None, normal indices
@@ -1208,4 +1247,5 @@ def path_tracer(sf: SceneFile):
     r = PathTracer(sf.path_tracer_props())
     r.set_scene(sf.scene)
     r.set_output(sf.width, sf.height)
+    r.output_filter = sf.output.get("filter")
     return r

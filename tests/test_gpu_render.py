@@ -192,3 +192,30 @@ def test_device_tonemap_matches_host_model(cuda, tmp_path):
     p = tmp_path / "plain.png"
     imageio.write_png(str(p), dev)
     assert np.array_equal(imageio.read_png(str(p)), dev)
+
+
+@pytest.mark.parametrize("kind,support,params", [("box", 2.0, {}), ("triangle", 2.0, {}),
+                                                 ("gaussian", 3.0, {"sigma": 0.8}),
+                                                 ("mitchell", 2.0, {"B": 1 / 3, "C": 1 / 3}),
+                                                 ("lanczosSinc", 2.0, {"tau": 3.0})])
+def test_reconstruction_filters(cuda, kind, support, params):
+    from oracle import filters, pyoracle
+    s = scenegen.plain(0)
+    acc = pt.Accel(s)
+    ds = pt.DeviceScene(s, acc)
+    W, H, spp = 20, 16, 4
+    st = pt.RenderSettings(W, H, spp, max_depth=5, rr_start_depth=3, seed=3)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st, accel=acc, dscene=ds)
+    f = pt.Film(W, H)
+    f.set_filter(kind, support, **params)
+    pt.render(ds, st, f)
+    got = f.mean()
+    want = filters.splat(paths_g, spp, 0, 3, 0, kind, support, params, pyoracle.uniforms)
+    assert np.allclose(got, want, rtol=2e-5, atol=1e-6)
+    # the splat sums are order-independent: the same image from tiny waves and split passes
+    f2 = pt.Film(W, H)
+    f2.set_filter(kind, support, **params)
+    pt.render(ds, pt.RenderSettings(W, H, spp, sample_count=1, max_depth=5, rr_start_depth=3, seed=3,
+                                    wave_paths=64), f2)
+    pt.render(ds, pt.RenderSettings(W, H, spp, sample_begin=1, max_depth=5, rr_start_depth=3, seed=3), f2)
+    assert np.array_equal(f2.mean(), got)

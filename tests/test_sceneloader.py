@@ -234,3 +234,18 @@ def test_thin_lens_camera_record():
     # a pinhole camera ignores its aperture key
     cam = L.loads(_scene('"triangle" : { }', '"camera" : { "type" : "pinhole", "aperture" : 100 },')).scene.camera
     assert cam[11] == 0.0
+
+
+def test_output_filters():
+    sf = L.loads(_scene('"triangle" : { }', '"output" : { "type" : "default", "width" : 8, "height" : 8 },'))
+    assert sf.output["filter"] == ("lanczosSinc", 2.0, {"tau": 3.0})
+    sf = L.loads(_scene('"triangle" : { }', '"output" : { "filter" : { "type" : "gaussian", "support" : 3, '
+                                            '"sigma" : 0.7 } },'))
+    assert sf.output["type"] == "reconstruction" and sf.output["filter"] == ("gaussian", 3.0, {"sigma": 0.7})
+    sf = L.loads(_scene('"triangle" : { }', '"output" : { "type" : "naive", "width" : 8 },'))
+    assert "filter" not in sf.output
+    assert L.path_tracer(L.loads(_scene('"triangle" : { }', '"renderer" : { "type" : "pathTracer" }, '
+                                        '"output" : { "filter" : "mitchell" },'))).output_filter == \
+        ("mitchell", 2.0, {"B": 1 / 3, "C": 1 / 3})
+    with pytest.raises(L.SceneFileError, match="invalid filter"):
+        L.loads(_scene('"triangle" : { }', '"output" : { "filter" : { "type" : "sharp" } },'))
