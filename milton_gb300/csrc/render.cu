@@ -40,6 +40,13 @@ constexpr int kCtrFetchSh = 3 * (kHardCap + 8);    // ... and of the persistent 
 constexpr int kCtrTrunc = 4 * (kHardCap + 8);
 constexpr int kNumCounters = kCtrTrunc + 8;
 constexpr int kBins = 4096;             // queue binning keys
+#ifndef MGPU_TRAV_MIN_BLOCKS
+#define MGPU_TRAV_MIN_BLOCKS 12
+#endif
+// Resident 128-thread blocks per SM the traversal kernels are compiled for: 12 caps them at 40
+// registers (a few bytes of spills to L1) for 48 warps per SM instead of 36-40, which hides more
+// of the node-load latency (mid frame: 215 -> 226 Mpaths/s; 10 and 16 blocks measured 221).
+constexpr int kTravMinBlocks = MGPU_TRAV_MIN_BLOCKS;
 
 // One job chunk of a wave (device memory).
 struct JobArgs {
@@ -227,7 +234,7 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
 
 // extend: closest hit for the live queue of bounce b
 template <bool COUNT, bool PERSIST>
-__global__ void __launch_bounds__(kBlock) k_extend(RenderArgs a, int b) {
+__global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_extend(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
   float4 *qhit = a.qhit;
@@ -448,7 +455,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
 
 // shadow: any-hit query per queued light sample; an occluded sample's slot is zeroed
 template <bool COUNT, bool PERSIST>
-__global__ void __launch_bounds__(kBlock) k_shadow(RenderArgs a, int b) {
+__global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_shadow(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrNee + b];
   const float4 *so = a.so, *sd = a.sd;
   float4 *slots = a.slots;
