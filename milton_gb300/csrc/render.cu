@@ -47,6 +47,12 @@ constexpr int kBins = 4096;             // queue binning keys
 // registers (a few bytes of spills to L1) for 48 warps per SM instead of 36-40, which hides more
 // of the node-load latency (mid frame: 215 -> 226 Mpaths/s; 10 and 16 blocks measured 221).
 constexpr int kTravMinBlocks = MGPU_TRAV_MIN_BLOCKS;
+#ifndef MGPU_SHADE_MIN_BLOCKS
+#define MGPU_SHADE_MIN_BLOCKS 8
+#endif
+// the shade kernel at 8 blocks per SM (64 registers, spilling ~0.8 KB to L1) against its natural
+// 125 registers: 211 -> 184 ms per 5 mid frames
+constexpr int kShadeMinBlocks = MGPU_SHADE_MIN_BLOCKS;
 
 // One job chunk of a wave (device memory).
 struct JobArgs {
@@ -279,7 +285,7 @@ __device__ __forceinline__ V3 fold_slots(const RenderArgs &a, int nl, int64_t p,
   return L;
 }
 
-__global__ void __launch_bounds__(kBlock) k_shade(RenderArgs a, int b) {
+__global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const int cur = b & 1, nxt = (b + 1) & 1;
   const uint32_t stride = gridDim.x * blockDim.x;
