@@ -33,7 +33,9 @@ extern "C" {
 #define MGPU_E_NOMEM (-3)    /* allocation failed (host or device) */
 #define MGPU_E_BUDGET (-4)   /* request exceeds the memory budget it was admitted under */
 #define MGPU_E_STATE (-5)    /* call not valid in the object's current state */
-#define MGPU_E_DEVICE (-6)   /* a kernel reported a fault it guarded against (bounds, stack) */
+#define MGPU_E_DEVICE (-6)   /* reserved: kernels stay in bounds by construction (tree depth <= 64
+                                checked at build, queue sizes bounded by the wave) and never
+                                report a guarded fault today */
 
 /* triangle flags */
 #define MGPU_TRI_CULLED 1u   /* back-face culled, Milton `Triangle` (Triangle.cpp:245-272); else two-sided `MeshTriangle` */
