@@ -317,6 +317,7 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic (seeded scene generator, no external assets)",
         "config": {"workload": WORKLOAD, "paths_per_step": paths_per_step,
                    "l2": "a 256 MiB buffer (larger than the 129 MB L2) is written before every step",
+                   "wave_paths": "automatic (up to 2^26 paths per wave, workspace within 40 GB)",
                    "parallelism": f"replicas x{ws} (independent sample streams, no collective in the step)",
                    "kd_build_s": round(build_s, 3), "kd_nodes": kst["node_pairs"], "kd_refs": kst["refs"],
                    "rays_per_path": (stats["extension_rays"] + stats["shadow_rays"]) / paths_per_step,

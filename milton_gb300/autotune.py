@@ -10,7 +10,7 @@ import math
 
 from . import pathtracer as pt
 
-WAVES = (1 << 21, 1 << 22, 1 << 23, 1 << 24)
+WAVES = (1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26)
 SHAPES = ((0, 1, 1), (1, 1, 1), (0, 0, 0))  # (persistent, bin_shadow, bin_extension)
 
 _cache: dict = {}
@@ -22,7 +22,7 @@ def _size_class(requests) -> tuple:
     return (int(math.log2(max(paths, 1))), int(math.log2(max(tris, 1))))
 
 
-def tune(requests, stream=None, calib_samples: int = 1, waves=WAVES, shapes=SHAPES) -> dict:
+def tune(requests, stream=None, calib_samples: int = 4, waves=WAVES, shapes=SHAPES) -> dict:
     """requests: list of (DeviceScene, RenderSettings).  Returns {"wave_paths", "persistent",
     "bin_shadow", "bin_extension", "ms"} for the fastest calibration render and applies the
     kernel-shape knobs process-wide."""
@@ -41,8 +41,12 @@ def tune(requests, stream=None, calib_samples: int = 1, waves=WAVES, shapes=SHAP
             c = pt.RenderSettings(st.width, st.height, st.spp, sample_begin=0, sample_count=min(calib_samples, st.spp),
                                   max_depth=st.max_depth or 8, rr_start_depth=st.rr_start_depth, seed=st.seed)
             b.add(ds, c, f)
-        b.render(stream)  # warm
-        torch.cuda.synchronize()
+        try:
+            b.render(stream)  # warm
+            torch.cuda.synchronize()
+        except pt.N.MgpuError:  # a wave whose workspace does not fit the device: skip it
+            b.close()
+            continue
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         b.render(stream)
