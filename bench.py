@@ -430,7 +430,8 @@ def run_serving(args):
     t0 = time.perf_counter()
     scenes = [workloads.build_scene(sp) for sp in specs]
     gen_s = time.perf_counter() - t0
-    settings = ServerSettings(hbm_budget=120_000_000_000, tick_paths=args.tick_paths, use_graph=args.graph)
+    settings = ServerSettings(hbm_budget=120_000_000_000, tick_paths=args.tick_paths, use_graph=args.graph,
+                              policy=args.policy)
     srv = Server(settings)
     ids = [srv.add_scene(s) for s in scenes]
     t0 = time.perf_counter()
@@ -508,7 +509,8 @@ def run_serving(args):
            "config": {"requests": len(reqs), "rate_per_s": args.rate, "scenes": len(scenes),
                       "triangles": [s.ntri for s in scenes], "target_rmse": target_rmse,
                       "hbm_budget": settings.hbm_budget, "tick_paths": settings.tick_paths,
-                      "use_graph": settings.use_graph, "paths": paths, "busy_s": round(busy, 3),
+                      "use_graph": settings.use_graph, "policy": settings.policy, "paths": paths,
+                      "busy_s": round(busy, 3),
                       "wall_s": round(t_end - t_start, 3), "plain_s": round(plain_s, 3),
                       "peak_resident_bytes": s1["peak_resident_bytes"], "ticks": s1["ticks"] - s0["ticks"],
                       "spp_done_histogram": {str(k): v for k, v in sorted(spp_hist.items())},
@@ -618,6 +620,7 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--tick-paths", type=int, default=1 << 26, help="serving: paths per scheduling tick")
     ap.add_argument("--graph", type=int, default=0, help="serving: capture each tick in a CUDA graph")
+    ap.add_argument("--policy", default="fair", choices=["fair", "oldest"], help="serving: tick scheduling policy")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)

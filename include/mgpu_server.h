@@ -15,9 +15,10 @@
  *      active job) are evicted least recently used first to make room; a job that still does
  *      not fit stops admission for this tick.  Trees and films stay on the device between
  *      ticks.
- *   2. Rendering: active jobs get sample passes up to the tick's path budget -- first one
- *      sample each, least recently served first, then the rest of the budget oldest job first,
- *      never past a job's next checkpoint -- and the passes of all jobs render together in one
+ *   2. Rendering: active jobs get sample passes up to the tick's path budget -- under the fair
+ *      policy first one sample each, least recently served first, then the rest of the budget
+ *      oldest job first; under the oldest-first policy only the latter -- never past a job's
+ *      next checkpoint -- and the passes of all jobs render together in one
  *      batch (mgpu_batch_*: jobs of different scenes share waves; passes are grouped by
  *      scene so that a wave touches few trees).
  *   3. Checkpoints: a job's checkpoints are its sample counts c0 = min(spp, max_spp),
@@ -55,7 +56,13 @@ typedef struct {
   int32_t use_graph;     /* capture each tick's launches in one CUDA graph */
   int32_t build_threads; /* background kd-tree builds at once; 0 = 2 */
   mgpu_kd_params kd;     /* kd-tree parameters for every scene (threads 0 = all cores) */
+  int32_t policy;        /* MGPU_SERVE_FAIR (0): one sample per active job first, least recently
+                            served first, then the rest oldest first; MGPU_SERVE_OLDEST (1): the
+                            whole tick oldest job first (fewer jobs and scenes per wave) */
 } mgpu_server_params;
+
+#define MGPU_SERVE_FAIR 0
+#define MGPU_SERVE_OLDEST 1
 
 #define MGPU_JOB_QUEUED 0
 #define MGPU_JOB_ACTIVE 1

@@ -48,7 +48,7 @@ class RenderParams(C.Structure):
 class ServerParams(C.Structure):
     _fields_ = [("hbm_budget", C.c_uint64), ("tick_paths", C.c_int64), ("max_active", C.c_int32),
                 ("wave_paths", C.c_int32), ("use_graph", C.c_int32), ("build_threads", C.c_int32),
-                ("kd", KdParams)]
+                ("kd", KdParams), ("policy", C.c_int32)]
 
 
 class ServerJobInfo(C.Structure):

@@ -285,13 +285,18 @@ void plan(mgpu_server *s, std::vector<Pass> &out) {
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t a, size_t b) { return act[a]->last_served < act[b]->last_served; });
   bool any = false;
-  for (size_t i : order) {
-    const int64_t px = (int64_t)act[i]->pixels();
-    if (px <= left || !any) {
-      k[i] = 1;
-      left -= px;
-      any = true;
+  if (s->p.policy == MGPU_SERVE_FAIR) {
+    for (size_t i : order) {
+      const int64_t px = (int64_t)act[i]->pixels();
+      if (px <= left || !any) {
+        k[i] = 1;
+        left -= px;
+        any = true;
+      }
     }
+  } else if (!act.empty()) {
+    k[0] = 1;  // the oldest job always advances, even when one sample exceeds the tick
+    left -= (int64_t)act[0]->pixels();
   }
   for (size_t i = 0; i < act.size() && left > 0; ++i) {
     const int64_t px = (int64_t)act[i]->pixels();
@@ -316,6 +321,8 @@ int mgpu_server_create(const mgpu_server_params *params, mgpu_server **out) {
   if (!params || !out) return fail(MGPU_E_INVALID, "mgpu_server_create: null argument");
   if (params->tick_paths < 0 || params->max_active < 0 || params->wave_paths < 0 || params->build_threads < 0)
     return fail(MGPU_E_INVALID, "mgpu_server_create: negative parameter");
+  if (params->policy != MGPU_SERVE_FAIR && params->policy != MGPU_SERVE_OLDEST)
+    return fail(MGPU_E_INVALID, "mgpu_server_create: unknown policy");
   mgpu_server *s = new (std::nothrow) mgpu_server();
   if (!s) return fail(MGPU_E_NOMEM, "mgpu_server_create: out of host memory");
   s->p = *params;

@@ -51,9 +51,10 @@ def _run(scenes, jobs, settings=None, keys=None):
         return [res[j] for j in jids], srv.stats(), peak
 
 
-def test_same_image_alone_and_in_the_mix(cuda):
+@pytest.mark.parametrize("policy", ["fair", "oldest"])
+def test_same_image_alone_and_in_the_mix(cuda, policy):
     scenes = _scenes()
-    mix, st, _ = _run(scenes, JOBS)
+    mix, st, _ = _run(scenes, JOBS, ServerSettings(tick_paths=20000, policy=policy))
     assert st["finished"] == len(JOBS) and st["failed"] == 0
     assert st["ticks"] > 3  # the small tick budget spreads the jobs over many shared ticks
     stopped_early = 0
