@@ -76,7 +76,37 @@ struct Shared {
   std::atomic<int> spare_threads;
 };
 
-constexpr size_t kSpawnMin = 4096;  // subtrees smaller than this stay on the calling thread
+constexpr size_t kSpawnMin = 4096;       // subtrees smaller than this stay on the calling thread
+constexpr size_t kAxisThreadMin = 262144;  // nodes at least this large evaluate their axes in parallel
+constexpr size_t kRadixMin = 65536;        // event lists at least this long are radix sorted
+
+// LSD radix sort of 64-bit keys, 11-bit digits; digits that are equal in every key are skipped.
+// Produces the same order as std::sort (a total order on the integers).
+void radix_sort(std::vector<uint64_t> &a, std::vector<uint64_t> &tmp) {
+  constexpr int kBits = 11, kDigits = (64 + kBits - 1) / kBits;
+  constexpr uint32_t kMask = (1u << kBits) - 1u;
+  const size_t n = a.size();
+  std::vector<uint32_t> hist((size_t)kDigits << kBits, 0u);
+  for (size_t i = 0; i < n; ++i) {
+    const uint64_t k = a[i];
+    for (int d = 0; d < kDigits; ++d) ++hist[((size_t)d << kBits) + ((k >> (d * kBits)) & kMask)];
+  }
+  tmp.resize(n);
+  uint64_t *src = a.data(), *dst = tmp.data();
+  for (int d = 0; d < kDigits; ++d) {
+    uint32_t *h = &hist[(size_t)d << kBits];
+    if (h[(src[0] >> (d * kBits)) & kMask] == n) continue;  // one bucket holds every key
+    uint32_t sum = 0;
+    for (uint32_t b = 0; b <= kMask; ++b) {
+      const uint32_t c = h[b];
+      h[b] = sum;
+      sum += c;
+    }
+    for (size_t i = 0; i < n; ++i) dst[h[(src[i] >> (d * kBits)) & kMask]++] = src[i];
+    std::swap(src, dst);
+  }
+  if (src != a.data()) a.swap(tmp);
+}
 
 class Task {
  public:
@@ -109,51 +139,40 @@ class Task {
       leaf(nd, std::move(prims), depth);
       return;
     }
+    // each axis' best plane (axes in parallel for large nodes), then the first axis whose cost
+    // is strictly lowest, as the reference's sequential loop picks it
+    double cost_ax[3] = {INFINITY, INFINITY, INFINITY}, pos_ax[3] = {0, 0, 0};
+    int axes[3], na = 0;
+    for (int axis = 0; axis < 3; ++axis)
+      if (axis != parent_axis && box.mn[axis] < box.mx[axis]) axes[na++] = axis;
+    if (n >= kAxisThreadMin && na > 1) {
+      std::thread th[2];
+      bool spawned[2] = {false, false};
+      std::vector<uint64_t> keys_extra[2], tmp_extra[2];
+      for (int k = 1; k < na; ++k) {
+        if (!take_thread()) continue;
+        spawned[k - 1] = true;
+        const int axis = axes[k];
+        th[k - 1] = std::thread([&, axis, k]() {
+          best_plane(prims, axis, box, keys_extra[k - 1], tmp_extra[k - 1], cost_ax[axis], pos_ax[axis]);
+        });
+      }
+      best_plane(prims, axes[0], box, keys_, tmp_, cost_ax[axes[0]], pos_ax[axes[0]]);
+      for (int k = 1; k < na; ++k) {
+        if (spawned[k - 1]) {
+          th[k - 1].join();
+          s_->spare_threads.fetch_add(1);
+        } else {
+          best_plane(prims, axes[k], box, keys_, tmp_, cost_ax[axes[k]], pos_ax[axes[k]]);
+        }
+      }
+    } else {
+      for (int k = 0; k < na; ++k) best_plane(prims, axes[k], box, keys_, tmp_, cost_ax[axes[k]], pos_ax[axes[k]]);
+    }
     double best_cost = INFINITY, best_pos = 0;
     int best_axis = 0;
-    for (int axis = 0; axis < 3; ++axis) {
-      if (axis == parent_axis || box.mn[axis] >= box.mx[axis]) continue;
-      keys_.clear();
-      for (size_t i = n; i--;) {
-        int32_t t = prims[i];
-        if (s_->point[t]) continue;
-        float mn = s_->tmin[3 * (size_t)t + axis], mx = s_->tmax[3 * (size_t)t + axis];
-        if (mn == mx) {
-          keys_.push_back(((uint64_t)order_bits(mn) << 2) | 1u);
-        } else {
-          keys_.push_back(((uint64_t)order_bits(mn) << 2) | 2u);
-          keys_.push_back(((uint64_t)order_bits(mx) << 2) | 0u);
-        }
-      }
-      const size_t m = keys_.size();
-      if (m == 0) continue;
-      std::sort(keys_.begin(), keys_.end());
-      size_t idx = 0;
-      uint64_t nl = 0, nr = n;
-      while (idx < m - 1) {
-        uint64_t cur = keys_[idx] >> 2;
-        uint64_t cnt[3] = {0, 0, 0};
-        do {
-          ++cnt[keys_[idx] & 3u];
-        } while (idx < m - 1 && (keys_[++idx] >> 2) == cur);
-        uint64_t np = cnt[1];
-        nr -= cnt[0] + np;
-        uint32_t ob = (uint32_t)cur;
-        uint32_t fb = (ob & 0x80000000u) ? (ob & 0x7FFFFFFFu) : ~ob;
-        float fpos;
-        memcpy(&fpos, &fb, 4);
-        double pos = fpos;
-        if (pos > box.mn[axis] && pos < box.mx[axis]) {
-          double la, ra;
-          split_areas(box, axis, pos, la, ra);
-          unsigned l = (unsigned)(nl + np);
-          double cost = la * l + ra * (unsigned)nr;
-          if (l + np == 0 || nr == 0) cost *= p.empty_bias;
-          if (cost < best_cost) { best_cost = cost; best_pos = pos; best_axis = axis; }
-        }
-        nl += cnt[2] + np;
-      }
-    }
+    for (int axis = 0; axis < 3; ++axis)
+      if (cost_ax[axis] < best_cost) { best_cost = cost_ax[axis]; best_pos = pos_ax[axis]; best_axis = axis; }
     if (best_cost == INFINITY) { leaf(nd, std::move(prims), depth); return; }
     double leaf_cost = ((double)(int)n - p.cost_traversal) * box_area(box);
     if (best_cost > leaf_cost) { leaf(nd, std::move(prims), depth); return; }
@@ -197,6 +216,55 @@ class Task {
   }
 
  private:
+  // _computeSplitPlaneSAH for one axis (kdTreeAccel.cpp:722-811): sorted min / planar / max
+  // events, sweep with SAH cost SA_L (n_L + n_P) + SA_R n_R, empty-side bias
+  void best_plane(const std::vector<int32_t> &prims, int axis, const Box &box, std::vector<uint64_t> &keys,
+                  std::vector<uint64_t> &tmp, double &best_cost, double &best_pos) const {
+    const KdParams &p = s_->p;
+    const size_t n = prims.size();
+    keys.clear();
+    for (size_t i = n; i--;) {
+      int32_t t = prims[i];
+      if (s_->point[t]) continue;
+      float mn = s_->tmin[3 * (size_t)t + axis], mx = s_->tmax[3 * (size_t)t + axis];
+      if (mn == mx) {
+        keys.push_back(((uint64_t)order_bits(mn) << 2) | 1u);
+      } else {
+        keys.push_back(((uint64_t)order_bits(mn) << 2) | 2u);
+        keys.push_back(((uint64_t)order_bits(mx) << 2) | 0u);
+      }
+    }
+    const size_t m = keys.size();
+    if (m == 0) return;
+    if (m >= kRadixMin) radix_sort(keys, tmp);
+    else std::sort(keys.begin(), keys.end());
+    size_t idx = 0;
+    uint64_t nl = 0, nr = n;
+    while (idx < m - 1) {
+      uint64_t cur = keys[idx] >> 2;
+      uint64_t cnt[3] = {0, 0, 0};
+      do {
+        ++cnt[keys[idx] & 3u];
+      } while (idx < m - 1 && (keys[++idx] >> 2) == cur);
+      uint64_t np = cnt[1];
+      nr -= cnt[0] + np;
+      uint32_t ob = (uint32_t)cur;
+      uint32_t fb = (ob & 0x80000000u) ? (ob & 0x7FFFFFFFu) : ~ob;
+      float fpos;
+      memcpy(&fpos, &fb, 4);
+      double pos = fpos;
+      if (pos > box.mn[axis] && pos < box.mx[axis]) {
+        double la, ra;
+        split_areas(box, axis, pos, la, ra);
+        unsigned l = (unsigned)(nl + np);
+        double cost = la * l + ra * (unsigned)nr;
+        if (l + np == 0 || nr == 0) cost *= p.empty_bias;
+        if (cost < best_cost) { best_cost = cost; best_pos = pos; }
+      }
+      nl += cnt[2] + np;
+    }
+  }
+
   bool take_thread() {
     int cur = s_->spare_threads.load();
     while (cur > 0) {
@@ -205,7 +273,7 @@ class Task {
     return false;
   }
   Shared *s_;
-  std::vector<uint64_t> keys_;
+  std::vector<uint64_t> keys_, tmp_;
 };
 
 // -------------------------------------------------------------------------------------------

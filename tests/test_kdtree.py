@@ -82,3 +82,9 @@ def test_rejects_too_deep_trees():
     from milton_gb300._native import MgpuError
     with pytest.raises(MgpuError):
         Accel(scenegen.plain(0), KdSettings(max_depth=65))
+
+
+def test_identical_to_oracle_on_a_large_soup(oracle):
+    # 300,000 triangles: the root's axes are evaluated on parallel threads and its event lists
+    # are radix sorted (the small cases above take std::sort); the tree must not change
+    _same(oracle, _soup(7, 300_000), KdSettings(threads=4))
