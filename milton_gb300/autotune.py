@@ -11,7 +11,7 @@ import math
 from . import pathtracer as pt
 
 WAVES = (1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26)
-SHAPES = ((0, 1, 1), (1, 1, 1), (0, 0, 0))  # (persistent, bin_shadow, bin_extension)
+SHAPES = ((0, 1, 1), (0, 1, 0), (0, 0, 1), (1, 1, 1), (0, 0, 0))  # (persistent, bin_shadow, bin_extension)
 
 _cache: dict = {}
 
