@@ -34,9 +34,13 @@ frame and object-space area, a mesh one mesh light over its triangles (include/m
 ``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
 element: analytic shapes other than planes and cubes (sphere, cylinder, cone, blob, point),
 emitting cubes, omni and environment emitters, textures and bump maps, per-channel IOR or
-Phong exponents, instancing.  A thin-lens camera keeps its aperture, f-stop and focal distance;
-its autofocus is resolved against the resident scene (pathtracer.resolve_autofocus).  A "cube" becomes the 12 triangles of
-Milton's unit cube (Cube.cpp), which is the same surface but 12 primitive ids instead of one.
+Phong exponents.  Spheres are taken when the caller passes tessellate=(nu, nv): each becomes an
+nu x nv UV sphere with radial normals under Milton's T(position) S(2 radius) (:596-611), an
+approximation of the analytic surface.  Instances of named shapes are copied (their geometry
+under the instance's transform chain, with the material active at the instance).  A thin-lens
+camera keeps its aperture, f-stop and focal distance; its autofocus is resolved against the
+resident scene (pathtracer.resolve_autofocus).  A "cube" becomes the 12 triangles of Milton's
+unit cube (Cube.cpp), which is the same surface but 12 primitive ids instead of one.
 """
 from __future__ import annotations
 
@@ -413,7 +417,8 @@ class _Loader:
     SHAPES = ("blob", "cube", "cone", "cylinder", "mesh", "plane", "point", "shape", "sphere", "shapeSet",
               "triangle")
 
-    def __init__(self, base_dir: str):
+    def __init__(self, base_dir: str, tessellate=None):
+        self.tessellate = tessellate
         self.base_dir = base_dir
         self.stack: list[_Node] = []
         self.root: _Node | None = None
@@ -422,6 +427,7 @@ class _Loader:
         self.output = None
         self.output_props: dict = {}
         self.version = None
+        self.named: dict = {}
 
     # -- scene graph stack (SceneGraph::beginNode / endNode)
     def begin(self, node: _Node):
@@ -695,8 +701,20 @@ class _Loader:
     def shape(self, v):
         if not isinstance(v, JObj):
             raise SceneFileError(f"shape must be of type 'object', found '{_tname(v)}'")
-        if "instance" in v:
-            raise SceneFileError("instanced shapes are not supported by the GPU path loader")
+        inst = v.find("instance")
+        if inst is not _MISSING:
+            # an instance of a named shape (SceneNodeInstance, SceneGraph.cpp:135-181): resolved
+            # when the graph is flattened, so the name may be defined anywhere in the file
+            if not isinstance(inst, str):
+                raise SceneFileError(f"shape.instance must be of type 'string', found '{_tname(inst)}'")
+            props = {}
+            _properties({"name": "string"}, v, props)
+            node = _Node("instance", inst)
+            self.name_node(props, node)
+            self.begin(node)
+            self.visit(v, {"material": self.material}, strict=False)
+            self.end()
+            return
         t = v.find("type")
         if t is _MISSING:
             raise SceneFileError("unable to infer shape type")
@@ -713,9 +731,12 @@ class _Loader:
             return self.shape_set(v)
         elif t == "cube":
             pass
+        elif t == "sphere" and self.tessellate:
+            req.update(position="point3", radius="real_t")
         elif t in ("sphere", "cylinder", "cone", "blob", "point", "dynamic"):
             raise SceneFileError(f"shape '{t}' is not a triangle shape; the GPU path renders planes, cubes, "
-                                 "triangles and meshes")
+                                 "triangles and meshes" + (" (spheres with tessellate=(nu, nv))" if t == "sphere"
+                                                           else ""))
         else:
             raise SceneFileError("invalid shape type")
         props = {}
@@ -732,6 +753,22 @@ class _Loader:
             node = _Node("shape", _Shape("triangle", {"v": verts, "uvs": props.get("uvs", (0, 0, 1, 0, 0, 1))}))
         elif t == "cube":
             node = _Node("shape", _Shape("cube"))
+        elif t == "sphere":
+            # Milton's Sphere: a unit-diameter sphere under T(position) S(2 radius) (:575-589),
+            # here an nu x nv UV sphere with radial normals -- an approximation of the analytic
+            # surface, used only when the caller asks for it
+            local = np.eye(4)
+            pos = props.get("position")
+            if pos is not None:
+                local = local @ _trans(pos)
+            if "radius" in props:
+                local = local @ _scale([2.0 * props["radius"]] * 3)
+            tris, nrm = _unit_sphere(*self.tessellate)
+            node = _Node("shape", _Shape("mesh", {"v": tris.reshape(-1, 3).astype(np.float64),
+                                                  "f": np.arange(tris.shape[0] * 3).reshape(-1, 3),
+                                                  "n": nrm.reshape(-1, 3).astype(np.float64),
+                                                  "nf": np.arange(tris.shape[0] * 3).reshape(-1, 3),
+                                                  "path": "sphere"}, local))
         else:  # mesh
             if "path" not in props:
                 raise SceneFileError("missing required key 'path' in 'mesh' (path to mesh data file)")
@@ -747,9 +784,18 @@ class _Loader:
                 verts = (verts - center) / diag
             node = _Node("shape", _Shape("mesh", {"v": verts, "f": faces, "n": normals, "nf": nfaces,
                                                   "path": props["path"]}))
+        self.name_node(props, node)
         self.begin(node)
         self.visit(v, {"material": self.material, "spatialAccel": None}, strict=False)
         self.end()
+
+    def name_node(self, props: dict, node: "_Node"):
+        """Records a 'name'd node for instancing (MiltonJSONSceneLoader.cpp:634-648).  For a plane
+        given by vertices that is its second triangle node, as in the reference."""
+        if "name" in props:
+            if props["name"] in self.named:
+                raise SceneFileError(f"error: duplicate definitions for named node '{props['name']}'")
+            self.named[props["name"]] = node
 
 
 # ------------------------------------------------------------------------------------------
@@ -984,7 +1030,9 @@ def _xf_normals(m, n):
 
 
 class _Flattener:
-    def __init__(self):
+    def __init__(self, named=None):
+        self.named = named or {}
+        self.depth = 0
         self.b = S.SceneBuilder()
         self.mat_index = {}   # id(_Material) -> material record index
         self.default = _Material()
@@ -1008,6 +1056,20 @@ class _Flattener:
             self.active = node.payload
         elif node.kind == "shape":
             self.shape(node.payload, trans)
+        elif node.kind == "instance":
+            # the named node flattened again here: an InstancedShape undoes the instancee's own
+            # transform and applies the instance's (InstancedShape.cpp:16-40), so the copy is the
+            # named shape's object-space geometry under this node's transform chain
+            target = self.named.get(node.payload)
+            if target is None or target.kind != "shape":
+                raise SceneFileError(f"error: instanced node '{node.payload}' not found")
+            if self.depth > 64:
+                raise SceneFileError("instances nested more than 64 deep (a cycle?)")
+            active, in_root = self.active, self.in_root
+            self.depth += 1
+            self.flatten(target, trans)
+            self.depth -= 1
+            self.active, self.in_root = active, in_root
         active, in_root = self.active, self.in_root
         for child in node.children:
             self.flatten(child, trans)
@@ -1203,11 +1265,18 @@ class SceneFile:
         return {k: v for k, v in self.renderer.items() if k not in ("type", "path")}
 
 
-def loads(text: str, base_dir: str = ".", source: str = "<string>") -> SceneFile:
-    """Parses already-read scene text (see read_scene_text for how a file becomes text)."""
-    ld = _Loader(base_dir)
+def _unit_sphere(nu: int, nv: int):
+    from .scenegen import _uv_sphere_fast
+    return _uv_sphere_fast((0.0, 0.0, 0.0), 0.5, nu, nv)
+
+
+def loads(text: str, base_dir: str = ".", source: str = "<string>", tessellate=None) -> SceneFile:
+    """Parses already-read scene text (see read_scene_text for how a file becomes text).
+    tessellate=(nu, nv) turns analytic spheres into UV spheres of that resolution (an
+    approximation of Milton's Sphere; without it they are refused)."""
+    ld = _Loader(base_dir, tessellate)
     ld.root_obj(parse_text(text))
-    fl = _Flattener()
+    fl = _Flattener(ld.named)
     fl.run(ld.root)
     out = dict(ld.output_props)
     w, h, found = 480, 480, False
@@ -1233,10 +1302,11 @@ def loads(text: str, base_dir: str = ".", source: str = "<string>") -> SceneFile
                      width=w, height=h, source=source)
 
 
-def load(path: str) -> SceneFile:
+def load(path: str, tessellate=None) -> SceneFile:
     """Loads a Milton scene file (MiltonJSONSceneLoader::parse); mesh paths are taken relative
     to the scene file's directory when not absolute."""
-    return loads(read_scene_text(path), base_dir=os.path.dirname(os.path.abspath(path)), source=path)
+    return loads(read_scene_text(path), base_dir=os.path.dirname(os.path.abspath(path)), source=path,
+                 tessellate=tessellate)
 
 
 def path_tracer(sf: SceneFile):

@@ -249,3 +249,39 @@ def test_output_filters():
         ("mitchell", 2.0, {"B": 1 / 3, "C": 1 / 3})
     with pytest.raises(L.SceneFileError, match="invalid filter"):
         L.loads(_scene('"triangle" : { }', '"output" : { "filter" : { "type" : "sharp" } },'))
+
+
+def test_instances_copy_named_shapes():
+    text = _scene('"material" : { "bsdf" : { "type" : "diffuse", "kd" : 0.2 }, '
+                  '"triangle" : { "name" : "t", "vertices" : [0,0,0, 1,0,0, 0,0,1] } }, '
+                  '"transform" : { "translate" : [0, 5, 0], "shape" : { "instance" : "t" } }, '
+                  '"material" : { "bsdf" : { "type" : "diffuse", "kd" : 0.7 }, '
+                  '"transform" : { "translate" : [3, 0, 0], "shape" : { "instance" : "t" } } }')
+    s = L.loads(text).scene
+    assert s.ntri == 3
+    # materials first: the original, then the instance under the second material, then the one
+    # under the top-level transform (default material)
+    assert np.allclose(s.tri_v[0, 0], [0, 0, 0]) and np.allclose(s.tri_v[1, 0], [3, 0, 0])
+    assert np.allclose(s.tri_v[2, 0], [0, 5, 0])
+    assert s.materials[s.tri_mat[0], 1] == np.float32(0.2) and s.materials[s.tri_mat[1], 1] == np.float32(0.7)
+    assert s.tri_mat[2] == 0
+    with pytest.raises(L.SceneFileError, match="not found"):
+        L.loads(_scene('"shape" : { "instance" : "nope" }'))
+    with pytest.raises(L.SceneFileError, match="duplicate"):
+        L.loads(_scene('"triangle" : { "name" : "a" }, "plane" : { "name" : "a" }'))
+
+
+def test_spheres_tessellate_only_on_request():
+    body = ('"transform" : { "translate" : [0, 1, 0], '
+            '"sphere" : { "position" : [2, 0, 0], "radius" : 0.75 } }')
+    with pytest.raises(L.SceneFileError, match="not a triangle shape"):
+        L.loads(_scene(body))
+    s = L.loads(_scene(body), tessellate=(16, 9)).scene
+    assert s.ntri == 16 * 9 * 2 - 2 * 16
+    # graph transform after the sphere's own T(position) S(2 radius) on a unit-diameter sphere
+    v = s.tri_v.reshape(-1, 3).astype(np.float64)
+    r = np.linalg.norm(v - [2, 1, 0], axis=1)
+    assert np.allclose(r, 0.75, atol=1e-5)
+    # mesh normals keep the inverse-transpose length (normalised per hit after interpolation)
+    n = s.tri_n.reshape(-1, 3).astype(np.float64)
+    assert np.allclose(n / np.linalg.norm(n, axis=1, keepdims=True), (v - [2, 1, 0]) / 0.75, atol=1e-5)
