@@ -71,7 +71,10 @@ typedef struct {
  *   tri_mat    ntri material indices
  *   tri_light  ntri light indices (-1 = not an emitter); NULL = none
  *   tri_flags  ntri MGPU_TRI_* flags; NULL = all two-sided
- *   materials  nmat*16 floats: type, kd[3], ks[3], n, ior, transparency, 0...
+ *   materials  nmat*16 floats: type, kd[3], ks[3], n, ior, transparency, then texture slots
+ *              [10] kd, [11] ks, [12] transparency, [13] bump map: 1 + index into textures
+ *              (0 = none; a textured key replaces the constant, Material::getSpectralSampleSet,
+ *              Material.cpp:229-283), [14..15] 0
  *   lights     nlight*16 floats: center[3], ex[3], ez[3], normal[3], area, Le[3]
  *              (a Milton `Plane` under a transform: getPosition(u,v) = center + (u-.5)ex + (v-.5)ez,
  *               Plane.cpp:91-93; Le = power / (area * pi), Emitter.cpp:34-50)
@@ -89,7 +92,13 @@ typedef struct {
  *                                   and lands at barycentrics (r1, v, r2) / (r1 + v + r2) with two
  *                                   more uniforms r1, r2, normal = interpolated vertex normals
  *                                   (Mesh::getPosition / getPoint, Mesh.cpp:436-448,
- *                                   MeshTriangle::getPosition, MeshTriangle.cpp:299-333)          */
+ *                                   MeshTriangle::getPosition, MeshTriangle.cpp:299-333)
+ *   tri_uv     NULL (every uv is (0, 0)) or ntri*6 floats: the uv of each vertex; a hit's uv is
+ *              their barycentric interpolation (Shape::_getUV of the shape the triangle came from:
+ *              Triangle.cpp:23-39, Plane.cpp:52-59, Cube.cpp:84-105 and Mesh.cpp:408-416 are
+ *              all affine over a triangle, so per-vertex uvs reproduce them)
+ *   textures   ntex records (mgpu_texture), referenced by the material texture slots          */
+typedef struct mgpu_texture mgpu_texture;
 typedef struct {
   int64_t ntri;
   const float *tri_v;
@@ -102,7 +111,38 @@ typedef struct {
   int32_t nlight;
   const float *lights;
   const float *light_ext;
+  const float *tri_uv;
+  int32_t ntex;
+  const mgpu_texture *textures;
 } mgpu_scene_desc;
+
+/* A material's image map (Material::getSample, Material.cpp:285-301, and the bump map of
+ * Material::_initShadingNormal, :179-225).  rgb: width*height*3 linear values, row 0 = the
+ * image's first (top) row; 8-bit images are byte / 255 (Rgba32 -> RgbaHDR, Rgba.inl:32-40).
+ * A lookup at uv takes texel (floor(clamp(frac(u repeat_u) width, 0, width - 1)), same for v
+ * and rows).
+ *   MGPU_TEX_COLOR  the texel value is KernelFilter::apply (KernelFilter.cpp:106-140) of the
+ *                   image at that texel: sum w(i, j) rgb[clamped row + i, col + j] / sum w with
+ *                   the material's filter (type, support, p1, p2 as mgpu_film_set_filter; w =
+ *                   filter(i - 1/2, j - 1/2) over the (ceil(support) | 1)^2 offsets, the
+ *                   kernel KernelFilter::_computeKernel builds).  Computed once per texel on the
+ *                   device when the scene is created.
+ *   MGPU_TEX_BUMP   the shading normal becomes normalize(N + bump_intensity (gx U + gy V)), with
+ *                   U, V = N's orthonormal basis and gx, gy central luminance differences
+ *                   (0.2126 r + 0.7152 g + 0.0722 b) at the texel, clamped at the edges; N
+ *                   unchanged where both are 0.  A bump-mapped material may not emit.       */
+struct mgpu_texture {
+  int32_t width, height;
+  const float *rgb;
+  int32_t kind;        /* MGPU_TEX_COLOR or MGPU_TEX_BUMP */
+  int32_t filter;      /* MGPU_FILTER_BOX .. MGPU_FILTER_LANCZOS_SINC (colour maps) */
+  float support, p1, p2;
+  float repeat_u, repeat_v;
+  float bump_intensity;
+};
+
+#define MGPU_TEX_COLOR 0
+#define MGPU_TEX_BUMP 1
 
 #define MGPU_LIGHT_PLANE 0
 #define MGPU_LIGHT_TRIANGLE 1
@@ -160,6 +200,11 @@ int mgpu_scene_bytes(const mgpu_scene *scene, uint64_t *out);
 /* Device bytes mgpu_scene_create would allocate for this accel with nmat materials and nlight
  * lights (admission against a memory budget before uploading).  No reference counterpart. */
 int mgpu_accel_device_bytes(const mgpu_accel *accel, int32_t nmat, int32_t nlight, uint64_t *out);
+/* The same for a full description, textures and uvs included. */
+int mgpu_scene_device_bytes(const mgpu_scene_desc *desc, const mgpu_accel *accel, uint64_t *out);
+/* Texel values of texture tex as the device holds them (after filtering): width*height*4
+ * floats (colour maps: rgb, 0; bump maps: gx, gy, 0, 0).  Synchronises.  For tests. */
+int mgpu_scene_read_texels(const mgpu_scene *scene, int32_t tex, float *out, void *stream);
 /* Tuning: how many of the breadth-first top 16-byte pairs the traversal kernels stage in
  * shared memory per block (0 = none; clamped to what the builder laid out breadth-first). */
 int mgpu_scene_set_top_pairs(mgpu_scene *scene, uint32_t n);

@@ -31,11 +31,18 @@ class KdStats(C.Structure):
                                           "bytes_nodes", "bytes_refs")] + [("build_seconds", C.c_double)]
 
 
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.c_void_p), ("kind", C.c_int32),
+                ("filter", C.c_int32), ("support", C.c_float), ("p1", C.c_float), ("p2", C.c_float),
+                ("repeat_u", C.c_float), ("repeat_v", C.c_float), ("bump_intensity", C.c_float)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("ntri", C.c_int64), ("tri_v", C.c_void_p), ("tri_n", C.c_void_p), ("tri_mat", C.c_void_p),
                 ("tri_light", C.c_void_p), ("tri_flags", C.c_void_p), ("nmat", C.c_int32),
                 ("materials", C.c_void_p), ("nlight", C.c_int32), ("lights", C.c_void_p),
-                ("light_ext", C.c_void_p)]
+                ("light_ext", C.c_void_p), ("tri_uv", C.c_void_p), ("ntex", C.c_int32),
+                ("textures", C.POINTER(Texture))]
 
 
 class RenderParams(C.Structure):
@@ -85,6 +92,8 @@ SIGNATURES = [
     ("mgpu_scene_bytes", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     ("mgpu_scene_set_top_pairs", C.c_int, [C.c_void_p, C.c_uint32]),
     ("mgpu_accel_device_bytes", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]),
+    ("mgpu_scene_device_bytes", C.c_int, [C.POINTER(SceneDesc), C.c_void_p, C.POINTER(C.c_uint64)]),
+    ("mgpu_scene_read_texels", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     ("mgpu_trace_closest", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("mgpu_trace_any", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("mgpu_trace_closest_counted", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,

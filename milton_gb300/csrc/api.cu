@@ -84,9 +84,12 @@ static void register_staging(mgpu_accel *a) {
 
 // Offsets of the arrays in a scene's one device allocation (256-byte aligned each).
 struct SceneLayout {
-  size_t off_pairs, off_refs, off_tris, off_shade, off_mats, off_lights, off_err, total;
+  size_t off_pairs, off_refs, off_tris, off_shade, off_mats, off_lights, off_uv, off_texrec, off_texels, off_err,
+      total;
 };
-static SceneLayout scene_layout(const mgpu_accel *a, int32_t nmat, int32_t nlight) {
+// uv_tris: triangles with uploaded uvs (0 or all); ntex textures holding texels texels in all
+static SceneLayout scene_layout(const mgpu_accel *a, int32_t nmat, int32_t nlight, int64_t uv_tris = 0,
+                                int32_t ntex = 0, uint64_t texels = 0) {
   SceneLayout L;
   L.off_pairs = 0;
   L.off_refs = align_up(L.off_pairs + a->dpairs.size() * sizeof(Pair), 256);
@@ -94,7 +97,10 @@ static SceneLayout scene_layout(const mgpu_accel *a, int32_t nmat, int32_t nligh
   L.off_shade = align_up(L.off_tris + std::max<size_t>(a->tris.size(), 1) * sizeof(F4), 256);
   L.off_mats = align_up(L.off_shade + std::max<size_t>(a->shade.size(), 1) * sizeof(float4), 256);
   L.off_lights = align_up(L.off_mats + (size_t)std::max(nmat, 0) * 16 * sizeof(float), 256);
-  L.off_err = align_up(L.off_lights + std::max<size_t>((size_t)std::max(nlight, 0), 1) * 32 * sizeof(float), 256);
+  L.off_uv = align_up(L.off_lights + std::max<size_t>((size_t)std::max(nlight, 0), 1) * 32 * sizeof(float), 256);
+  L.off_texrec = align_up(L.off_uv + (size_t)std::max<int64_t>(uv_tris, 0) * 3 * sizeof(float2), 256);
+  L.off_texels = align_up(L.off_texrec + (size_t)std::max(ntex, 0) * 2 * sizeof(float4), 256);
+  L.off_err = align_up(L.off_texels + (size_t)texels * sizeof(float4), 256);
   L.total = L.off_err + 256;
   return L;
 }
@@ -372,13 +378,15 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
         return fail(MGPU_E_INVALID, "mgpu_scene_create: mesh light " + std::to_string(i) + " has a bad triangle run");
     }
   }
+  TexPlan tp;
+  if (int rc = tex_plan(desc, tp)) return rc;
   const KdTree &tr = accel->tree;
   mgpu_accel *acc = const_cast<mgpu_accel *>(accel);
   register_staging(acc);
   const std::vector<Pair> &dpairs = accel->dpairs;
   const std::vector<F4> &ltris = accel->ltris, &tris = accel->tris;
   const std::vector<float4> &shade = accel->shade;
-  const SceneLayout L = scene_layout(accel, desc->nmat, desc->nlight);
+  const SceneLayout L = scene_layout(accel, desc->nmat, desc->nlight, tp.uv ? T : 0, desc->ntex, tp.texels);
   const size_t off_pairs = L.off_pairs, off_refs = L.off_refs, off_tris = L.off_tris, off_shade = L.off_shade,
                off_mats = L.off_mats, off_lights = L.off_lights, off_err = L.off_err, total = L.total;
   const size_t sz_pairs = dpairs.size() * sizeof(Pair), sz_mats = (size_t)desc->nmat * 16 * sizeof(float);
@@ -403,6 +411,7 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   if (e == cudaSuccess) e = up(off_shade, shade.data(), shade.size() * sizeof(float4));
   if (e == cudaSuccess) e = up(off_mats, desc->materials, sz_mats);
   if (e == cudaSuccess && desc->nlight > 0) e = up(off_lights, lrec.data(), lrec.size() * sizeof(float));
+  if (e == cudaSuccess && tp.uv) e = up(L.off_uv, desc->tri_uv, (size_t)T * 6 * sizeof(float));
   if (e == cudaSuccess) e = cudaMemsetAsync(base + off_err, 0, 256, st);
   // materials and lights are the caller's pageable arrays: wait for the copies
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -411,6 +420,21 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     delete s;
     return cuda_fail(e, "mgpu_scene_create: upload");
   }
+  if (desc->ntex > 0) {
+    if (int rc = tex_upload(desc, tp, (float4 *)(base + L.off_texrec), (float4 *)(base + L.off_texels), st)) {
+      cudaFree(s->d_block);
+      delete s;
+      return rc;
+    }
+    s->d_texrec = (float4 *)(base + L.off_texrec);
+    s->d_texels = (float4 *)(base + L.off_texels);
+    s->tex_offset = tp.offset;
+    for (int i = 0; i < desc->ntex; ++i) {
+      s->tex_w.push_back(desc->textures[i].width);
+      s->tex_h.push_back(desc->textures[i].height);
+    }
+  }
+  if (tp.uv) s->d_uv = (float2 *)(base + L.off_uv);
   s->view.pairs = (const Pair *)(base + off_pairs);
   s->view.ltris = (const F4 *)(base + off_refs);
   s->view.tris = (const F4 *)(base + off_tris);
@@ -462,6 +486,25 @@ int mgpu_scene_bytes(const mgpu_scene *s, uint64_t *out) {
 int mgpu_accel_device_bytes(const mgpu_accel *a, int32_t nmat, int32_t nlight, uint64_t *out) {
   if (!a || !out || nmat < 0 || nlight < 0) return fail(MGPU_E_INVALID, "mgpu_accel_device_bytes: bad argument");
   *out = scene_layout(a, nmat, nlight).total;
+  return MGPU_OK;
+}
+
+int mgpu_scene_device_bytes(const mgpu_scene_desc *desc, const mgpu_accel *a, uint64_t *out) {
+  if (!desc || !a || !out || desc->nmat < 0 || desc->nlight < 0)
+    return fail(MGPU_E_INVALID, "mgpu_scene_device_bytes: bad argument");
+  TexPlan tp;
+  if (int rc = tex_plan(desc, tp)) return rc;
+  *out = scene_layout(a, desc->nmat, desc->nlight, tp.uv ? desc->ntri : 0, desc->ntex, tp.texels).total;
+  return MGPU_OK;
+}
+
+int mgpu_scene_read_texels(const mgpu_scene *s, int32_t tex, float *out, void *stream) {
+  if (!s || !out || tex < 0 || tex >= (int32_t)s->tex_offset.size())
+    return fail(MGPU_E_INVALID, "mgpu_scene_read_texels: bad argument");
+  cudaStream_t st = as_stream(stream);
+  const size_t n = (size_t)s->tex_w[tex] * s->tex_h[tex];
+  MGPU_CUDA(cudaMemcpyAsync(out, s->d_texels + s->tex_offset[tex], n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  MGPU_CUDA(cudaStreamSynchronize(st));
   return MGPU_OK;
 }
 

@@ -35,6 +35,16 @@ constexpr uint32_t kErrIndex = 2u;
 
 int device_sm_count();
 
+// material image maps (texture.cu): texel offsets of each texture in the scene's texel pool
+struct TexPlan {
+  bool uv = false;               // per-vertex uvs uploaded
+  std::vector<uint64_t> offset;  // first texel of each texture
+  uint64_t texels = 0;           // texels in the pool
+  uint64_t max_src = 0;          // texels of the largest texture
+};
+int tex_plan(const mgpu_scene_desc *desc, TexPlan &plan);
+int tex_upload(const mgpu_scene_desc *desc, const TexPlan &plan, float4 *d_texrec, float4 *d_texels, cudaStream_t st);
+
 }  // namespace mgpu
 
 struct mgpu_accel {
@@ -56,6 +66,11 @@ struct mgpu_scene {
   float4 *d_shade = nullptr;    // 3 per triangle: (n0, mat), (n1, light), (n2, 0)
   float *d_mats = nullptr;
   float *d_lights = nullptr;
+  float2 *d_uv = nullptr;       // 3 per triangle by id (nullptr: every uv is (0, 0))
+  float4 *d_texrec = nullptr;   // 2 per texture: (texel offset, width, height, kind), (repeat u, v, bump intensity, 0)
+  float4 *d_texels = nullptr;   // filtered colour texels / bump gradients
+  std::vector<uint64_t> tex_offset;
+  std::vector<int32_t> tex_w, tex_h;
   int32_t nmat = 0, nlight = 0;
   uint32_t top_pairs = 0;       // pairs staged in shared memory by the traversal kernels
   uint32_t top_pairs_max = 0;   // breadth-first pairs available for staging

@@ -19,6 +19,7 @@ struct Material {
   V3 kd, ks;
   float n, ior, transparency;
   float kda, ksa;    // channel averages (ModifiedPhongBSDF::init)
+  int tex_kd, tex_ks, tex_tr, tex_bump;  // 1 + texture index, 0 = none
 };
 
 MGPU_HD Material material_from(const float *m) {
@@ -31,7 +32,35 @@ MGPU_HD Material material_from(const float *m) {
   r.transparency = m[9];
   r.kda = (r.kd.x + r.kd.y + r.kd.z) / 3.0f;
   r.ksa = (r.ks.x + r.ks.y + r.ks.z) / 3.0f;
+  r.tex_kd = (int)m[10];
+  r.tex_ks = (int)m[11];
+  r.tex_tr = (int)m[12];
+  r.tex_bump = (int)m[13];
   return r;
+}
+
+// Texel of a lookup at (u, v) in a width x height map repeated (ru, rv) times: Milton's
+// getSample / _initShadingNormal position, x = clamp((s - floor(s)) width, 0, width - 1) with
+// s = u ru, floored (Material.cpp:196-201, 292-299).
+MGPU_HD int tex_texel(float u, float v, int w, int h, float ru, float rv) {
+  const float s = u * ru, t = v * rv;
+  const float x = fminf(fmaxf((s - floorf(s)) * (float)w, 0.0f), (float)(w - 1));
+  const float y = fminf(fmaxf((t - floorf(t)) * (float)h, 0.0f), (float)(h - 1));
+  return (int)y * w + (int)x;
+}
+
+// Textured keys replace the constants (Material::getSpectralSampleSet with a file name,
+// Material.cpp:260-283); DielectricBSDF uses the average transparency (DielectricBSDF.cpp:51-52).
+MGPU_HD void tex_apply(Material &m, int slot, float r, float g, float b) {
+  if (slot == 0) {
+    m.kd = v3(r, g, b);
+    m.kda = (r + g + b) / 3.0f;
+  } else if (slot == 1) {
+    m.ks = v3(r, g, b);
+    m.ksa = (r + g + b) / 3.0f;
+  } else {
+    m.transparency = (r + g + b) / 3.0f;
+  }
 }
 
 MGPU_HD bool is_specular(const Material &m) { return m.type == 2; }
@@ -193,6 +222,16 @@ MGPU_HD void onb(V3 n, V3 &U, V3 &W) {
   if (fabsf(dot(up, n)) > 0.8f) up = v3(1.0f, 0.0f, 0.0f);
   U = normalize(cross(up, n));
   W = normalize(cross(n, U));
+}
+
+// Bump-mapped shading normal (Material::_initShadingNormal, Material.cpp:205-224): N unchanged
+// where both luminance differences are 0 (EQ against 0 is |x| < EPSILON), else
+// normalize(N + intensity (gx U + gy V)) with U, V = N's orthonormal basis.
+MGPU_HD V3 bump_normal(V3 N, float gx, float gy, float intensity) {
+  if (fabsf(gx) < kEps && fabsf(gy) < kEps) return N;
+  V3 U, W;
+  onb(N, U, W);
+  return normalize(N + (U * gx + W * gy) * intensity);
 }
 
 // Vector3::cosRandom + convertHemisphere (Vector.cpp:21-29, Vector3.inl:18-21):

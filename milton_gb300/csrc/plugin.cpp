@@ -13,9 +13,11 @@ struct mgpu_renderer {
   std::map<std::string, std::string> props;  // PropertyMap (text values)
   // owned copies of the scene arrays
   int64_t ntri = 0;
-  std::vector<float> v, n, mats, lights, light_ext;
+  std::vector<float> v, n, mats, lights, light_ext, uv;
   std::vector<int32_t> mat, light;
   std::vector<uint32_t> flags;
+  std::vector<std::vector<float>> tex_rgb;  // owned texel data of each texture
+  std::vector<mgpu_texture> tex;
   bool has_scene = false, has_n = false, has_light = false, has_flags = false;
   int32_t nmat = 0, nlight = 0;
   float camera[16] = {0, 0, 0, 0, 0, -1, 0, 1, 0, 45, 1, 0, 0, 1, 0, 0};
@@ -57,6 +59,9 @@ struct mgpu_renderer {
     d.nlight = nlight;
     d.lights = lights.data();
     d.light_ext = light_ext.empty() ? nullptr : light_ext.data();
+    d.tri_uv = uv.empty() ? nullptr : uv.data();
+    d.ntex = (int32_t)tex.size();
+    d.textures = tex.empty() ? nullptr : tex.data();
     return d;
   }
 };
@@ -112,6 +117,18 @@ int mgpu_renderer_set_scene(mgpu_renderer *r, const mgpu_scene_desc *d) {
   else r->lights.assign(16, 0.0f);
   if (d->nlight > 0 && d->light_ext) r->light_ext.assign(d->light_ext, d->light_ext + 16 * (size_t)d->nlight);
   else r->light_ext.clear();
+  if (d->tri_uv) r->uv.assign(d->tri_uv, d->tri_uv + 6 * T);
+  else r->uv.clear();
+  if (d->ntex < 0 || (d->ntex > 0 && !d->textures)) return bad("mgpu_renderer_set_scene: bad textures");
+  r->tex_rgb.clear();
+  r->tex.clear();
+  for (int32_t i = 0; i < d->ntex; ++i) {
+    mgpu_texture t = d->textures[i];
+    if (t.width <= 0 || t.height <= 0 || !t.rgb) return bad("mgpu_renderer_set_scene: bad texture");
+    r->tex_rgb.emplace_back(t.rgb, t.rgb + (size_t)t.width * t.height * 3);
+    r->tex.push_back(t);
+  }
+  for (int32_t i = 0; i < d->ntex; ++i) r->tex[i].rgb = r->tex_rgb[i].data();
   r->has_scene = true;
   r->initted = false;
   return MGPU_OK;

@@ -61,6 +61,9 @@ struct JobArgs {
   const float4 *shade;
   const float4 *mats;    // 4 per material
   const float4 *lights;  // 4 per light
+  const float2 *uv;      // 3 per triangle (nullptr: every uv is (0, 0))
+  const float4 *texrec;  // 2 per texture
+  const float4 *texels;
   int32_t nlight, nl_slots, sh_cell_bits;
   Camera cam;
   Rng rng;
@@ -153,6 +156,30 @@ __device__ __forceinline__ Material load_mat(const JobArgs &J, int i) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) mm[k] = __ldg(J.mats + 4 * i + k);
   return material_from(m);
+}
+
+// Image maps at a hit of triangle prim with barycentrics (b0, b1, b2): the uv (Shape::_getUV,
+// interpolated from the per-vertex uvs), then each textured key of the material and the bump
+// map (Material::initSurfacePoint, Material.cpp:157-225).
+__device__ __noinline__ void apply_textures(const JobArgs &J, int prim, float b0, float b1, float b2, Material &m,
+                                            V3 &ns) {
+  float u = 0.0f, v = 0.0f;
+  if (J.uv) {
+    const float2 a = __ldg(J.uv + 3 * (int64_t)prim), b = __ldg(J.uv + 3 * (int64_t)prim + 1),
+                 c = __ldg(J.uv + 3 * (int64_t)prim + 2);
+    u = a.x * b0 + b.x * b1 + c.x * b2;
+    v = a.y * b0 + b.y * b1 + c.y * b2;
+  }
+  const int slots[4] = {m.tex_kd, m.tex_ks, m.tex_tr, m.tex_bump};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (slots[k] == 0) continue;
+    const float4 r0 = __ldg(J.texrec + 2 * (slots[k] - 1)), r1 = __ldg(J.texrec + 2 * (slots[k] - 1) + 1);
+    const int w = __float_as_int(r0.y), h = __float_as_int(r0.z);
+    const float4 t = __ldg(J.texels + __float_as_uint(r0.x) + tex_texel(u, v, w, h, r1.x, r1.y));
+    if (k < 3) tex_apply(m, k, t.x, t.y, t.z);
+    else ns = bump_normal(ns, t.x, t.y, r1.z);
+  }
 }
 
 // light records: 8 float4 each (base record, then the extension)
@@ -335,6 +362,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         int mi = __float_as_int(s0.w);
         self = __float_as_int(s1.w);
         m = load_mat(J, mi);
+        if ((m.tex_kd | m.tex_ks | m.tex_tr | m.tex_bump) != 0) apply_textures(J, prim, b0, b1, b2, m, ns);
         bool spec = is_specular(m);
         if (spec) flags |= kFlagSpecular;
         if (self >= 0) {
@@ -911,6 +939,9 @@ static JobArgs job_args(const Job &j) {
   J.shade = sc->d_shade;
   J.mats = (const float4 *)sc->d_mats;
   J.lights = (const float4 *)sc->d_lights;
+  J.uv = sc->d_uv;
+  J.texrec = sc->d_texrec;
+  J.texels = sc->d_texels;
   J.nlight = sc->nlight;
   J.cam = make_camera(rp->camera);
   J.rng.k0 = (uint32_t)rp->seed;

@@ -32,9 +32,11 @@ enum SceneState { kIdle = 0, kBuilding = 1, kBuilt = 2, kBuildFailed = 3 };
 
 struct SrvScene {
   int64_t ntri = 0;
-  std::vector<float> v, n, mats, lights, light_ext;
+  std::vector<float> v, n, mats, lights, light_ext, uv;
   std::vector<int32_t> mat, light;
   std::vector<uint32_t> flags;
+  std::vector<std::vector<float>> tex_rgb;  // owned texel data of each texture
+  std::vector<mgpu_texture> tex;
   int32_t nmat = 0, nlight = 0;
   // written by a build thread, read under the server mutex
   int state = kIdle;
@@ -60,6 +62,9 @@ struct SrvScene {
     d.nlight = nlight;
     d.lights = lights.empty() ? nullptr : lights.data();
     d.light_ext = light_ext.empty() ? nullptr : light_ext.data();
+    d.tri_uv = uv.empty() ? nullptr : uv.data();
+    d.ntex = (int32_t)tex.size();
+    d.textures = tex.empty() ? nullptr : tex.data();
     return d;
   }
 };
@@ -128,7 +133,7 @@ void build_worker(mgpu_server *s) {
     mgpu_accel *acc = nullptr;
     uint64_t bytes = 0;
     int rc = mgpu_accel_build(&d, &s->p.kd, &acc);
-    if (rc == MGPU_OK) rc = mgpu_accel_device_bytes(acc, d.nmat, d.nlight, &bytes);
+    if (rc == MGPU_OK) rc = mgpu_scene_device_bytes(&d, acc, &bytes);
     const std::string err = rc == MGPU_OK ? std::string() : std::string(mgpu_last_error());
     std::lock_guard<std::mutex> lk(s->mu);
     if (rc == MGPU_OK) {
@@ -387,6 +392,17 @@ int mgpu_server_add_scene(mgpu_server *s, const mgpu_scene_desc *d, int32_t *sce
     sc->nlight = d->nlight;
     if (d->nlight > 0) sc->lights.assign(d->lights, d->lights + 16 * (size_t)d->nlight);
     if (d->nlight > 0 && d->light_ext) sc->light_ext.assign(d->light_ext, d->light_ext + 16 * (size_t)d->nlight);
+    if (d->tri_uv) sc->uv.assign(d->tri_uv, d->tri_uv + 6 * T);
+    if (d->ntex < 0 || (d->ntex > 0 && !d->textures))
+      return fail(MGPU_E_INVALID, "mgpu_server_add_scene: bad textures");
+    for (int32_t i = 0; i < d->ntex; ++i) {
+      mgpu_texture t = d->textures[i];
+      if (t.width <= 0 || t.height <= 0 || !t.rgb)
+        return fail(MGPU_E_INVALID, "mgpu_server_add_scene: bad texture " + std::to_string(i));
+      sc->tex_rgb.emplace_back(t.rgb, t.rgb + (size_t)t.width * t.height * 3);
+      sc->tex.push_back(t);
+    }
+    for (int32_t i = 0; i < d->ntex; ++i) sc->tex[i].rgb = sc->tex_rgb[i].data();
   } catch (...) {
     return fail(MGPU_E_NOMEM, "mgpu_server_add_scene: out of host memory");
   }

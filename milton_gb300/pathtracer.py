@@ -48,7 +48,16 @@ def _desc(scene: Scene) -> N.SceneDesc:
     lights = scene.lights if len(scene.lights) else np.zeros((1, 16), np.float32)
     d.lights = N.ptr(lights)
     d.light_ext = N.ptr(scene.light_ext) if len(scene.lights) else None
-    d._keep = (scene, lights)  # keep buffers alive while the struct is used
+    d.tri_uv = None if scene.tri_uv is None else N.ptr(scene.tri_uv)
+    d.ntex = len(scene.textures)
+    texs = (N.Texture * max(1, len(scene.textures)))()
+    for i, t in enumerate(scene.textures):
+        h, w, _ = t.rgb.shape
+        f, support, p1, p2 = t.filter_params()
+        texs[i] = N.Texture(w, h, N.ptr(t.rgb), t.kind, f, support, p1, p2, t.repeat_u, t.repeat_v,
+                            t.bump_intensity)
+    d.textures = texs
+    d._keep = (scene, lights, texs)  # keep buffers alive while the struct is used
     return d
 
 
@@ -121,6 +130,13 @@ class DeviceScene:
         v = C.c_uint64()
         N.check(self._lib.mgpu_scene_bytes(self.handle, C.byref(v)))
         return v.value
+
+    def texels(self, tex: int, stream=None) -> np.ndarray:
+        """Texture tex as the device holds it: (H, W, 4) float32 (filtered rgb, or bump gx, gy)."""
+        h, w, _ = self.scene.textures[tex].rgb.shape
+        out = np.zeros((h, w, 4), np.float32)
+        N.check(self._lib.mgpu_scene_read_texels(self.handle, tex, N.ptr(out), _stream_handle(stream)))
+        return out
 
     def close(self):
         if self.handle:

@@ -15,6 +15,9 @@ A `Scene` holds exactly what crosses the C ABI (``mgpu_scene_desc``):
                                    (include/mgpu.h); all zeros = planes
 * ``camera``    (16,)     float32  eye[3], look[3], up[3], heightAngle (deg), aspectRatio, aperture (m),
                                    focal length, focal distance, 0, 0 (aperture 0 = pinhole)
+* ``tri_uv``    (T, 3, 2) float32  per-vertex uvs, or None (every uv is (0, 0))
+* ``textures``  list of `Texture`: image maps named by the material texture slots
+                                   [10] kd, [11] ks, [12] transparency, [13] bump (1 + index)
 
 Materials use Milton's keys and defaults (Material.cpp:67-92, DiffuseBSDF.cpp:44-46,
 ModifiedPhongBSDF.cpp:48-81, DielectricBSDF.cpp:48-53): diffuse ``kd`` (0.5), Phong ``kd``/
@@ -114,6 +117,38 @@ def camera(eye, focus=None, look=None, up=(0, 1, 0), height_angle=45.0, aspect=1
     return c
 
 
+TEX_COLOR = 0
+TEX_BUMP = 1
+FILTERS = {"box": 1, "triangle": 2, "gaussian": 3, "mitchell": 4, "lanczosSinc": 5}
+
+
+@dataclass
+class Texture:
+    """A material's image map (include/mgpu.h, mgpu_texture): rgb (H, W, 3) linear values, row 0
+    the top row.  Colour maps are filtered per texel with the material's filter (kind, support,
+    params as for the film); bump maps keep luminance differences."""
+    rgb: np.ndarray
+    kind: int = TEX_COLOR
+    filter: tuple = ("triangle", 2.0, {})
+    repeat_u: float = 1.0
+    repeat_v: float = 1.0
+    bump_intensity: float = 5.0
+
+    def __post_init__(self):
+        self.rgb = np.ascontiguousarray(self.rgb, np.float32)
+        if self.rgb.ndim != 3 or self.rgb.shape[2] != 3 or self.rgb.shape[0] < 1 or self.rgb.shape[1] < 1:
+            raise ValueError("texture rgb must be (H, W, 3)")
+        if self.filter[0] not in FILTERS:
+            raise ValueError(f"unknown texture filter {self.filter[0]!r}")
+
+    def filter_params(self) -> tuple[int, float, float, float]:
+        kind, support, params = self.filter
+        p1 = {"gaussian": params.get("sigma", 1.0), "mitchell": params.get("B", 1.0 / 3.0),
+              "lanczosSinc": params.get("tau", 3.0)}.get(kind, 0.0)
+        p2 = params.get("C", 1.0 / 3.0) if kind == "mitchell" else 0.0
+        return FILTERS[kind], float(support), float(p1), float(p2)
+
+
 @dataclass
 class Scene:
     tri_v: np.ndarray
@@ -127,6 +162,8 @@ class Scene:
     name: str = "scene"
     shapes: list = field(default_factory=list)  # (name, first triangle, count) in ShapeSet order
     light_ext: np.ndarray | None = None
+    tri_uv: np.ndarray | None = None
+    textures: list = field(default_factory=list)
 
     def __post_init__(self):
         self.tri_v = np.ascontiguousarray(self.tri_v, np.float32).reshape(-1, 3, 3)
@@ -155,14 +192,22 @@ class Scene:
             raise ValueError("material index out of range")
         if T and (self.tri_light.min() < -1 or self.tri_light.max() >= len(self.lights)):
             raise ValueError("light index out of range")
+        if self.tri_uv is not None:
+            self.tri_uv = np.ascontiguousarray(self.tri_uv, np.float32).reshape(-1, 3, 2)
+            if self.tri_uv.shape[0] != T:
+                raise ValueError(f"tri_uv has {self.tri_uv.shape[0]} rows, expected {T}")
+        slots = self.materials[:, 10:14] if len(self.materials) else np.zeros((0, 4), np.float32)
+        if np.any(slots < 0) or np.any(slots > len(self.textures)) or np.any(slots != np.floor(slots)):
+            raise ValueError("material texture slot out of range")
 
     @property
     def ntri(self) -> int:
         return int(self.tri_v.shape[0])
 
     def nbytes(self) -> int:
-        return sum(a.nbytes for a in (self.tri_v, self.tri_n, self.tri_mat, self.tri_light, self.tri_flags,
-                                      self.materials, self.lights, self.light_ext))
+        extra = (0 if self.tri_uv is None else self.tri_uv.nbytes) + sum(t.rgb.nbytes for t in self.textures)
+        return extra + sum(a.nbytes for a in (self.tri_v, self.tri_n, self.tri_mat, self.tri_light, self.tri_flags,
+                                              self.materials, self.lights, self.light_ext))
 
 
 class SceneBuilder:
@@ -170,6 +215,8 @@ class SceneBuilder:
 
     def __init__(self):
         self.v, self.n, self.mat, self.light, self.flags = [], [], [], [], []
+        self.uv: list[np.ndarray | None] = []
+        self.textures: list[Texture] = []
         self.materials: list[np.ndarray] = []
         self.lights: list[np.ndarray] = []
         self.light_ext: list[np.ndarray] = []
@@ -180,8 +227,15 @@ class SceneBuilder:
         self.materials.append(np.asarray(rec, np.float32))
         return len(self.materials) - 1
 
-    def add(self, name: str, v: np.ndarray, n: np.ndarray | None, mat: int, light: int = -1, culled: bool = False):
+    def texture(self, tex: Texture) -> int:
+        """Appends an image map; returns the value for a material texture slot (1 + index)."""
+        self.textures.append(tex)
+        return len(self.textures)
+
+    def add(self, name: str, v: np.ndarray, n: np.ndarray | None, mat: int, light: int = -1, culled: bool = False,
+            uv: np.ndarray | None = None):
         v = np.asarray(v, np.float32).reshape(-1, 3, 3)
+        self.uv.append(None if uv is None else np.asarray(uv, np.float32).reshape(v.shape[0], 3, 2))
         if n is None:
             fn = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
             fn = fn / np.linalg.norm(fn, axis=1, keepdims=True)
@@ -245,7 +299,7 @@ class SceneBuilder:
         self.add(name, v[None], np.broadcast_to(rec[9:12], (1, 3, 3)), mat, light=li, culled=culled)
         return li
 
-    def add_mesh_light(self, name: str, v_world, n_world, radiance, mat: int) -> int:
+    def add_mesh_light(self, name: str, v_world, n_world, radiance, mat: int, uv=None) -> int:
         """An emitting Milton `Mesh`: its two-sided triangles and one light record (type 2) over
         their run in the soup, area = the world-space area (Mesh::_getSurfaceArea)."""
         v = np.asarray(v_world, np.float64).reshape(-1, 3, 3)
@@ -259,12 +313,17 @@ class SceneBuilder:
         ext.view(np.uint32)[8] = self._ntri
         ext.view(np.uint32)[9] = v.shape[0]
         li = self.add_light(rec, ext)
-        self.add(name, v, n_world, mat, light=li)
+        self.add(name, v, n_world, mat, light=li, uv=uv)
         return li
 
     def build(self, camera: np.ndarray, name: str = "scene") -> Scene:
         cat = lambda xs, shape, dt: np.concatenate(xs) if xs else np.zeros(shape, dt)  # noqa: E731
+        tri_uv = None
+        if any(u is not None for u in self.uv):
+            tri_uv = np.concatenate([np.zeros((v.shape[0], 3, 2), np.float32) if u is None else u
+                                     for u, v in zip(self.uv, self.v)])
         return Scene(
+            tri_uv=tri_uv, textures=list(self.textures),
             tri_v=cat(self.v, (0, 3, 3), np.float32), tri_n=cat(self.n, (0, 3, 3), np.float32),
             tri_mat=cat(self.mat, (0,), np.int32), tri_light=cat(self.light, (0,), np.int32),
             tri_flags=cat(self.flags, (0,), np.uint32),

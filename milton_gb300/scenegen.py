@@ -9,6 +9,10 @@
              materials 60% Lambertian / 30% modified Phong (n ~ U[10, 200], kd + ks <= 1) / 10%
              dielectric (IOR 1.5); 4 quad lights; 1024x1024, 64 spp, depth 8.
 * ``batch``  many independent scenes of uneven size built from the same recipes.
+* ``textured`` the plain box with image maps: a checker ``kd`` map repeated on the floor, a
+             noise ``ks`` map on a Phong sphere, a ``transparency`` map on a dielectric sphere
+             and a bump map on the back wall (seeded procedural images, material filters of
+             every kind).
 * ``large``  a displaced-grid terrain (fBm heights; 2,800 x 2,800 cells = 15,680,000 triangles
              by default: a 4096^2 vertex grid would be 33.5 M triangles, above the configuration's
              stated ~20 M total) plus 2,000 copied UV spheres of 2,160 triangles resting on it
@@ -21,7 +25,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .scene import SceneBuilder, Scene, camera, dielectric, diffuse, phong
+from .scene import TEX_BUMP, TEX_COLOR, SceneBuilder, Scene, Texture, camera, dielectric, diffuse, phong
 
 
 # ------------------------------------------------------------------------------------------
@@ -136,6 +140,64 @@ def plain(seed: int = 0) -> Scene:
     b.add_quad_light("light", (0.0, 1.999, 0.0), (0.5, 0.0, 0.0), (0.0, 0.0, -0.5), 15.0, lm)
     cam = camera(eye=(0.0, 1.0, 3.75), look=(0.0, 0.0, -1.0), up=(0, 1, 0), height_angle=40.0, aspect=1.0)
     return b.build(cam, name="plain")
+
+
+def textured(seed: int = 0, filters=("triangle", 2.0, {})) -> Scene:
+    """The plain box with image maps (module docstring).  filters: the colour maps' filter
+    (kind, support, params)."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    uv_quad = np.array([[(0, 0), (1, 0), (1, 1)], [(0, 0), (1, 1), (0, 1)]], np.float32)
+    # checker with seeded colours, 16 x 12 texels, repeated 3 x 2 times over the floor
+    cells = (np.add.outer(np.arange(12) // 3, np.arange(16) // 4) % 2).astype(bool)
+    c0, c1 = rng.uniform(0.1, 0.4, 3), rng.uniform(0.5, 0.9, 3)
+    checker = np.where(cells[..., None], c1, c0).astype(np.float32)
+    checker += rng.uniform(-0.05, 0.05, checker.shape).astype(np.float32)
+    kd_tex = b.texture(Texture(np.clip(checker, 0, 1), TEX_COLOR, filters, repeat_u=3.0, repeat_v=2.0))
+    floor = diffuse(0.5)
+    floor[10] = kd_tex
+    walls = {
+        "floor": (((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)), floor),
+        "ceiling": (((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)), diffuse(rng.uniform(0.3, 0.7, 3))),
+        "left": (((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)), diffuse(rng.uniform(0.3, 0.7, 3))),
+        "right": (((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)), diffuse(rng.uniform(0.3, 0.7, 3))),
+    }
+    for name, (pts, rec) in walls.items():
+        b.add(name, quad_tris(*[np.asarray(p, np.float32) for p in pts]), None, b.material(rec), uv=uv_quad)
+    # bump-mapped back wall: seeded height field, 40 x 40 texels
+    heights = rng.uniform(0, 1, (10, 10))
+    heights = np.kron(heights, np.ones((4, 4)))
+    bump = b.texture(Texture(np.repeat(heights[..., None], 3, 2).astype(np.float32), TEX_BUMP,
+                             repeat_u=1.0, repeat_v=1.0, bump_intensity=3.0))
+    back = diffuse(rng.uniform(0.4, 0.8, 3))
+    back[13] = bump
+    b.add("back", quad_tris(*[np.asarray(p, np.float32) for p in ((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1))]),
+          None, b.material(back), uv=uv_quad)
+    # Phong sphere with a ks map, dielectric sphere with a transparency map (uvs: Sphere::_getUV)
+    noise = rng.uniform(0.1, 0.5, (8, 8, 3)).astype(np.float32)
+    ks_tex = b.texture(Texture(noise, TEX_COLOR, filters))
+    ph = phong((0.3, 0.3, 0.3), (0.4, 0.4, 0.4), 30.0)
+    ph[11] = ks_tex
+    tr_tex = b.texture(Texture(rng.uniform(0.2, 1.0, (6, 10, 3)).astype(np.float32), TEX_COLOR, filters,
+                               repeat_u=2.0))
+    di = dielectric(1.5)
+    di[12] = tr_tex
+    for name, center, r, rec in (("phongSphere", (-0.45, 0.35, -0.2), 0.35, ph),
+                                 ("glassSphere", (0.45, 0.3, 0.3), 0.3, di)):
+        tris, nrm = _uv_sphere_fast(center, r, 24, 13)
+        d = (tris.reshape(-1, 3) - np.asarray(center, np.float32)) / r
+        u = 1.0 - np.arctan2(d[:, 2], d[:, 0]) / (2 * np.pi)
+        v = 0.5 - np.arcsin(np.clip(d[:, 1], -1, 1)) / np.pi
+        uv = np.stack([u, v], -1).reshape(-1, 3, 2)
+        # keep each triangle on one side of the seam (a lookup only uses the fractional part)
+        span = uv[:, :, 0].max(1) - uv[:, :, 0].min(1)
+        fix = (span > 0.5)[:, None] & (uv[:, :, 0] < 1.0)
+        uv[:, :, 0] += fix
+        b.add(name, tris, nrm, b.material(rec), uv=uv.astype(np.float32))
+    lm = b.material(diffuse(0.0))
+    b.add_quad_light("light", (0.0, 1.999, 0.0), (0.5, 0.0, 0.0), (0.0, 0.0, -0.5), 15.0, lm)
+    cam = camera(eye=(0.0, 1.0, 3.75), look=(0.0, 0.0, -1.0), up=(0, 1, 0), height_angle=40.0, aspect=1.0)
+    return b.build(cam, name="textured")
 
 
 def _place_spheres(rng, n, rmin, rmax, half_extent, max_tries=200000):

@@ -33,8 +33,13 @@ Emitters: a unit plane becomes a parallelogram light, a Triangle a triangle ligh
 frame and object-space area, a mesh one mesh light over its triangles (include/mgpu.h,
 ``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
 element: analytic shapes other than planes and cubes (sphere, cylinder, cone, blob, point),
-emitting cubes, omni and environment emitters, textures and bump maps, per-channel IOR or
-Phong exponents.  Spheres are taken when the caller passes tessellate=(nu, nv): each becomes an
+emitting cubes, omni and environment emitters, bump-mapped emitters, per-channel IOR or Phong
+exponents.  Image maps are taken: a material's kd / ks / transparency given as a file name and
+its bumpMap become textures (PNG, PPM / PGM) with the material's filter, repeatU / repeatV and
+bumpIntensity, and every triangle carries the uvs of Shape::_getUV for the shape it came from
+(Plane, Triangle, Cube -- from the world position, as the reference does -- and Mesh: the first
+vertex's texture coordinate for the whole triangle).  An image that fails to load leaves the
+key at 0.7 or the normal unbumped, as the reference's Material does.  Spheres are taken when the caller passes tessellate=(nu, nv): each becomes an
 nu x nv UV sphere with radial normals under Milton's T(position) S(2 radius) (:596-611), an
 approximation of the analytic surface.  Instances of named shapes are copied (their geometry
 under the instance's transform chain, with the material active at the instance).  A thin-lens
@@ -46,11 +51,13 @@ from __future__ import annotations
 
 import math
 import os
+import warnings
 from dataclasses import dataclass, field
 
 import numpy as np
 
 from . import scene as S
+from .imageio import read_image
 
 
 class SceneFileError(ValueError):
@@ -393,6 +400,7 @@ class _Node:
 @dataclass
 class _Material:
     props: dict = field(default_factory=dict)
+    filter: tuple | None = None  # the material's "filter" object (texture lookups); None = triangle, 2
 
 
 @dataclass
@@ -588,7 +596,7 @@ class _Loader:
             raise SceneFileError(f"material must be of type 'object', found '{_tname(v)}'")
         fns = self.node_fns()
         fns.update(bsdf=lambda b: self.bsdf(mat, b), emitter=lambda e: self.emitter(mat, e),
-                   medium=lambda m: self.medium(mat, m), filter=None)
+                   medium=lambda m: self.medium(mat, m), filter=lambda f: setattr(mat, "filter", parse_filter(f)))
         _properties({"bumpMap": "string", "bumpIntensity": "real_t", "repeatU": "real_t", "repeatV": "real_t"},
                     v, mat.props)
         self.begin(_Node("material", mat))
@@ -763,19 +771,19 @@ class _Loader:
                 local = local @ _trans(pos)
             if "radius" in props:
                 local = local @ _scale([2.0 * props["radius"]] * 3)
-            tris, nrm = _unit_sphere(*self.tessellate)
+            tris, nrm, uv = _unit_sphere(*self.tessellate)
             node = _Node("shape", _Shape("mesh", {"v": tris.reshape(-1, 3).astype(np.float64),
                                                   "f": np.arange(tris.shape[0] * 3).reshape(-1, 3),
                                                   "n": nrm.reshape(-1, 3).astype(np.float64),
                                                   "nf": np.arange(tris.shape[0] * 3).reshape(-1, 3),
-                                                  "path": "sphere"}, local))
+                                                  "uv": uv, "path": "sphere"}, local))
         else:  # mesh
             if "path" not in props:
                 raise SceneFileError("missing required key 'path' in 'mesh' (path to mesh data file)")
             path = props["path"]
             if not os.path.isabs(path) and not os.path.exists(path):
                 path = os.path.join(self.base_dir, path)  # the reference opens it from the cwd
-            verts, faces, normals, nfaces = load_mesh(path)
+            verts, faces, normals, nfaces, face_uv = load_mesh(path, with_uv=True)
             if props.get("normalize"):
                 lo, hi = verts.min(0), verts.max(0)
                 center = (lo + hi) * 0.5
@@ -783,6 +791,7 @@ class _Loader:
                 diag = diag + (diag == 0)
                 verts = (verts - center) / diag
             node = _Node("shape", _Shape("mesh", {"v": verts, "f": faces, "n": normals, "nf": nfaces,
+                                                  "uv": np.repeat(face_uv[:, None, :], 3, axis=1),
                                                   "path": props["path"]}))
         self.name_node(props, node)
         self.begin(node)
@@ -834,21 +843,34 @@ def parse_filter(v) -> tuple:
     return (t, float(props.get("support", 2)), params)
 
 
-def load_mesh(path: str):
+def load_mesh(path: str, with_uv: bool = False):
     """(vertices (V, 3) float64, triangles (T, 3) int, normals (N, 3) or None, normal indices
-    (T, 3) or None)."""
+    (T, 3) or None), and with_uv: each triangle's uv (T, 2) -- Mesh::_getUV takes the uv of the
+    triangle's first texture index for the whole triangle (Mesh.cpp:408-416), index 0 for faces
+    without texture indices (MeshLoaderOBJ.cpp:117-162), (0, 0) for meshes without uvs."""
     suffix = path[path.rfind(".") + 1:]
     if suffix in ("obj", "OBJ"):
-        return _load_obj(path)
-    if suffix in ("ply", "PLY"):
-        return _load_ply(path)
-    raise SceneFileError(f"mesh '{path}' failed to load (unable to infer mesh type '{suffix}')")
+        r = _load_obj(path)
+    elif suffix in ("ply", "PLY"):
+        r = _load_ply(path) + (np.zeros((0, 2)), None)
+    else:
+        raise SceneFileError(f"mesh '{path}' failed to load (unable to infer mesh type '{suffix}')")
+    if not with_uv:
+        return r[:4]
+    verts, faces, normals, nfaces, uvs, t_first = r
+    if len(uvs) == 0:
+        face_uv = np.zeros((len(faces), 2))
+    else:
+        if t_first.min() < 0 or t_first.max() >= len(uvs):
+            raise SceneFileError(f"mesh '{path}': texture index out of range")
+        face_uv = uvs[t_first]
+    return verts, faces, normals, nfaces, face_uv
 
 
 def _load_obj(path):
     if not os.path.exists(path):
         raise SceneFileError(f"mesh '{path}' failed to load")
-    v, vn, tris, ntris = [], [], [], []
+    v, vn, vt, tris, ntris, tfirst = [], [], [], [], [], []
     with open(path, "r", encoding="latin-1") as f:
         for ln, line in enumerate(f, 1):
             parts = line.split()
@@ -859,6 +881,8 @@ def _load_obj(path):
                 v.append([float(x) for x in parts[1:4]])
             elif tag == "vn":
                 vn.append([float(x) for x in parts[1:4]])
+            elif tag == "vt":
+                vt.append([float(x) for x in parts[1:3]])
             elif tag == "f":
                 idx = []
                 for p in parts[1:]:
@@ -868,16 +892,20 @@ def _load_obj(path):
                                              "supported by the reference's OBJ loader")
                     vi = int(fs[0])
                     ni = int(fs[2]) if len(fs) == 3 else None
+                    ti = int(fs[1]) if len(fs) == 3 and fs[1] != "" else None
                     vi = vi - 1 if vi > 0 else len(v) + vi
                     if ni is not None:
                         ni = ni - 1 if ni > 0 else len(vn) + ni
-                    idx.append((vi, ni))
+                    if ti is not None:
+                        ti = ti - 1 if ti > 0 else len(vt) + ti
+                    idx.append((vi, ni, ti))
                 if len(idx) < 3:
                     raise SceneFileError(f"{path}:{ln}: face with fewer than 3 vertices")
                 for k in range(1, len(idx) - 1):
                     a, b, c = idx[0], idx[k], idx[k + 1]
                     tris.append((a[0], b[0], c[0]))
                     ntris.append((a[1], b[1], c[1]))
+                    tfirst.append(a[2] if a[2] is not None else 0)
     verts = np.array(v, np.float64).reshape(-1, 3)
     faces = np.array(tris, np.int64).reshape(-1, 3)
     if len(faces) == 0 or len(verts) == 0:
@@ -888,8 +916,8 @@ def _load_obj(path):
         nf = np.array(ntris, np.int64)
         if nf.min() < 0 or nf.max() >= len(vn):
             raise SceneFileError(f"mesh '{path}': normal index out of range")
-        return verts, faces, np.array(vn, np.float64), nf
-    return verts, faces, None, None
+        return verts, faces, np.array(vn, np.float64), nf, np.array(vt, np.float64).reshape(-1, 2), np.array(tfirst)
+    return verts, faces, None, None, np.array(vt, np.float64).reshape(-1, 2), np.array(tfirst)
 
 
 _PLY_TYPES = {"char": "i1", "int8": "i1", "uchar": "u1", "uint8": "u1", "short": "i2", "int16": "i2",
@@ -1016,6 +1044,27 @@ _CUBE_FACES = [  # (normal axis, sign): two triangles per face of [-.5, .5]^3
 ]
 
 
+def _cube_uv(q_world, n_obj):
+    """Cube::_getUV (Cube.cpp:84-105) at the corners of one face: it reads the hit position in
+    world space (not object space) and the face's normalCase (axis, 4 + axis on the negative
+    side, Cube.cpp:27-48); affine in the position, so corner values interpolate exactly."""
+    axis = int(np.flatnonzero(np.asarray(n_obj))[0])
+    case = axis if n_obj[axis] > 0 else 4 + axis
+    side = case & 3
+    out = np.zeros((len(q_world), 2))
+    for k, P in enumerate(q_world):
+        v = P[side + 1 - 3 * (side == 2)] + 0.5
+        u = P[side + 2 - 3 * (side >= 1)] + 0.5
+        if side == 2:
+            u, v = 1 - v, u
+        if case & 4:
+            v = 1 - v
+        if not (case & 5):
+            u, v = 1 - u, 1 - v
+        out[k] = (u, v)
+    return out
+
+
 def _xf_points(m, p):
     p = np.asarray(p, np.float64).reshape(-1, 3)
     return p @ m[:3, :3].T + m[:3, 3]
@@ -1030,11 +1079,14 @@ def _xf_normals(m, n):
 
 
 class _Flattener:
-    def __init__(self, named=None):
+    def __init__(self, named=None, base_dir: str = "."):
         self.named = named or {}
+        self.base_dir = base_dir
         self.depth = 0
         self.b = S.SceneBuilder()
         self.mat_index = {}   # id(_Material) -> material record index
+        self.tex_index = {}   # (file, kind, filter, repeat, intensity) -> texture slot
+        self.images = {}      # file -> (H, W, 3) float32 or None (ResourceManager's image cache)
         self.default = _Material()
         self.active = self.default
         self.in_root = True   # shapes go to the root ShapeSet (nested sets are never attached)
@@ -1042,8 +1094,58 @@ class _Flattener:
     def material_record(self, mat: _Material) -> int:
         key = id(mat)
         if key not in self.mat_index:
-            self.mat_index[key] = self.b.material(material_record(mat.props))
+            slots = self.texture_slots(mat)
+            rec = material_record(mat.props)
+            rec[10:14] = slots
+            self.mat_index[key] = self.b.material(rec)
         return self.mat_index[key]
+
+    def image(self, name: str):
+        """ResourceManager::getImage (ResourceManager.h:48-66): the image or None when it fails
+        to load (the reference logs the failure and renders on)."""
+        if name not in self.images:
+            path = name
+            if not os.path.isabs(path) and not os.path.exists(path):
+                path = os.path.join(self.base_dir, path)  # the reference opens it from the cwd
+            try:
+                self.images[name] = read_image(path)
+            except (OSError, ValueError) as e:
+                warnings.warn(f"failed to load image '{name}': {e}")
+                self.images[name] = None
+        return self.images[name]
+
+    def texture_slots(self, mat: _Material) -> list[float]:
+        """Texture slots [kd, ks, transparency, bump map] of a material record.  A textured key
+        whose image fails to load is the constant 0.7 (Material::getSpectralSampleSet,
+        Material.cpp:281), a bump map that fails leaves the normal alone (:189-193)."""
+        props = mat.props
+        flt = mat.filter or ("triangle", 2.0, {})
+        ru, rv = float(props.get("repeatU", 1.0)), float(props.get("repeatV", 1.0))
+        intensity = float(props.get("bumpIntensity", 5.0))
+        slots = [0.0, 0.0, 0.0, 0.0]
+        keys = {"diffuse": ("kd",), "modifiedPhong": ("kd", "ks"), "phong": ("kd", "ks"),
+                "dielectric": ("ks", "transparency")}.get(props.get("bsdf", "diffuse"), ())
+        for k, key in enumerate(("kd", "ks", "transparency")):
+            name = props.get(key)
+            if key in keys and isinstance(name, str):
+                img = self.image(name)
+                if img is None:
+                    props[key] = 0.7
+                    continue
+                slots[k] = self.texture(name, img, S.TEX_COLOR, flt, ru, rv, intensity)
+        bump = props.get("bumpMap")
+        if isinstance(bump, str) and bump:
+            img = self.image(bump)
+            if img is not None:
+                slots[3] = self.texture(bump, img, S.TEX_BUMP, flt, ru, rv, intensity)
+        return slots
+
+    def texture(self, name, img, kind, flt, ru, rv, intensity) -> int:
+        key = (name, kind, repr(flt) if kind == S.TEX_COLOR else "", ru, rv, intensity)
+        if key not in self.tex_index:
+            self.tex_index[key] = self.b.texture(S.Texture(img, kind=kind, filter=flt, repeat_u=ru, repeat_v=rv,
+                                                           bump_intensity=intensity))
+        return self.tex_index[key]
 
     def run(self, root: _Node):
         self.material_record(self.default)
@@ -1088,9 +1190,10 @@ class _Flattener:
         if emitter not in ("null", "oriented"):
             raise SceneFileError(f"'{emitter}' emitters are not supported by the GPU path (oriented area lights "
                                  "on planes are)")
-        if props.get("bumpMap"):
-            raise SceneFileError("bump maps are not supported by the GPU path")
         mi = self.material_record(self.active)
+        if emitter != "null" and self.b.materials[mi][13] != 0:
+            raise SceneFileError("a bump-mapped emitter is not supported by the GPU path (its light samples "
+                                 "would need the bumped normal)")
         m = trans @ sh.local
         name = sh.kind
         if sh.kind == "plane":
@@ -1108,7 +1211,10 @@ class _Flattener:
             else:
                 li = -1
             tris = np.array([corners[[0, 3, 2]], corners[[0, 2, 1]]], np.float64)
-            self.b.add(name, tris, np.broadcast_to(nrm, (2, 3, 3)), mi, light=li)
+            # Plane::_getUV (Plane.cpp:52-59): (x + 1/2, z + 1/2) in object space
+            cuv = np.array([(0, 0), (1, 0), (1, 1), (0, 1)], np.float64)
+            self.b.add(name, tris, np.broadcast_to(nrm, (2, 3, 3)), mi, light=li,
+                       uv=np.array([cuv[[0, 3, 2]], cuv[[0, 2, 1]]]))
             return
         power = np.broadcast_to(np.asarray(props.get("power", (1.0, 1.0, 1.0)), np.float64), 3)
         if sh.kind == "triangle":
@@ -1134,19 +1240,23 @@ class _Flattener:
                 ext[0] = 1
                 ext[1:3], ext[3:5], ext[5:7], ext[7] = uv[0], a, b, 1.0 / cross
                 li = self.b.add_light(rec, ext)
-            self.b.add(name, vi[None], np.broadcast_to(nrm, (1, 3, 3)), mi, light=li, culled=True)
+            tuv = np.asarray(sh.data["uvs"], np.float64).reshape(3, 2)
+            tuv = tuv[[0, 2, 1]] if np.linalg.det(m[:3, :3]) < 0 else tuv
+            self.b.add(name, vi[None], np.broadcast_to(nrm, (1, 3, 3)), mi, light=li, culled=True, uv=tuv[None])
             return
         if emitter != "null" and sh.kind != "mesh":
             raise SceneFileError(f"an emitting {sh.kind} is not supported by the GPU path (emitters must be "
                                  "planes, triangles or meshes)")
         if sh.kind == "cube":
-            tris, nrms = [], []
+            tris, nrms, uvs = [], [], []
             for n_obj, q in _CUBE_FACES:
                 q = _xf_points(m, q)
                 nw = _xf_normals(m, [n_obj])[0]
+                fu = _cube_uv(q, n_obj)
                 tris += [q[[0, 1, 2]], q[[0, 2, 3]]]
                 nrms += [np.broadcast_to(nw, (3, 3))] * 2
-            self.b.add(name, np.array(tris), np.array(nrms), mi)
+                uvs += [fu[[0, 1, 2]], fu[[0, 2, 3]]]
+            self.b.add(name, np.array(tris), np.array(nrms), mi, uv=np.array(uvs))
         elif sh.kind == "mesh":
             verts, faces, normals, nfaces = sh.data["v"], sh.data["f"], sh.data["n"], sh.data["nf"]
             if normals is None:
@@ -1154,12 +1264,13 @@ class _Flattener:
             vw = _xf_points(m, verts)
             inv = np.linalg.inv(m)
             nw = normals @ inv[:3, :3]  # not normalised: interpolated, then normalised per hit
+            fuv = sh.data.get("uv")
             if emitter == "oriented":
                 tv = vw[faces]
                 area = 0.5 * float(np.linalg.norm(np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0]), axis=1).sum())
-                self.b.add_mesh_light(sh.data["path"], tv, nw[nfaces], power / (area * math.pi), mi)
+                self.b.add_mesh_light(sh.data["path"], tv, nw[nfaces], power / (area * math.pi), mi, uv=fuv)
             else:
-                self.b.add(sh.data["path"], vw[faces], nw[nfaces], mi)
+                self.b.add(sh.data["path"], vw[faces], nw[nfaces], mi, uv=fuv)
 
 
 def material_record(props: dict) -> np.ndarray:
@@ -1170,12 +1281,14 @@ def material_record(props: dict) -> np.ndarray:
     def spec(key, default):
         v = props.get(key, default)
         if isinstance(v, str):
-            raise SceneFileError(f"textured '{key}' ('{v}') is not supported by the GPU path")
+            return np.zeros(3)  # an image map (texture slot) replaces the constant
         return np.broadcast_to(np.asarray(v, np.float64), 3)
 
     def scalar(key, default):
         v = props.get(key, default)
         if isinstance(v, str):
+            if key == "transparency":
+                return 1.0  # an image map (texture slot) replaces the constant
             raise SceneFileError(f"'{key}' = '{v}' is not supported by the GPU path")
         a = np.broadcast_to(np.asarray(v, np.float64), 3)
         if not (a[0] == a[1] == a[2]):
@@ -1266,8 +1379,22 @@ class SceneFile:
 
 
 def _unit_sphere(nu: int, nv: int):
+    """The UV sphere of scenegen (radius 1/2) with Sphere::_getUV at its vertices
+    (Sphere.cpp:78-85: u = 1 - atan2(z, x) / 2 pi, v = 1/2 - asin(2 y) / pi), u taken continuous
+    in the longitude so that no triangle straddles the seam (the fractional part, which is all
+    a lookup uses, is the reference's)."""
     from .scenegen import _uv_sphere_fast
-    return _uv_sphere_fast((0.0, 0.0, 0.0), 0.5, nu, nv)
+    tris, nrm = _uv_sphere_fast((0.0, 0.0, 0.0), 0.5, nu, nv)
+    th = np.linspace(0.0, np.pi, nv + 1)
+    ph = np.linspace(0.0, 2 * np.pi, nu + 1)
+    T, PH = np.meshgrid(th, ph, indexing="ij")
+    uvg = np.stack([1.0 - PH / (2 * np.pi), T / np.pi], -1)
+    i, j = np.meshgrid(np.arange(nv), np.arange(nu), indexing="ij")
+    a, b, cc, d = (i, j), (i, j + 1), (i + 1, j + 1), (i + 1, j)
+    u1 = np.stack([uvg[a], uvg[d], uvg[b]], -2)
+    u2 = np.stack([uvg[b], uvg[d], uvg[cc]], -2)
+    keep = np.stack([i != 0, i != nv - 1], 2)
+    return tris, nrm, np.stack([u1, u2], 2)[keep].astype(np.float32)
 
 
 def loads(text: str, base_dir: str = ".", source: str = "<string>", tessellate=None) -> SceneFile:
@@ -1276,7 +1403,7 @@ def loads(text: str, base_dir: str = ".", source: str = "<string>", tessellate=N
     approximation of Milton's Sphere; without it they are refused)."""
     ld = _Loader(base_dir, tessellate)
     ld.root_obj(parse_text(text))
-    fl = _Flattener(ld.named)
+    fl = _Flattener(ld.named, base_dir)
     fl.run(ld.root)
     out = dict(ld.output_props)
     w, h, found = 480, 480, False
@@ -1298,6 +1425,8 @@ def loads(text: str, base_dir: str = ".", source: str = "<string>", tessellate=N
     cam_props = dict(ld.camera or {"type": "pinhole"})
     cam = camera_record(cam_props, w, h)
     scene = fl.b.build(cam, name=os.path.basename(source))
+    if not scene.textures:
+        scene.tri_uv = None  # uvs only matter to image maps
     return SceneFile(scene=scene, renderer=dict(ld.renderer or {"type": "preview"}), camera=cam_props, output=out,
                      width=w, height=h, source=source)
 

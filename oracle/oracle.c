@@ -34,6 +34,11 @@
  *                          M/common/math/sisd/Vector3.inl:18-21, M/common/math/Vector.h:113-117
  *   emitters               M/materials/Emitter.cpp:34-50, M/materials/emitters/OrientedEmitter.cpp:17-23
  *   film                   M/renderers/RenderOutput.cpp:72-101, M/filters/ProgressiveFilterValue.h:18-38
+ *   image maps             M/materials/Material.cpp:157-225 (uv, bump map), :229-301 (textured keys,
+ *                          getSample), M/filters/KernelFilter.cpp:18-40,106-156 (filter kernel and
+ *                          its application at one texel), M/filters/{Box,Triangle,Gaussian,Mitchell,
+ *                          LanczosSinc}Filter.cpp (evaluate), M/shapes/Triangle.cpp:23-39 (uv),
+ *                          M/common/image/Rgba.inl:32-45 (byte / 255, luminance)
  *   constants              M/common/arch.h:120-137 (EPSILON 1e-7, double), M/common/utilities.h:240 (EQ),
  *                          M/materials/IndexOfRefraction.cpp:16 (AIR = 1.0003)
  *
@@ -139,7 +144,18 @@ enum { MAT_DIFFUSE = 0, MAT_PHONG = 1, MAT_DIELECTRIC = 2 };
 typedef struct {
   int type;
   double kd[3], ks[3], n, ior, transparency;
+  int tex[4]; /* 1 + texture index for kd, ks, transparency, bump map; 0 = none */
 } orc_mat;
+
+/* A material's image map: rgb h x w x 3 linear values, row 0 on top.  Colour maps carry the
+ * kernel KernelFilter::_computeKernel builds for the material's filter. */
+typedef struct {
+  int w, h, kind; /* kind 0 colour, 1 bump */
+  const float *rgb;
+  int kw;         /* kernel width (ceil(support) | 1) */
+  double *wts;    /* kw * kw weights */
+  double ru, rv, intensity;
+} orc_tex;
 
 /* Area light: Milton Plane (type 0), Triangle (1) or Mesh (2) emitter.  Triangle: center = v1,
  * ex = v2 - v1, ez = v3 - v1, uv frame (uv0, a, b, 1/|a x b|).  Mesh: triangle run [first,
@@ -164,6 +180,9 @@ typedef struct {
   orc_mat *mats;
   int nlight;
   orc_light *lights;
+  const float *uv;     /* ntri * 6 per-vertex uvs, or NULL */
+  int ntex;
+  orc_tex *tex;
 } orc_scene;
 
 static inline v3 tri_vert(const orc_scene *s, int64_t t, int k) {
@@ -624,6 +643,65 @@ static int kd_any(const orc_scene *s, const orc_tree *tr, v3 o, v3 d, double cli
 /* scene construction from flat arrays                                         */
 /* material record (16 floats): type, kd[3], ks[3], n, ior, transparency, ...
  * light record (16 floats): center[3], ex[3], ez[3], normal[3], area, Le[3]   */
+/* Filter2D::evaluate of the kernel filters (M/filters/BoxFilter.cpp, TriangleFilter.cpp,
+ * GaussianFilter.cpp, MitchellFilter.cpp, LanczosSincFilter.cpp), in FP64.  kind: 1 box,
+ * 2 triangle, 3 gaussian (p1 sigma), 4 mitchell (p1 B, p2 C), 5 lanczosSinc (p1 tau).  The
+ * triangle filter is not mirrored for negative offsets and Mitchell's outer branch has no 1/6
+ * and no cut-off, as in the reference. */
+static double mitchell_1d(double x, double support, double B, double C) {
+  x = fabs(2.0 * x / support);
+  if (x > 1.0) return (((-B / 6.0 - C) * x + (B + 5.0 * C)) * x + (-2.0 * B - 8.0 * C)) * x + (4.0 / 3.0 * B + 4.0 * C);
+  return x * x * ((2.0 - 1.5 * B - C) * x + (-3.0 + 2.0 * B + C)) + (1.0 - B / 3.0);
+}
+
+static double lanczos_1d(double x, double support, double tau) {
+  x = fabs(x / support);
+  if (x < ORC_EPS) return 1.0;
+  if (x > 1.0) return 0.0;
+  x *= ORC_PI;
+  return sin(x * tau) / (x * tau) * sin(x) / x;
+}
+
+static double filter_eval(int kind, double support, double p1, double p2, double x, double y) {
+  switch (kind) {
+    case 1: return 2.0 * sqrt(x * x + y * y) < support ? 1.0 : 0.0;
+    case 2: {
+      double r = support / 2.0;
+      double a = 1.0 - x / r, b = 1.0 - y / r;
+      return (a > 0 ? a : 0) * (b > 0 ? b : 0);
+    }
+    case 3: {
+      double g = (1.0 / (sqrt(2.0 * ORC_PI) * p1)) * exp(-0.5 / (p1 * p1) * (x * x + y * y));
+      return g > 0 ? g : 0;
+    }
+    case 4: return mitchell_1d(x, support, p1, p2) * mitchell_1d(y, support, p1, p2);
+    case 5: return lanczos_1d(x, support, p1) * lanczos_1d(y, support, p1);
+    default: return 0.0;
+  }
+}
+
+/* tex_params: 12 floats per texture: width, height, kind, filter, support, p1, p2, repeat u,
+ * repeat v, bump intensity, 0, 0 */
+static orc_tex *textures_from(int ntex, const float *params, const float *const *rgb) {
+  orc_tex *t = (orc_tex *)calloc(ntex > 0 ? ntex : 1, sizeof(orc_tex));
+  for (int i = 0; i < ntex; ++i) {
+    const float *q = params + 12 * i;
+    t[i].w = (int)q[0]; t[i].h = (int)q[1]; t[i].kind = (int)q[2];
+    t[i].rgb = rgb[i];
+    t[i].ru = q[7]; t[i].rv = q[8]; t[i].intensity = q[9];
+    if (t[i].kind == 0) {
+      /* KernelFilter::_computeKernel: kernel[i w + j] = evaluate(i - w / 2, j - w / 2) */
+      int kw = ((int)ceil((double)q[4])) | 1;
+      double half = kw / 2.0;
+      t[i].kw = kw;
+      t[i].wts = (double *)calloc((size_t)kw * kw, sizeof(double));
+      for (int a = 0; a < kw; ++a)
+        for (int b = 0; b < kw; ++b) t[i].wts[a * kw + b] = filter_eval((int)q[3], q[4], q[5], q[6], a - half, b - half);
+    }
+  }
+  return t;
+}
+
 static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n, const int32_t *mat,
                                     const int32_t *light, const uint32_t *flags, int nmat, const float *mats,
                                     int nlight, const float *lights, const float *light_ext) {
@@ -638,6 +716,7 @@ static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n
     s->mats[i].n = m[7];
     s->mats[i].ior = m[8];
     s->mats[i].transparency = m[9];
+    for (int k = 0; k < 4; ++k) s->mats[i].tex[k] = (int)m[10 + k];
   }
   s->nlight = nlight;
   s->lights = (orc_light *)calloc(nlight > 0 ? nlight : 1, sizeof(orc_light));
@@ -668,6 +747,8 @@ static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n
 
 static void scene_free(orc_scene *s) {
   if (!s) return;
+  for (int i = 0; i < s->ntex; ++i) free(s->tex[i].wts);
+  free(s->tex);
   free(s->mats);
   free(s->lights);
   free(s);
@@ -994,6 +1075,88 @@ static v3 shading_normal(const orc_scene *s, int64_t tri, v3 p) {
   return vnorm(n);
 }
 
+/* uv at a hit (Triangle::_getUV, Triangle.cpp:23-39: area-ratio barycentrics of the hit point
+ * weighting the three vertex uvs; the other shapes' _getUV are affine over each of their
+ * triangles, which the per-vertex uvs encode) */
+static void hit_uv(const orc_scene *s, int64_t tri, v3 p, double *u, double *v) {
+  *u = *v = 0.0;
+  if (!s->uv) return;
+  v3 a = tri_vert(s, tri, 0), b = tri_vert(s, tri, 1), c = tri_vert(s, tri, 2);
+  double A = 1.0 / vlen(vcross(vsub(b, a), vsub(c, a)));
+  double pa = vlen(vcross(vsub(b, p), vsub(c, p))) * A;
+  double pb = vlen(vcross(vsub(p, a), vsub(c, a))) * A;
+  double pc = 1 - pa - pb;
+  const float *q = s->uv + tri * 6;
+  *u = pa * q[0] + pb * q[2] + pc * q[4];
+  *v = pa * q[1] + pb * q[3] + pc * q[5];
+}
+
+/* lookup texel of Material::getSample / _initShadingNormal (Material.cpp:196-201, 292-299) */
+static void tex_texel(const orc_tex *t, double u, double v, int *x, int *y) {
+  double s = u * t->ru, r = v * t->rv;
+  double fx = (s - floor(s)) * t->w, fy = (r - floor(r)) * t->h;
+  fx = fx >= t->w - 1 ? t->w - 1 : (fx <= 0 ? 0 : fx);
+  fy = fy >= t->h - 1 ? t->h - 1 : (fy <= 0 ? 0 : fy);
+  *x = (int)floor(fx);
+  *y = (int)floor(fy);
+}
+
+static inline int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
+
+/* KernelFilter::apply(image, x, y) (KernelFilter.cpp:106-140) at the lookup texel */
+static void tex_color(const orc_tex *t, double u, double v, double out[3]) {
+  int x, y;
+  tex_texel(t, u, v, &x, &y);
+  int half = t->kw >> 1;
+  const double *w = t->wts;
+  double sum = 0, rgb[3] = {0, 0, 0};
+  for (int i = -half; i <= half; ++i) {
+    int row = clampi(i + y, 0, t->h - 1);
+    for (int j = -half; j <= half; ++j) {
+      int col = clampi(j + x, 0, t->w - 1);
+      const float *px = t->rgb + ((size_t)row * t->w + col) * 3;
+      double wt = *w++;
+      sum += wt;
+      for (int k = 0; k < 3; ++k) rgb[k] += px[k] * wt;
+    }
+  }
+  for (int k = 0; k < 3; ++k) out[k] = rgb[k] / sum;
+}
+
+static double tex_lum(const orc_tex *t, int row, int col) {
+  const float *px = t->rgb + ((size_t)row * t->w + col) * 3;
+  return 0.2126 * px[0] + 0.7152 * px[1] + 0.0722 * px[2]; /* Rgba32::luminance, on byte / 255 */
+}
+
+/* Material::_initShadingNormal with a bump map (Material.cpp:179-225) */
+static v3 tex_bump(const orc_tex *t, double u, double v, v3 N) {
+  int x, y;
+  tex_texel(t, u, v, &x, &y);
+  double gx = tex_lum(t, y, x - (x > 0)) - tex_lum(t, y, x + (x < t->w - 1));
+  double gy = tex_lum(t, y - (y > 0), x) - tex_lum(t, y + (y < t->h - 1), x);
+  if (orc_eq(gx, 0.0) && orc_eq(gy, 0.0)) return N;
+  v3 U, V2;
+  onb(N, &U, &V2);
+  return vnorm(vadd(N, vmul(vadd(vmul(U, gx), vmul(V2, gy)), t->intensity)));
+}
+
+/* Material::initSurfacePoint's textured inputs at a hit: kd, ks and transparency from their
+ * maps (getSpectralSampleSet with a file name, Material.cpp:260-283; DielectricBSDF averages
+ * the transparency, DielectricBSDF.cpp:51-52), the shading normal from the bump map */
+static void apply_textures(const orc_scene *s, int64_t tri, v3 p, orc_mat *m, v3 *ns) {
+  double u, v;
+  hit_uv(s, tri, p, &u, &v);
+  for (int k = 0; k < 3; ++k) {
+    if (!m->tex[k]) continue;
+    double c[3];
+    tex_color(&s->tex[m->tex[k] - 1], u, v, c);
+    if (k == 0) for (int q = 0; q < 3; ++q) m->kd[q] = c[q];
+    else if (k == 1) for (int q = 0; q < 3; ++q) m->ks[q] = c[q];
+    else m->transparency = (c[0] + c[1] + c[2]) / 3.0;
+  }
+  if (m->tex[3]) *ns = tex_bump(&s->tex[m->tex[3] - 1], u, v, *ns);
+}
+
 /* Shape::getPoint for light sample m at (u, v) (Shape.cpp:52-64): Plane::getPosition
  * (Plane.cpp:91-93); Triangle::getPosition (Triangle.cpp:332-354), whose "barycentrics" are
  * magnitudes of 2-D cross products in the triangle's uv frame; Mesh::getPosition / getPoint
@@ -1079,6 +1242,12 @@ static void evaluate(const orc_render_ctx *c, orc_path *ph, v3 o, v3 d, int dept
   v3 p = vadd(o, vmul(d, t));
   v3 ns = shading_normal(s, tri, p);
   const orc_mat *m = &s->mats[s->mat[tri]];
+  orc_mat mt;
+  if (m->tex[0] || m->tex[1] || m->tex[2] || m->tex[3]) {
+    mt = *m;
+    apply_textures(s, tri, p, &mt, &ns);
+    m = &mt;
+  }
   orc_bsdf b = {m, ns, d, ph->ior_index + 1};
   if (is_specular(m)) ph->specular = 1;
   int li = s->light ? s->light[tri] : -1;
@@ -1197,9 +1366,13 @@ static void *render_thread(void *arg) {
  * with its own counter-based random numbers, so the result does not depend on nthreads.     */
 int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat, const int32_t *light,
                const uint32_t *flags, int nmat, const float *mats, int nlight, const float *lights,
-               const float *light_ext, const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed,
+               const float *light_ext, const float *tri_uv, int ntex, const float *tex_params,
+               const float *const *tex_rgb, const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed,
                uint32_t stream, double *film_sum, double *path_out, uint64_t *stats_out) {
   orc_scene *s = scene_from_arrays(ntri, v, n, mat, light, flags, nmat, mats, nlight, lights, light_ext);
+  s->uv = tri_uv;
+  s->ntex = ntex;
+  s->tex = textures_from(ntex, tex_params, tex_rgb);
   orc_render_ctx c;
   c.s = s;
   c.tr = tr;
@@ -1281,6 +1454,27 @@ void orc_bsdf_eval(const float *mat16, const double *ns, const double *wi, const
   m.n = mat16[7]; m.ior = mat16[8]; m.transparency = mat16[9];
   orc_bsdf b = {&m, V(ns[0], ns[1], ns[2]), V(wi[0], wi[1], wi[2]), 1};
   bsdf_eval(&b, V(wo[0], wo[1], wo[2]), f_out);
+}
+
+/* One texture lookup at (u, v): params = the 12 floats of orc_render's tex_params.  Colour
+ * maps write the filtered rgb to out[0..2]; bump maps write the luminance differences (gx, gy)
+ * to out[0..1] and the bumped normal of N = n_in to out[2..4] (n_in may be NULL). */
+void orc_texture_lookup(const float *params, const float *rgb, double u, double v, const double *n_in, double *out) {
+  orc_tex *t = textures_from(1, params, &rgb);
+  if (t->kind == 0) {
+    tex_color(t, u, v, out);
+  } else {
+    int x, y;
+    tex_texel(t, u, v, &x, &y);
+    out[0] = tex_lum(t, y, x - (x > 0)) - tex_lum(t, y, x + (x < t->w - 1));
+    out[1] = tex_lum(t, y - (y > 0), x) - tex_lum(t, y + (y < t->h - 1), x);
+    if (n_in) {
+      v3 nb = tex_bump(t, u, v, vnorm(V(n_in[0], n_in[1], n_in[2])));
+      out[2] = nb.x; out[3] = nb.y; out[4] = nb.z;
+    }
+  }
+  free(t->wts);
+  free(t);
 }
 
 void orc_uniforms(uint64_t seed, uint32_t stream, uint64_t path, uint32_t depth, uint32_t block, double *u4) {

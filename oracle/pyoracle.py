@@ -33,8 +33,9 @@ def load() -> C.CDLL:
     lib.orc_trace_closest.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, vp]
     lib.orc_trace_any.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp]
     lib.orc_render.restype = C.c_int
-    lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, u64, u32, vp, vp,
-                               vp]
+    lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp, vp,
+                               vp, u64, u32, vp, vp, vp]
+    lib.orc_texture_lookup.argtypes = [vp, vp, C.c_double, C.c_double, vp, vp]
     lib.orc_philox4x32_10.argtypes = [vp, vp, vp]
     lib.orc_camera_dir.argtypes = [vp, C.c_double, C.c_double, vp]
     lib.orc_camera_ray.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, vp, vp]
@@ -135,14 +136,44 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
     cam[:np.asarray(scene.camera).reshape(-1).shape[0]] = np.asarray(scene.camera, np.float32).reshape(-1)
     ext = getattr(scene, "light_ext", None)
     ext = np.ascontiguousarray(ext, np.float32) if ext is not None and len(ext) else None
+    uv = getattr(scene, "tri_uv", None)
+    uv = None if uv is None else np.ascontiguousarray(uv, np.float32)
+    textures = list(getattr(scene, "textures", []))
+    tparams, trgb = texture_params(textures)
     lib.orc_render(scene.ntri, _p(scene.tri_v), _p(scene.tri_n), _p(scene.tri_mat), _p(scene.tri_light),
                    _p(scene.tri_flags), len(scene.materials), _p(scene.materials), len(scene.lights), _p(lights),
-                   _p(ext), tree.h, _p(cam), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
+                   _p(ext), _p(uv), len(textures), _p(tparams), C.cast(trgb, C.c_void_p), tree.h, _p(cam), _p(ip), seed,
+                   stream, _p(film), _p(paths), _p(st))
     mean = film[r0:r1] / max(sample_count, 1)
     if per_path:
         paths = paths.reshape(height, width, sample_count, 3)[r0:r1]
     stats = dict(extension_rays=int(st[0]), shadow_rays=int(st[1]), zero_pdf=int(st[2]), truncated=int(st[3]))
     return mean, paths, stats
+
+
+def texture_params(textures):
+    """(12 floats per texture, array of rgb pointers) for orc_render: width, height, kind,
+    filter, support, p1, p2, repeat u, repeat v, bump intensity."""
+    params = np.zeros((max(1, len(textures)), 12), np.float32)
+    ptrs = (C.c_void_p * max(1, len(textures)))()
+    for i, t in enumerate(textures):
+        h, w, _ = t.rgb.shape
+        f, support, p1, p2 = t.filter_params()
+        params[i, :10] = (w, h, t.kind, f, support, p1, p2, t.repeat_u, t.repeat_v, t.bump_intensity)
+        ptrs[i] = t.rgb.ctypes.data
+    return params, ptrs
+
+
+def texture_lookup(tex, u, v, normal=None) -> np.ndarray:
+    """One oracle lookup of a Texture at (u, v): filtered rgb (colour maps) or (gx, gy, bumped
+    normal xyz) (bump maps)."""
+    lib = load()
+    params, _ = texture_params([tex])
+    rgb = np.ascontiguousarray(tex.rgb, np.float32)
+    out = np.zeros(5, np.float64)
+    n = None if normal is None else np.ascontiguousarray(normal, np.float64)
+    lib.orc_texture_lookup(_p(params), rgb.ctypes.data, float(u), float(v), _p(n), _p(out))
+    return out[:3] if tex.kind == 0 else out
 
 
 def philox(ctr, key) -> np.ndarray:
