@@ -711,6 +711,7 @@ struct Tuning {
   // waves of fewer paths skip binning: sorting a few hundred thousand rays costs more (four
   // latency-bound launches per bounce) than the coherence it buys
   std::atomic<int64_t> bin_min_paths{(int64_t)1 << 22};
+  std::atomic<int> carveout{-1};      // shared-memory carveout (%) of the traversal / shade kernels; -1 = driver's
 };
 static Tuning g_tune;
 
@@ -1405,7 +1406,17 @@ int mgpu_tune_set(const char *key, int64_t value) {
   else if (k == "bin_shadow") g_tune.bin_shadow.store(value != 0);
   else if (k == "bin_extension") g_tune.bin_extension.store(value != 0);
   else if (k == "bin_min_paths" && value >= 0) g_tune.bin_min_paths.store(value);
-  else return fail(MGPU_E_INVALID, "mgpu_tune_set: unknown key or bad value " + k);
+  else if (k == "carveout" && value >= -1 && value <= 100) {
+    // the L1 / shared-memory split of the kernels that spill and chase pointers through L1
+    const void *kerns[] = {(const void *)k_extend<false, false>, (const void *)k_extend<false, true>,
+                           (const void *)k_extend<true, false>,  (const void *)k_extend<true, true>,
+                           (const void *)k_shadow<false, false>, (const void *)k_shadow<false, true>,
+                           (const void *)k_shadow<true, false>,  (const void *)k_shadow<true, true>,
+                           (const void *)k_shade};
+    for (const void *kf : kerns)
+      MGPU_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)value));
+    g_tune.carveout.store((int)value);
+  } else return fail(MGPU_E_INVALID, "mgpu_tune_set: unknown key or bad value " + k);
   return MGPU_OK;
 }
 
@@ -1416,6 +1427,7 @@ int mgpu_tune_get(const char *key, int64_t *value) {
   else if (k == "bin_shadow") *value = g_tune.bin_shadow.load();
   else if (k == "bin_extension") *value = g_tune.bin_extension.load();
   else if (k == "bin_min_paths") *value = g_tune.bin_min_paths.load();
+  else if (k == "carveout") *value = g_tune.carveout.load();
   else return fail(MGPU_E_INVALID, "mgpu_tune_get: unknown key " + k);
   return MGPU_OK;
 }
