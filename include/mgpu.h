@@ -97,7 +97,13 @@ typedef struct {
  *              their barycentric interpolation (Shape::_getUV of the shape the triangle came from:
  *              Triangle.cpp:23-39, Plane.cpp:52-59, Cube.cpp:84-105 and Mesh.cpp:408-416 are
  *              all affine over a triangle, so per-vertex uvs reproduce them)
- *   textures   ntex records (mgpu_texture), referenced by the material texture slots          */
+ *   textures   ntex records (mgpu_texture), referenced by the material texture slots
+ *   background radiance of rays that leave the scene (Scene::getBackgroundRadiance, Scene.cpp:
+ *              116-118, added at every depth; not sampled by next-event estimation):
+ *              background_tex = 1 + index of a colour map read as Milton's latitude-longitude
+ *              EnvironmentMap (EnvironmentMap.cpp:40-96: the map's texel at the uv of -d), or 0
+ *              for the constant background_le (an omni background: power / 4 pi; zeros = the
+ *              default black background)                                                   */
 typedef struct mgpu_texture mgpu_texture;
 typedef struct {
   int64_t ntri;
@@ -114,6 +120,8 @@ typedef struct {
   const float *tri_uv;
   int32_t ntex;
   const mgpu_texture *textures;
+  int32_t background_tex;
+  float background_le[3];
 } mgpu_scene_desc;
 
 /* A material's image map (Material::getSample, Material.cpp:285-301, and the bump map of

@@ -435,6 +435,8 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     }
   }
   if (tp.uv) s->d_uv = (float2 *)(base + L.off_uv);
+  s->bg_tex = desc->background_tex;
+  for (int k = 0; k < 3; ++k) s->bg_le[k] = desc->background_le[k];
   s->view.pairs = (const Pair *)(base + off_pairs);
   s->view.ltris = (const F4 *)(base + off_refs);
   s->view.tris = (const F4 *)(base + off_tris);

@@ -69,6 +69,8 @@ struct mgpu_scene {
   float2 *d_uv = nullptr;       // 3 per triangle by id (nullptr: every uv is (0, 0))
   float4 *d_texrec = nullptr;   // 2 per texture: (texel offset, width, height, kind), (repeat u, v, bump intensity, 0)
   float4 *d_texels = nullptr;   // filtered colour texels / bump gradients
+  int32_t bg_tex = 0;           // background: 1 + colour map index (environment), or 0
+  float bg_le[3] = {0, 0, 0};   // constant background radiance when bg_tex == 0
   std::vector<uint64_t> tex_offset;
   std::vector<int32_t> tex_w, tex_h;
   int32_t nmat = 0, nlight = 0;

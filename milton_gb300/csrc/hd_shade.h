@@ -49,6 +49,17 @@ MGPU_HD int tex_texel(float u, float v, int w, int h, float ru, float rv) {
   return (int)y * w + (int)x;
 }
 
+// uv of Milton's latitude-longitude EnvironmentMap in direction w (EnvironmentMap.cpp:62-86):
+// theta = asin(y / |w|) (acos(rho / |w|) with y's sign where rho = |(x, z)| < |y|), phi =
+// atan2(x, z) (0 on the y axis), u = phi / (-2 pi) + 1/2, v = theta / -pi + 1/2.
+MGPU_HD void env_uv(V3 w, float &u, float &v) {
+  const float rho = sqrtf(w.x * w.x + w.z * w.z), mag = length(w);
+  const float theta = rho < fabsf(w.y) ? acosf(rho / mag) * (w.y >= 0.0f ? 1.0f : -1.0f) : asinf(w.y / mag);
+  const float phi = (w.x == 0.0f && w.z == 0.0f) ? 0.0f : atan2f(w.x, w.z);
+  u = phi / (-2.0f * kPi) + 0.5f;
+  v = theta / -kPi + 0.5f;
+}
+
 // Textured keys replace the constants (Material::getSpectralSampleSet with a file name,
 // Material.cpp:260-283); DielectricBSDF uses the average transparency (DielectricBSDF.cpp:51-52).
 MGPU_HD void tex_apply(Material &m, int slot, float r, float g, float b) {

@@ -18,6 +18,8 @@ struct mgpu_renderer {
   std::vector<uint32_t> flags;
   std::vector<std::vector<float>> tex_rgb;  // owned texel data of each texture
   std::vector<mgpu_texture> tex;
+  int32_t bg_tex = 0;
+  float bg_le[3] = {0, 0, 0};
   bool has_scene = false, has_n = false, has_light = false, has_flags = false;
   int32_t nmat = 0, nlight = 0;
   float camera[16] = {0, 0, 0, 0, 0, -1, 0, 1, 0, 45, 1, 0, 0, 1, 0, 0};
@@ -62,6 +64,8 @@ struct mgpu_renderer {
     d.tri_uv = uv.empty() ? nullptr : uv.data();
     d.ntex = (int32_t)tex.size();
     d.textures = tex.empty() ? nullptr : tex.data();
+    d.background_tex = bg_tex;
+    for (int k = 0; k < 3; ++k) d.background_le[k] = bg_le[k];
     return d;
   }
 };
@@ -129,6 +133,8 @@ int mgpu_renderer_set_scene(mgpu_renderer *r, const mgpu_scene_desc *d) {
     r->tex.push_back(t);
   }
   for (int32_t i = 0; i < d->ntex; ++i) r->tex[i].rgb = r->tex_rgb[i].data();
+  r->bg_tex = d->background_tex;
+  for (int k = 0; k < 3; ++k) r->bg_le[k] = d->background_le[k];
   r->has_scene = true;
   r->initted = false;
   return MGPU_OK;

@@ -64,6 +64,8 @@ struct JobArgs {
   const float2 *uv;      // 3 per triangle (nullptr: every uv is (0, 0))
   const float4 *texrec;  // 2 per texture
   const float4 *texels;
+  int32_t bg_tex;          // background environment map (1 + texture index) or 0
+  float bg_le[3];          // constant background radiance (bg_tex == 0)
   int32_t nlight, nl_slots, sh_cell_bits;
   Camera cam;
   Rng rng;
@@ -180,6 +182,18 @@ __device__ __noinline__ void apply_textures(const JobArgs &J, int prim, float b0
     if (k < 3) tex_apply(m, k, t.x, t.y, t.z);
     else ns = bump_normal(ns, t.x, t.y, r1.z);
   }
+}
+
+// Background radiance of a ray leaving the scene in direction d: EnvironmentMap::getLe(-d)
+// (the map's filtered texel at the uv of -d) or the constant of an omni background.
+__device__ __noinline__ V3 background(const JobArgs &J, V3 d) {
+  if (J.bg_tex == 0) return v3(J.bg_le[0], J.bg_le[1], J.bg_le[2]);
+  float u, v;
+  env_uv(-d, u, v);
+  const float4 r0 = __ldg(J.texrec + 2 * (J.bg_tex - 1)), r1 = __ldg(J.texrec + 2 * (J.bg_tex - 1) + 1);
+  const int w = __float_as_int(r0.y), h = __float_as_int(r0.z);
+  const float4 t = __ldg(J.texels + __float_as_uint(r0.x) + tex_texel(u, v, w, h, r1.x, r1.y));
+  return v3(t.x, t.y, t.z);
 }
 
 // light records: 8 float4 each (base record, then the extension)
@@ -397,6 +411,8 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
             }
           }
         }
+      } else if (J.bg_tex != 0 || J.bg_le[0] != 0.0f || J.bg_le[1] != 0.0f || J.bg_le[2] != 0.0f) {
+        L = L + mul(thr, background(J, d));  // PathTracer.cpp:39-42: a miss adds the background
       }
       a.path_L[p] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
     }
@@ -943,6 +959,8 @@ static JobArgs job_args(const Job &j) {
   J.uv = sc->d_uv;
   J.texrec = sc->d_texrec;
   J.texels = sc->d_texels;
+  J.bg_tex = sc->bg_tex;
+  for (int k = 0; k < 3; ++k) J.bg_le[k] = sc->bg_le[k];
   J.nlight = sc->nlight;
   J.cam = make_camera(rp->camera);
   J.rng.k0 = (uint32_t)rp->seed;

@@ -37,6 +37,8 @@ struct SrvScene {
   std::vector<uint32_t> flags;
   std::vector<std::vector<float>> tex_rgb;  // owned texel data of each texture
   std::vector<mgpu_texture> tex;
+  int32_t bg_tex = 0;
+  float bg_le[3] = {0, 0, 0};
   int32_t nmat = 0, nlight = 0;
   // written by a build thread, read under the server mutex
   int state = kIdle;
@@ -65,6 +67,8 @@ struct SrvScene {
     d.tri_uv = uv.empty() ? nullptr : uv.data();
     d.ntex = (int32_t)tex.size();
     d.textures = tex.empty() ? nullptr : tex.data();
+    d.background_tex = bg_tex;
+    for (int k = 0; k < 3; ++k) d.background_le[k] = bg_le[k];
     return d;
   }
 };
@@ -403,6 +407,8 @@ int mgpu_server_add_scene(mgpu_server *s, const mgpu_scene_desc *d, int32_t *sce
       sc->tex.push_back(t);
     }
     for (int32_t i = 0; i < d->ntex; ++i) sc->tex[i].rgb = sc->tex_rgb[i].data();
+    sc->bg_tex = d->background_tex;
+    for (int k = 0; k < 3; ++k) sc->bg_le[k] = d->background_le[k];
   } catch (...) {
     return fail(MGPU_E_NOMEM, "mgpu_server_add_scene: out of host memory");
   }

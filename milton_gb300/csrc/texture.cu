@@ -82,6 +82,13 @@ int tex_plan(const mgpu_scene_desc *d, TexPlan &p) {
     }
     bumped[m] = r[13] != 0.0f;
   }
+  if (d->background_tex < 0 || d->background_tex > d->ntex)
+    return fail(MGPU_E_INVALID, "mgpu_scene_create: background texture out of range");
+  if (d->background_tex > 0 && d->textures[d->background_tex - 1].kind != MGPU_TEX_COLOR)
+    return fail(MGPU_E_INVALID, "mgpu_scene_create: the background must be a colour map");
+  for (int k = 0; k < 3; ++k)
+    if (!std::isfinite(d->background_le[k]) || d->background_le[k] < 0.0f)
+      return fail(MGPU_E_INVALID, "mgpu_scene_create: bad background radiance");
   if (d->tri_light)
     for (int64_t t = 0; t < d->ntri; ++t)
       if (d->tri_light[t] >= 0 && bumped[d->tri_mat[t]])

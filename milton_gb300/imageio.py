@@ -144,15 +144,80 @@ def read_pnm(path: str) -> np.ndarray:
     return np.repeat(px, 3, axis=2) if ch == 1 else px.copy()
 
 
+def read_hdr(path: str) -> np.ndarray:
+    """Reads a Radiance RGBE (.hdr) image, flat or run-length encoded scanlines, '-Y h +X w'
+    orientation: (H, W, 3) float32, row 0 on top.  A pixel is mantissa * 2^(e - 136), 0 for e = 0
+    (HDRUtils::loadHDR with rgbe2float, HDRUtils.cpp:36-70, rgbe.cpp:116-131)."""
+    data = open(path, "rb").read()
+    pos, fmt_ok, first = 0, False, True
+    while True:
+        nl = data.find(b"\n", pos)
+        if nl < 0:
+            raise ValueError("truncated HDR header")
+        line = data[pos:nl].strip()
+        pos = nl + 1
+        if first and not line.startswith(b"#?"):
+            raise ValueError("not a Radiance HDR file")
+        first = False
+        if line.startswith(b"FORMAT="):
+            fmt_ok = line == b"FORMAT=32-bit_rle_rgbe"
+            if not fmt_ok:
+                raise ValueError("only 32-bit_rle_rgbe HDR files are read")
+        if line.startswith(b"-Y "):
+            p = line.split()
+            if len(p) != 4 or p[2] != b"+X":
+                raise ValueError("only '-Y h +X w' HDR orientation is read")
+            h, w = int(p[1]), int(p[3])
+            break
+    if w <= 0 or h <= 0:
+        raise ValueError("bad HDR size")
+    buf = np.frombuffer(data, np.uint8)
+    rgbe = np.zeros((h, w, 4), np.uint8)
+    for y in range(h):
+        if w < 8 or w > 0x7FFF or pos + 4 > len(buf) or buf[pos] != 2 or buf[pos + 1] != 2 or (buf[pos + 2] & 0x80):
+            rest = buf[pos:pos + 4 * w * (h - y)]  # flat (uncompressed) pixels from here on
+            if rest.size != 4 * w * (h - y):
+                raise ValueError("truncated HDR data")
+            rgbe[y:] = rest.reshape(h - y, w, 4)
+            break
+        if (int(buf[pos + 2]) << 8 | int(buf[pos + 3])) != w:
+            raise ValueError("wrong HDR scanline width")
+        pos += 4
+        for c in range(4):
+            x = 0
+            while x < w:
+                if pos >= len(buf):
+                    raise ValueError("truncated HDR data")
+                n = int(buf[pos])
+                if n > 128:  # a run
+                    n -= 128
+                    if n == 0 or x + n > w or pos + 1 >= len(buf):
+                        raise ValueError("bad HDR run")
+                    rgbe[y, x:x + n, c] = buf[pos + 1]
+                    pos += 2
+                else:  # n literal bytes
+                    if n == 0 or x + n > w or pos + 1 + n > len(buf):
+                        raise ValueError("bad HDR run")
+                    rgbe[y, x:x + n, c] = buf[pos + 1:pos + 1 + n]
+                    pos += 1 + n
+                x += n
+    e = rgbe[..., 3].astype(np.int32)
+    f = np.where(e > 0, np.ldexp(np.float32(1.0), e - 136), 0.0).astype(np.float32)
+    return rgbe[..., :3].astype(np.float32) * f[..., None]
+
+
 def read_image(path: str) -> np.ndarray:
     """An image file as Milton's Image::load gives it to materials (Image.cpp:67-100, through
     Qt's Format_RGB32 and Rgba32 -> RgbaHDR, Rgba.inl:32-40): (H, W, 3) float32 byte / 255, row 0
-    on top.  PNG and PPM / PGM are read; other formats raise ValueError."""
+    on top.  PNG, PPM / PGM and Radiance HDR (float values as stored) are read; other formats
+    raise ValueError (the reference reads PFM as not implemented and EXR only with OpenEXR)."""
     suffix = path[path.rfind(".") + 1:].lower()
+    if suffix in ("hdr", "rgbe"):
+        return read_hdr(path)
     if suffix == "png":
         px = read_png(path, rgb=True)
     elif suffix in ("ppm", "pgm", "pnm"):
         px = read_pnm(path)
     else:
-        raise ValueError(f"unsupported image format '{suffix}' (PNG, PPM and PGM are read)")
+        raise ValueError(f"unsupported image format '{suffix}' (PNG, PPM, PGM and Radiance HDR are read)")
     return px.astype(np.float32) / np.float32(255.0)

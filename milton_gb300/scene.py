@@ -18,6 +18,8 @@ A `Scene` holds exactly what crosses the C ABI (``mgpu_scene_desc``):
 * ``tri_uv``    (T, 3, 2) float32  per-vertex uvs, or None (every uv is (0, 0))
 * ``textures``  list of `Texture`: image maps named by the material texture slots
                                    [10] kd, [11] ks, [12] transparency, [13] bump (1 + index)
+* ``background_tex`` int           1 + index of the environment map (latitude-longitude), or 0
+* ``background_le``  (3,) float32  constant background radiance when background_tex is 0
 
 Materials use Milton's keys and defaults (Material.cpp:67-92, DiffuseBSDF.cpp:44-46,
 ModifiedPhongBSDF.cpp:48-81, DielectricBSDF.cpp:48-53): diffuse ``kd`` (0.5), Phong ``kd``/
@@ -164,6 +166,8 @@ class Scene:
     light_ext: np.ndarray | None = None
     tri_uv: np.ndarray | None = None
     textures: list = field(default_factory=list)
+    background_tex: int = 0
+    background_le: np.ndarray = field(default_factory=lambda: np.zeros(3, np.float32))
 
     def __post_init__(self):
         self.tri_v = np.ascontiguousarray(self.tri_v, np.float32).reshape(-1, 3, 3)
@@ -196,6 +200,9 @@ class Scene:
             self.tri_uv = np.ascontiguousarray(self.tri_uv, np.float32).reshape(-1, 3, 2)
             if self.tri_uv.shape[0] != T:
                 raise ValueError(f"tri_uv has {self.tri_uv.shape[0]} rows, expected {T}")
+        self.background_le = np.ascontiguousarray(np.broadcast_to(np.asarray(self.background_le, np.float32), 3))
+        if not 0 <= self.background_tex <= len(self.textures):
+            raise ValueError("background texture out of range")
         slots = self.materials[:, 10:14] if len(self.materials) else np.zeros((0, 4), np.float32)
         if np.any(slots < 0) or np.any(slots > len(self.textures)) or np.any(slots != np.floor(slots)):
             raise ValueError("material texture slot out of range")
@@ -217,6 +224,8 @@ class SceneBuilder:
         self.v, self.n, self.mat, self.light, self.flags = [], [], [], [], []
         self.uv: list[np.ndarray | None] = []
         self.textures: list[Texture] = []
+        self.bg_tex = 0
+        self.bg_le = np.zeros(3, np.float32)
         self.materials: list[np.ndarray] = []
         self.lights: list[np.ndarray] = []
         self.light_ext: list[np.ndarray] = []
@@ -226,6 +235,12 @@ class SceneBuilder:
     def material(self, rec: np.ndarray) -> int:
         self.materials.append(np.asarray(rec, np.float32))
         return len(self.materials) - 1
+
+    def background(self, tex: int = 0, le=(0.0, 0.0, 0.0)) -> None:
+        """The scene's background: an environment map (tex = a value from texture()) or the
+        constant radiance le."""
+        self.bg_tex = int(tex)
+        self.bg_le = np.broadcast_to(np.asarray(le, np.float32), 3).copy()
 
     def texture(self, tex: Texture) -> int:
         """Appends an image map; returns the value for a material texture slot (1 + index)."""
@@ -323,7 +338,7 @@ class SceneBuilder:
             tri_uv = np.concatenate([np.zeros((v.shape[0], 3, 2), np.float32) if u is None else u
                                      for u, v in zip(self.uv, self.v)])
         return Scene(
-            tri_uv=tri_uv, textures=list(self.textures),
+            tri_uv=tri_uv, textures=list(self.textures), background_tex=self.bg_tex, background_le=self.bg_le,
             tri_v=cat(self.v, (0, 3, 3), np.float32), tri_n=cat(self.n, (0, 3, 3), np.float32),
             tri_mat=cat(self.mat, (0,), np.int32), tri_light=cat(self.light, (0,), np.int32),
             tri_flags=cat(self.flags, (0,), np.uint32),

@@ -33,8 +33,10 @@ Emitters: a unit plane becomes a parallelogram light, a Triangle a triangle ligh
 frame and object-space area, a mesh one mesh light over its triangles (include/mgpu.h,
 ``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
 element: analytic shapes other than planes and cubes (sphere, cylinder, cone, blob, point),
-emitting cubes, omni and environment emitters, bump-mapped emitters, per-channel IOR or Phong
-exponents.  Image maps are taken: a material's kd / ks / transparency given as a file name and
+emitting cubes, omni emitters on shapes, oriented backgrounds, bump-mapped emitters,
+per-channel IOR or Phong exponents.  A scene's background is taken: an environment map
+(latitude-longitude image: PNG, PPM / PGM or Radiance HDR) or an omni background's constant
+radiance, added where a ray leaves the scene.  Image maps are taken: a material's kd / ks / transparency given as a file name and
 its bumpMap become textures (PNG, PPM / PGM) with the material's filter, repeatU / repeatV and
 bumpIntensity, and every triangle carries the uvs of Shape::_getUV for the shape it came from
 (Plane, Triangle, Cube -- from the world position, as the reference does -- and Mesh: the first
@@ -427,6 +429,7 @@ class _Loader:
 
     def __init__(self, base_dir: str, tessellate=None):
         self.tessellate = tessellate
+        self.bg = None  # the background element's material
         self.base_dir = base_dir
         self.stack: list[_Node] = []
         self.root: _Node | None = None
@@ -584,7 +587,44 @@ class _Loader:
             self.end()
 
     def background(self, v):
-        raise SceneFileError("background emitters (environment maps) are not supported by the GPU path")
+        """MiltonJSONSceneLoader::_parse_background (:1693-1720): at most one, holding exactly one
+        emitter, which may be an environment map (latitude-longitude image, `path`)."""
+        if not isinstance(v, JObj):
+            raise SceneFileError(f"background must be of type 'object', found '{_tname(v)}'")
+        if self.bg is not None:
+            raise SceneFileError("scene may contain at most one background element")
+        if len(v.pairs) == 0:
+            self.bg = _Material()
+            return
+        e = v.find("emitter")
+        if len(v.pairs) > 1 or e is _MISSING:
+            raise SceneFileError("background element must have exactly one child emitter element")
+        mat = _Material()
+        if not isinstance(e, JObj):
+            raise SceneFileError(f"emitter must be of type 'object', found '{_tname(e)}'")
+        t = e.find("type")
+        if t is _MISSING:
+            raise SceneFileError("unable to infer emitter type")
+        if not isinstance(t, str):
+            raise SceneFileError("emitter.type must be of type 'string'")
+        req = {}
+        if t == "null":
+            mat.props["emitter"] = "null"
+        elif t in ("omni", "oriented", "environment"):
+            mat.props["emitter"] = t
+            req.update(power="spectrum", glDiffuseColor="color3", glSpecularColor="color3", glAttenuation="vector3")
+            if t == "environment":
+                req.update(coords="string", path="string")
+        else:
+            raise SceneFileError("invalid emitter type")
+        _properties(req, e, mat.props)
+        if t == "environment" and "path" not in mat.props:
+            raise SceneFileError("environment map must contain a 'path' child element specifying an absolute or "
+                                 "relative path to an environment texture")
+        if t == "oriented":
+            raise SceneFileError("an oriented background emitter is not supported by the GPU path (it has no "
+                                 "surface normal to orient by)")
+        self.bg = mat
 
     def material(self, v):
         mat = _Material()
@@ -1140,6 +1180,24 @@ class _Flattener:
                 slots[3] = self.texture(bump, img, S.TEX_BUMP, flt, ru, rv, intensity)
         return slots
 
+    def background(self, mat: "_Material | None"):
+        """The scene's background (Scene::setBackground, MiltonJSONSceneLoader.cpp:325-327): an
+        environment map is a colour map with the background material's default filter and
+        repeat (EnvironmentMap.cpp:21-56); an omni background is power / 4 pi
+        (OmniEmitter.cpp; the null surface point has no area)."""
+        if mat is None or mat.props.get("emitter", "null") == "null":
+            return
+        if mat.props["emitter"] == "environment":
+            name = mat.props["path"]
+            img = self.image(name)
+            if img is None:
+                # the reference asserts and then dereferences the missing image
+                raise SceneFileError(f"failed to load environment map image '{name}'")
+            self.b.background(tex=self.texture(name, img, S.TEX_COLOR, ("triangle", 2.0, {}), 1.0, 1.0, 5.0))
+        else:  # omni
+            power = np.broadcast_to(np.asarray(mat.props.get("power", 0.0), np.float64), 3)
+            self.b.background(le=power / (4.0 * math.pi))
+
     def texture(self, name, img, kind, flt, ru, rv, intensity) -> int:
         key = (name, kind, repr(flt) if kind == S.TEX_COLOR else "", ru, rv, intensity)
         if key not in self.tex_index:
@@ -1405,6 +1463,7 @@ def loads(text: str, base_dir: str = ".", source: str = "<string>", tessellate=N
     ld.root_obj(parse_text(text))
     fl = _Flattener(ld.named, base_dir)
     fl.run(ld.root)
+    fl.background(ld.bg)
     out = dict(ld.output_props)
     w, h, found = 480, 480, False
     for key in ("size", "dimensions"):

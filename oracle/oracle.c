@@ -39,6 +39,8 @@
  *                          its application at one texel), M/filters/{Box,Triangle,Gaussian,Mitchell,
  *                          LanczosSinc}Filter.cpp (evaluate), M/shapes/Triangle.cpp:23-39 (uv),
  *                          M/common/image/Rgba.inl:32-45 (byte / 255, luminance)
+ *   background             M/core/Scene.cpp:116-118, M/renderers/renderers/PathTracer.cpp:39-42,
+ *                          M/materials/emitters/EnvironmentMap.cpp:40-96, OmniEmitter.cpp
  *   constants              M/common/arch.h:120-137 (EPSILON 1e-7, double), M/common/utilities.h:240 (EQ),
  *                          M/materials/IndexOfRefraction.cpp:16 (AIR = 1.0003)
  *
@@ -183,6 +185,8 @@ typedef struct {
   const float *uv;     /* ntri * 6 per-vertex uvs, or NULL */
   int ntex;
   orc_tex *tex;
+  int bg_tex;          /* background: 1 + colour map (environment map) or 0 */
+  double bg_le[3];     /* constant background radiance when bg_tex == 0 */
 } orc_scene;
 
 static inline v3 tri_vert(const orc_scene *s, int64_t t, int k) {
@@ -1157,6 +1161,21 @@ static void apply_textures(const orc_scene *s, int64_t tri, v3 p, orc_mat *m, v3
   if (m->tex[3]) *ns = tex_bump(&s->tex[m->tex[3] - 1], u, v, *ns);
 }
 
+/* Scene::getBackgroundRadiance(d) = background->getLe(-d) (Scene.cpp:116-118): an
+ * EnvironmentMap's lookup (EnvironmentMap.cpp:40-96: latitude-longitude uv of the direction,
+ * then the material's getSample-style filtered texel) or an omni background's constant */
+static void background(const orc_scene *s, v3 d, double out[3]) {
+  if (!s->bg_tex) {
+    for (int k = 0; k < 3; ++k) out[k] = s->bg_le[k];
+    return;
+  }
+  v3 w = vneg(d);
+  double rho = sqrt(w.x * w.x + w.z * w.z), mag = vlen(w);
+  double theta = rho < fabs(w.y) ? acos(rho / mag) * (w.y >= 0 ? 1 : -1) : asin(w.y / mag);
+  double phi = (w.x == 0 && w.z == 0) ? 0 : atan2(w.x, w.z);
+  tex_color(&s->tex[s->bg_tex - 1], phi / (-2 * ORC_PI) + 0.5, theta / -ORC_PI + 0.5, out);
+}
+
 /* Shape::getPoint for light sample m at (u, v) (Shape.cpp:52-64): Plane::getPosition
  * (Plane.cpp:91-93); Triangle::getPosition (Triangle.cpp:332-354), whose "barycentrics" are
  * magnitudes of 2-D cross products in the triangle's uv frame; Mesh::getPosition / getPoint
@@ -1238,7 +1257,10 @@ static void evaluate(const orc_render_ctx *c, orc_path *ph, v3 o, v3 d, int dept
   int64_t tri;
   ph->rays_ext++;
   double t = kd_closest(s, c->tr, o, d, &tri, NULL);
-  if (!(t > ORC_EPS && t < ORC_INF)) return; /* background is black */
+  if (!(t > ORC_EPS && t < ORC_INF)) { /* PathTracer.cpp:39-42: a miss adds the background */
+    background(s, d, out);
+    return;
+  }
   v3 p = vadd(o, vmul(d, t));
   v3 ns = shading_normal(s, tri, p);
   const orc_mat *m = &s->mats[s->mat[tri]];
@@ -1367,12 +1389,18 @@ static void *render_thread(void *arg) {
 int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat, const int32_t *light,
                const uint32_t *flags, int nmat, const float *mats, int nlight, const float *lights,
                const float *light_ext, const float *tri_uv, int ntex, const float *tex_params,
-               const float *const *tex_rgb, const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed,
-               uint32_t stream, double *film_sum, double *path_out, uint64_t *stats_out) {
+               const float *const *tex_rgb, const float *bg, const orc_tree *tr, const float *camera,
+               const int32_t *ip, uint64_t seed, uint32_t stream, double *film_sum, double *path_out,
+               uint64_t *stats_out) {
   orc_scene *s = scene_from_arrays(ntri, v, n, mat, light, flags, nmat, mats, nlight, lights, light_ext);
   s->uv = tri_uv;
   s->ntex = ntex;
   s->tex = textures_from(ntex, tex_params, tex_rgb);
+  /* bg: 1 + background texture, then the constant background radiance (NULL = black) */
+  if (bg) {
+    s->bg_tex = (int)bg[0];
+    for (int k = 0; k < 3; ++k) s->bg_le[k] = bg[1 + k];
+  }
   orc_render_ctx c;
   c.s = s;
   c.tr = tr;
@@ -1475,6 +1503,25 @@ void orc_texture_lookup(const float *params, const float *rgb, double u, double 
   }
   free(t->wts);
   free(t);
+}
+
+/* background radiance of a ray with direction d (tests): params / rgb describe the environment
+ * map (NULL: constant le) */
+void orc_background(const float *params, const float *rgb, const double *le, const double *d, double *out) {
+  orc_scene s;
+  memset(&s, 0, sizeof(s));
+  if (params) {
+    s.ntex = 1;
+    s.tex = textures_from(1, params, &rgb);
+    s.bg_tex = 1;
+  } else {
+    for (int k = 0; k < 3; ++k) s.bg_le[k] = le[k];
+  }
+  background(&s, V(d[0], d[1], d[2]), out);
+  if (s.tex) {
+    free(s.tex[0].wts);
+    free(s.tex);
+  }
 }
 
 void orc_uniforms(uint64_t seed, uint32_t stream, uint64_t path, uint32_t depth, uint32_t block, double *u4) {

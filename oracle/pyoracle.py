@@ -34,7 +34,8 @@ def load() -> C.CDLL:
     lib.orc_trace_any.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp]
     lib.orc_render.restype = C.c_int
     lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp, vp,
-                               vp, u64, u32, vp, vp, vp]
+                               vp, vp, u64, u32, vp, vp, vp]
+    lib.orc_background.argtypes = [vp, vp, vp, vp, vp]
     lib.orc_texture_lookup.argtypes = [vp, vp, C.c_double, C.c_double, vp, vp]
     lib.orc_philox4x32_10.argtypes = [vp, vp, vp]
     lib.orc_camera_dir.argtypes = [vp, C.c_double, C.c_double, vp]
@@ -140,10 +141,13 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
     uv = None if uv is None else np.ascontiguousarray(uv, np.float32)
     textures = list(getattr(scene, "textures", []))
     tparams, trgb = texture_params(textures)
+    bg = np.zeros(4, np.float32)
+    bg[0] = getattr(scene, "background_tex", 0)
+    bg[1:4] = getattr(scene, "background_le", (0.0, 0.0, 0.0))
     lib.orc_render(scene.ntri, _p(scene.tri_v), _p(scene.tri_n), _p(scene.tri_mat), _p(scene.tri_light),
                    _p(scene.tri_flags), len(scene.materials), _p(scene.materials), len(scene.lights), _p(lights),
-                   _p(ext), _p(uv), len(textures), _p(tparams), C.cast(trgb, C.c_void_p), tree.h, _p(cam), _p(ip), seed,
-                   stream, _p(film), _p(paths), _p(st))
+                   _p(ext), _p(uv), len(textures), _p(tparams), C.cast(trgb, C.c_void_p), _p(bg), tree.h, _p(cam),
+                   _p(ip), seed, stream, _p(film), _p(paths), _p(st))
     mean = film[r0:r1] / max(sample_count, 1)
     if per_path:
         paths = paths.reshape(height, width, sample_count, 3)[r0:r1]
@@ -174,6 +178,21 @@ def texture_lookup(tex, u, v, normal=None) -> np.ndarray:
     n = None if normal is None else np.ascontiguousarray(normal, np.float64)
     lib.orc_texture_lookup(_p(params), rgb.ctypes.data, float(u), float(v), _p(n), _p(out))
     return out[:3] if tex.kind == 0 else out
+
+
+def background(direction, tex=None, le=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Background radiance of a ray with this direction: the environment map tex, or the
+    constant le."""
+    lib = load()
+    out = np.zeros(3, np.float64)
+    d = np.ascontiguousarray(direction, np.float64)
+    if tex is None:
+        lib.orc_background(None, None, _p(np.ascontiguousarray(le, np.float64)), _p(d), _p(out))
+    else:
+        params, _ = texture_params([tex])
+        rgb = np.ascontiguousarray(tex.rgb, np.float32)
+        lib.orc_background(_p(params), rgb.ctypes.data, None, _p(d), _p(out))
+    return out
 
 
 def philox(ctr, key) -> np.ndarray:

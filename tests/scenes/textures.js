@@ -1,7 +1,8 @@
 {
    /* Image maps: a checker kd map repeated on the floor (Lanczos filter), a bump-mapped back
     * wall, a Phong cube with a ks map (cube uvs) and a diffuse OBJ mesh with the checker, under
-    * a unit-plane light.  make_textures.py writes checker.png and bumps.ppm. */
+    * a unit-plane light, in a Radiance HDR environment seen through the open sides.
+    * make_textures.py writes checker.png, bumps.ppm and sky.hdr. */
    "scenefile" : {
       "renderer" : { "type" : "pathTracer", "noSuperSamples" : 16, "noDirectSamples" : 2,
                      "maxDepth" : 5, "rrStartDepth" : 3, },
@@ -9,6 +10,7 @@
                    "heightAngle" : 42, },
       "output" : { "width" : 40, "height" : 40, },
       "scene" : {
+         "background" : { "emitter" : { "type" : "environment", "path" : "sky.hdr", }, },
          "material" : {
             "repeatU" : 3, "repeatV" : 2,
             "filter" : { "type" : "lanczosSinc", "support" : 3, "tau" : 2 },

@@ -78,3 +78,28 @@ def test_texture_validation(cuda):
     sc.materials[sc.tri_mat[emit][0], 13] = 1 + [t.kind for t in sc.textures].index(S.TEX_BUMP)
     with pytest.raises(Exception, match="bump-mapped emitter"):
         pt.DeviceScene(sc, pt.Accel(sc))
+
+
+@pytest.mark.parametrize("kind", ["environment", "constant"])
+def test_background_per_path(cuda, oracle, kind):
+    # the plain box is open toward the camera: camera rays and bounces that leave it see the
+    # background (an environment map, or an omni background's constant radiance)
+    sc = scenegen.plain(2)
+    rng = np.random.default_rng(9)
+    if kind == "environment":
+        env = rng.uniform(0.0, 2.0, (24, 48, 3)).astype(np.float32)
+        sc.textures = [S.Texture(env, S.TEX_COLOR, ("gaussian", 3.0, {"sigma": 1.0}))]
+        sc.background_tex = 1
+    else:
+        sc.background_le = np.array([0.4, 0.5, 0.8], np.float32)
+    st = pt.RenderSettings(48, 48, 16, max_depth=5, rr_start_depth=3, seed=3)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, sc, st)
+    tree = oracle.Tree(sc.tri_v)
+    mean_o, paths_o, _ = oracle.render(sc, tree, st.width, st.height, st.spp, nds=1, max_depth=5, rr_start=3, seed=3,
+                                       per_path=True)
+    close = np.abs(paths_g - paths_o) <= 1e-4 + 2e-3 * np.maximum(np.abs(paths_g), np.abs(paths_o))
+    agree = np.all(close, axis=-1).mean()
+    print(f"background ({kind}): path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
+    assert agree >= 0.98
+    black, _, _ = gpu_render_paths(cuda, scenegen.plain(2), st)
+    assert mean_g.mean() > black.mean() + 0.02  # the background reaches the film

@@ -224,3 +224,88 @@ def test_bump_mapped_emitter_refused(tmp_path):
     with pytest.raises(L.SceneFileError, match="bump-mapped emitter"):
         L.loads(_scene('"material" : { "bumpMap" : "b.ppm", "emitter" : { "type" : "oriented" }, "plane" : { } }'),
                 base_dir=str(tmp_path))
+
+
+# --- backgrounds ---------------------------------------------------------------------------------
+
+def _rgbe_bytes(img: np.ndarray, rle_rows=()) -> bytes:
+    """Radiance RGBE encoding of (H, W, 3) floats; rows in rle_rows as new-style RLE scanlines
+    (one literal run and one repeat run per channel), the others flat."""
+    h, w, _ = img.shape
+    m = img.max(axis=2)
+    mant, ex = np.frexp(m)
+    scale = np.where(m > 1e-32, mant * 256.0 / np.where(m > 0, m, 1), 0.0)
+    px = np.zeros((h, w, 4), np.uint8)
+    px[..., :3] = np.clip(img * scale[..., None], 0, 255).astype(np.uint8)
+    px[..., 3] = np.where(m > 1e-32, ex + 128, 0).astype(np.uint8)
+    out = bytearray(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n" + f"-Y {h} +X {w}\n".encode())
+    for y in range(h):
+        if y in rle_rows:
+            out += bytes([2, 2, w >> 8, w & 0xFF])
+            for c in range(4):
+                lit = px[y, : w // 2, c]
+                out += bytes([len(lit)]) + lit.tobytes()
+                rest = px[y, w // 2:, c]
+                px[y, w // 2:, c] = rest[0]  # the repeat run carries the first value
+                out += bytes([128 + len(rest), int(rest[0])])
+        else:
+            out += px[y].tobytes()
+    return bytes(out), px
+
+
+def test_hdr_reader(tmp_path):
+    rng = np.random.default_rng(2)
+    img = (rng.random((5, 12, 3)) * 20).astype(np.float32)
+    img[1, 3] = 0.0
+    # a scanline that does not start with the RLE marker makes the rest of the file flat pixels
+    # (rgbe.cpp's RGBE_ReadPixels_RLE), so files are all flat or all run-length encoded
+    for name, rows in (("flat.hdr", ()), ("rle.hdr", range(5))):
+        data, px = _rgbe_bytes(img, rle_rows=rows)
+        (tmp_path / name).write_bytes(data)
+        got = imageio.read_image(str(tmp_path / name))
+        e = px[..., 3].astype(np.int64)
+        want = np.where(e[..., None] > 0, px[..., :3] * np.ldexp(1.0, e - 136)[..., None], 0.0)
+        assert got.shape == (5, 12, 3) and np.array_equal(got, want.astype(np.float32)), name
+        if not rows:
+            # 8-bit mantissas with a shared exponent: error below max(r, g, b) / 128
+            assert np.all(np.abs(got - img) <= img.max(axis=2, keepdims=True) / 128 + 1e-6)
+
+
+def _np_env_uv(d):
+    w = -np.asarray(d, np.float64)
+    rho, mag = math.hypot(w[0], w[2]), np.linalg.norm(w)
+    theta = math.acos(rho / mag) * (1 if w[1] >= 0 else -1) if rho < abs(w[1]) else math.asin(w[1] / mag)
+    phi = 0.0 if (w[0] == 0 and w[2] == 0) else math.atan2(w[0], w[2])
+    return phi / (-2 * math.pi) + 0.5, theta / -math.pi + 0.5
+
+
+def test_oracle_background(oracle):
+    rng = np.random.default_rng(4)
+    env = S.Texture(rng.random((16, 32, 3)).astype(np.float32) * 3)
+    for d in list(rng.normal(size=(30, 3))) + [np.array([0.0, 1.0, 0.0]), np.array([0.0, -1.0, 0.0])]:
+        d = d / np.linalg.norm(d)
+        u, v = _np_env_uv(d)
+        assert np.allclose(oracle.background(d, env), _np_lookup(env, u, v), rtol=1e-6, atol=1e-9)
+    assert np.allclose(oracle.background([0, 0, 1], le=(0.5, 1.0, 2.0)), (0.5, 1.0, 2.0))
+
+
+def test_loader_background(tmp_path):
+    (tmp_path / "sky.ppm").write_bytes(b"P6 2 1 255\n\x10\x20\x30\x40\x50\x60")
+    sf = L.loads(_scene('"background" : { "emitter" : { "type" : "environment", "path" : "sky.ppm" } }, '
+                        '"triangle" : { }'), base_dir=str(tmp_path))
+    s = sf.scene
+    assert s.background_tex == 1 and s.textures[0].filter == ("triangle", 2.0, {})
+    assert np.allclose(s.textures[0].rgb[0, 1], np.array([0x40, 0x50, 0x60]) / 255)
+    sf = L.loads(_scene('"background" : { "emitter" : { "type" : "omni", "power" : [1, 2, 4] } }, "triangle" : { }'))
+    assert sf.scene.background_tex == 0 and np.allclose(sf.scene.background_le, np.array([1, 2, 4]) / (4 * math.pi))
+    assert np.all(L.loads(_scene('"background" : { }, "triangle" : { }')).scene.background_le == 0)
+    with pytest.warns(UserWarning, match="nope.hdr"), pytest.raises(L.SceneFileError, match="failed to load environment"):
+        L.loads(_scene('"background" : { "emitter" : { "type" : "environment", "path" : "nope.hdr" } }'))
+    with pytest.raises(L.SceneFileError, match="must contain a 'path'"):
+        L.loads(_scene('"background" : { "emitter" : { "type" : "environment" } }'))
+    with pytest.raises(L.SceneFileError, match="at most one background"):
+        L.loads(_scene('"background" : { }, "background" : { }'))
+    with pytest.raises(L.SceneFileError, match="exactly one child emitter"):
+        L.loads(_scene('"background" : { "emitter" : { "type" : "null" }, "x" : 1 }'))
+    with pytest.raises(L.SceneFileError, match="oriented background"):
+        L.loads(_scene('"background" : { "emitter" : { "type" : "oriented" } }'))
