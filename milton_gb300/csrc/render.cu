@@ -327,6 +327,9 @@ __device__ __forceinline__ V3 fold_slots(const RenderArgs &a, int nl, int64_t p,
   return L;
 }
 
+// SURF: the wave has a scene with image maps or a background.  Scenes without them run the
+// variant that has neither branch, whose register allocation (and spilling) is the lighter.
+template <bool SURF>
 __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const int cur = b & 1, nxt = (b + 1) & 1;
@@ -376,7 +379,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         int mi = __float_as_int(s0.w);
         self = __float_as_int(s1.w);
         m = load_mat(J, mi);
-        if ((m.tex_kd | m.tex_ks | m.tex_tr | m.tex_bump) != 0) apply_textures(J, prim, b0, b1, b2, m, ns);
+        if (SURF && (m.tex_kd | m.tex_ks | m.tex_tr | m.tex_bump) != 0) apply_textures(J, prim, b0, b1, b2, m, ns);
         bool spec = is_specular(m);
         if (spec) flags |= kFlagSpecular;
         if (self >= 0) {
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
             }
           }
         }
-      } else if (J.bg_tex != 0 || J.bg_le[0] != 0.0f || J.bg_le[1] != 0.0f || J.bg_le[2] != 0.0f) {
+      } else if (SURF && (J.bg_tex != 0 || J.bg_le[0] != 0.0f || J.bg_le[1] != 0.0f || J.bg_le[2] != 0.0f)) {
         L = L + mul(thr, background(J, d));  // PathTracer.cpp:39-42: a miss adds the background
       }
       a.path_L[p] = make_float4(L.x, L.y, L.z, __uint_as_float(flags));
@@ -1143,7 +1146,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   auto kshw = persist ? k_shadow<COUNT, true> : k_shadow<COUNT, false>;
   const int g_gen = grid_for((const void *)k_generate, 0);
   const int g_ext = grid_for((const void *)kext, 0);
-  const int g_sha = grid_for((const void *)k_shade, 0);
+  const int g_sha = grid_for((const void *)k_shade<true>, 0);
   const int g_shw = grid_for((const void *)kshw, 0);
   const int g_acc = grid_for((const void *)k_accumulate, 0);
   const int g_bin = device_sm_count() * 4;
@@ -1196,6 +1199,10 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
     a.tcount = w->tcount;
     a.max_b = wv.max_b;
     const int max_b = wv.max_b;
+    bool surf = false;  // a chunk's scene has image maps or a background
+    for (const JobArgs &c : wv.chunks)
+      surf = surf || c.texrec != nullptr || c.bg_tex != 0 || c.bg_le[0] != 0.0f || c.bg_le[1] != 0.0f ||
+             c.bg_le[2] != 0.0f;
     err = cudaMemsetAsync(w->counters, 0, kNumCounters * sizeof(uint32_t), st);
     int m = pf.begin(kProfGenerate, st);
     k_generate<<<g_gen, kBlock, 0, st>>>(a);
@@ -1211,7 +1218,8 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
         kext<<<g_ext, kBlock, 0, st>>>(a, b);
         pf.end(m, st);
         m = pf.begin(kProfShade, st);
-        k_shade<<<g_sha, kBlock, 0, st>>>(a, b);
+        if (surf) k_shade<true><<<g_sha, kBlock, 0, st>>>(a, b);
+        else k_shade<false><<<g_sha, kBlock, 0, st>>>(a, b);
         pf.end(m, st);
         if (a.bin_sh || a.bin_ext) {
           m = pf.begin(kProfBin, st);
@@ -1430,7 +1438,7 @@ int mgpu_tune_set(const char *key, int64_t value) {
                            (const void *)k_extend<true, false>,  (const void *)k_extend<true, true>,
                            (const void *)k_shadow<false, false>, (const void *)k_shadow<false, true>,
                            (const void *)k_shadow<true, false>,  (const void *)k_shadow<true, true>,
-                           (const void *)k_shade};
+                           (const void *)k_shade<false>, (const void *)k_shade<true>};
     for (const void *kf : kerns)
       MGPU_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)value));
     g_tune.carveout.store((int)value);
