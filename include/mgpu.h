@@ -93,6 +93,11 @@ typedef struct {
  *                                   more uniforms r1, r2, normal = interpolated vertex normals
  *                                   (Mesh::getPosition / getPoint, Mesh.cpp:436-448,
  *                                   MeshTriangle::getPosition, MeshTriangle.cpp:299-333)
+ *              MGPU_LIGHT_POINT     nothing more: a Milton `PointShape` at center, area 0, one
+ *                                   light sample, no normal (cosine 1) and no triangles
+ *                                   (DirectIllumination.cpp:90-130)
+ *              [15] 1 = an OmniEmitter: Le in every direction, both sides (OmniEmitter.cpp);
+ *                   0 = OrientedEmitter (the normal's side); points are omni either way
  *   tri_uv     NULL (every uv is (0, 0)) or ntri*6 floats: the uv of each vertex; a hit's uv is
  *              their barycentric interpolation (Shape::_getUV of the shape the triangle came from:
  *              Triangle.cpp:23-39, Plane.cpp:52-59, Cube.cpp:84-105 and Mesh.cpp:408-416 are
@@ -155,6 +160,7 @@ struct mgpu_texture {
 #define MGPU_LIGHT_PLANE 0
 #define MGPU_LIGHT_TRIANGLE 1
 #define MGPU_LIGHT_MESH 2
+#define MGPU_LIGHT_POINT 3
 
 /* Render parameters.  Defaults mirror Milton's PathTracer/DirectIllumination keys:
  * noDirectSamples 1, efficientDirect 1, no maximum depth, Russian roulette from depth 2

@@ -368,7 +368,7 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     if (!desc->light_ext) continue;
     const float *x = desc->light_ext + 16 * (size_t)i;
     memcpy(&lrec[32 * (size_t)i + 16], x, 16 * sizeof(float));
-    if (!(x[0] == 0.0f || x[0] == 1.0f || x[0] == 2.0f))
+    if (!(x[0] == 0.0f || x[0] == 1.0f || x[0] == 2.0f || x[0] == 3.0f))
       return fail(MGPU_E_INVALID, "mgpu_scene_create: unknown light type at light " + std::to_string(i));
     if (x[0] == 2.0f) {
       uint32_t first, count;
@@ -380,6 +380,11 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   }
   TexPlan tp;
   if (int rc = tex_plan(desc, tp)) return rc;
+  // triangles cannot emit as a point light (it has no surface)
+  if (desc->tri_light && desc->light_ext)
+    for (int64_t t = 0; t < T; ++t)
+      if (desc->tri_light[t] >= 0 && desc->light_ext[16 * (size_t)desc->tri_light[t]] == 3.0f)
+        return fail(MGPU_E_INVALID, "mgpu_scene_create: triangle " + std::to_string(t) + " names a point light");
   const KdTree &tr = accel->tree;
   mgpu_accel *acc = const_cast<mgpu_accel *>(accel);
   register_staging(acc);

@@ -76,10 +76,10 @@ MGPU_HD void tex_apply(Material &m, int slot, float r, float g, float b) {
 
 MGPU_HD bool is_specular(const Material &m) { return m.type == 2; }
 
-// Area light: a Milton `Plane` under a transform (type 0), a standalone `Triangle` (type 1) or
-// a `Mesh` (type 2).  Record: 16 floats (center / v1, ex, ez, normal, area, Le) + 16 extension
-// floats (type, triangle uv frame, mesh triangle run).
-constexpr int kLightPlane = 0, kLightTriangle = 1, kLightMesh = 2;
+// Light: a Milton `Plane` under a transform (type 0), a standalone `Triangle` (type 1), a `Mesh`
+// (type 2) or a `PointShape` (type 3, area 0).  Record: 16 floats (center / v1, ex, ez, normal,
+// area, Le) + 16 extension floats (type, triangle uv frame, mesh triangle run, [15] omni).
+constexpr int kLightPlane = 0, kLightTriangle = 1, kLightMesh = 2, kLightPoint = 3;
 constexpr uint32_t kMeshLightBlock = 0x4000u;  // RNG block of a mesh light sample's extra pair
 
 struct Light {
@@ -89,6 +89,7 @@ struct Light {
   int type;
   float u0, v0, ax, ay, bx, by, inv_ab;  // Triangle: uv0, a = uv1 - uv0, b = uv2 - uv0, 1/|a x b|
   uint32_t first, count;                  // Mesh: triangle run in the soup
+  bool omni;                              // OmniEmitter: emits on both sides (and points)
 };
 
 MGPU_HD Light light_from(const float *l, const float *x) {
@@ -103,6 +104,7 @@ MGPU_HD Light light_from(const float *l, const float *x) {
   r.u0 = x[1]; r.v0 = x[2]; r.ax = x[3]; r.ay = x[4]; r.bx = x[5]; r.by = x[6]; r.inv_ab = x[7];
   r.first = f_bits(x[8]);
   r.count = f_bits(x[9]);
+  r.omni = x[15] != 0.0f || r.type == kLightPoint;
   return r;
 }
 
@@ -138,6 +140,12 @@ MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, V
     p = a * b0 + b * b1 + c * b2;
     n = normalize(nrm(t, 0) * b0 + nrm(t, 1) * b1 + nrm(t, 2) * b2);
     g = normalize(cross(b - a, c - a));
+  } else if (L.type == kLightPoint) {
+    // PointShape: the point itself, no normal (SurfacePoint's stand-in dot product is 1) and no
+    // surface to move the shadow ray's end off
+    p = L.center;
+    n = v3(0.0f, 0.0f, 0.0f);
+    g = n;
   } else {
     p = L.center + L.ex * (u - 0.5f) + L.ez * (v - 0.5f);
     n = L.normal;
@@ -398,6 +406,10 @@ MGPU_HD int bsdf_sample(const Material &m, V3 ns, V3 wi, uint32_t ior_index, flo
 
 // OrientedEmitter::getLe (OrientedEmitter.cpp:17-23) with radiance already power/(area pi)
 MGPU_HD V3 emitted(V3 Le, V3 n, V3 w) { return dot(n, w) > 0.0f ? Le : v3(0.0f, 0.0f, 0.0f); }
+
+// Emitter::getLe of a light in direction w from a point with normal n: OrientedEmitter on the
+// normal's side only (OrientedEmitter.cpp:17-23), OmniEmitter in every direction (OmniEmitter.cpp)
+MGPU_HD V3 light_le(const Light &L, V3 n, V3 w) { return L.omni ? L.Le : emitted(L.Le, n, w); }
 
 // Origin offset against self-intersection: Waechter and Binder, "A Fast and Robust Method
 // for Avoiding Self-Intersection", Ray Tracing Gems ch. 6 (2019).  n points to the side the

@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         if (spec) flags |= kFlagSpecular;
         if (self >= 0) {
           Light lt = load_light(J, self);
-          V3 Le = emitted(lt.Le, ns, -d);
+          V3 Le = light_le(lt, ns, -d);
           if (!J.efficient || depth == 0) L = L + mul(thr, Le);
           else if (ec) L = L + mul(thr, Le) * (lt.area / (t * t));
         }
@@ -444,8 +444,9 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         int li = k / s2n, within = k - li * s2n;
         int sy = within / J.nds_side, sx = within - sy * J.nds_side;
         V3 c = v3(0.0f, 0.0f, 0.0f);
-        if (li != self) {
-          Light lt = load_light(J, li);
+        Light lt = load_light(J, li);
+        // a point light takes one sample (DirectIllumination.cpp:97-99): the first stratum
+        if (li != self && (lt.type != kLightPoint || within == 0)) {
           F4u u = uniforms(J.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
           float ux = ((float)sx + ((k & 1) ? u.c : u.a)) / (float)J.nds_side;
           float uy = ((float)sy + ((k & 1) ? u.d : u.b)) / (float)J.nds_side;
@@ -470,11 +471,13 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
           V3 wo = lp - P;
           float t = length(wo);
           wo = wo * (1.0f / t);
-          float cwo = fabsf(dot(ns, wo)), cwi = fabsf(dot(ln, wo));
+          const bool point = lt.type == kLightPoint;
+          float cwo = fabsf(dot(ns, wo)), cwi = point ? 1.0f : fabsf(dot(ln, wo));
           V3 fr = bsdf_eval(m, ns, d, wo);
           if (cwo > 0.0f && cwi > 0.0f && nonzero(fr)) {
-            V3 Le = emitted(lt.Le, ln, -wo);
-            c = mul(thr, mul(fr, Le)) * (cwo * cwi / (t * t) * lt.area * inv_nds);
+            V3 Le = light_le(lt, ln, -wo);
+            // area / samples for an area light, 1 for a point (DirectIllumination.cpp:127-128)
+            c = mul(thr, mul(fr, Le)) * (cwo * cwi / (t * t) * (point ? 1.0f : lt.area * inv_nds));
             if (nonzero(c)) {
               want = true;
               // both ends of the shadow segment are moved off their surfaces toward each other

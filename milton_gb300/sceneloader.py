@@ -32,9 +32,11 @@ which material are kept as the reference has them:
 Emitters: a unit plane becomes a parallelogram light, a Triangle a triangle light with its uv
 frame and object-space area, a mesh one mesh light over its triangles (include/mgpu.h,
 ``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
-element: analytic shapes other than planes and cubes (sphere, cylinder, cone, blob, point),
-emitting cubes, omni emitters on shapes, oriented backgrounds, bump-mapped emitters,
-per-channel IOR or Phong exponents.  A scene's background is taken: an environment map
+element: analytic shapes other than planes, cubes and points (sphere, cylinder, cone, blob),
+emitting cubes, oriented backgrounds, bump-mapped emitters, per-channel IOR or Phong exponents.
+Emitters are oriented (one-sided, power / (area pi)) or omni (both sides, power / (area 4 pi))
+on planes, triangles and meshes, and point lights (a "point" shape with either emitter: one
+light sample, no area).  A scene's background is taken: an environment map
 (latitude-longitude image: PNG, PPM / PGM or Radiance HDR) or an omni background's constant
 radiance, added where a ray leaves the scene.  Image maps are taken: a material's kd / ks / transparency given as a file name and
 its bumpMap become textures (PNG, PPM / PGM) with the material's filter, repeatU / repeatV and
@@ -777,14 +779,14 @@ class _Loader:
             req.update(vertices="vector9", normals="vector9", normal="vector3", uvs="vector6")
         elif t == "shapeSet":
             return self.shape_set(v)
-        elif t == "cube":
+        elif t in ("cube", "point"):
             pass
         elif t == "sphere" and self.tessellate:
             req.update(position="point3", radius="real_t")
-        elif t in ("sphere", "cylinder", "cone", "blob", "point", "dynamic"):
+        elif t in ("sphere", "cylinder", "cone", "blob", "dynamic"):
             raise SceneFileError(f"shape '{t}' is not a triangle shape; the GPU path renders planes, cubes, "
-                                 "triangles and meshes" + (" (spheres with tessellate=(nu, nv))" if t == "sphere"
-                                                           else ""))
+                                 "triangles, meshes and points" + (" (spheres with tessellate=(nu, nv))"
+                                                                   if t == "sphere" else ""))
         else:
             raise SceneFileError("invalid shape type")
         props = {}
@@ -801,6 +803,8 @@ class _Loader:
             node = _Node("shape", _Shape("triangle", {"v": verts, "uvs": props.get("uvs", (0, 0, 1, 0, 0, 1))}))
         elif t == "cube":
             node = _Node("shape", _Shape("cube"))
+        elif t == "point":
+            node = _Node("shape", _Shape("point"))
         elif t == "sphere":
             # Milton's Sphere: a unit-diameter sphere under T(position) S(2 radius) (:575-589),
             # here an nu x nv UV sphere with radial normals -- an approximation of the analytic
@@ -1245,9 +1249,26 @@ class _Flattener:
             return
         props = self.active.props
         emitter = props.get("emitter", "null")
-        if emitter not in ("null", "oriented"):
-            raise SceneFileError(f"'{emitter}' emitters are not supported by the GPU path (oriented area lights "
-                                 "on planes are)")
+        if emitter not in ("null", "oriented", "omni"):
+            raise SceneFileError(f"'{emitter}' emitters are not supported by the GPU path (oriented and omni "
+                                 "emitters are)")
+        # OrientedEmitter: Le = power / (area pi) on the normal's side; OmniEmitter: power / (area
+        # 4 pi) in every direction (Emitter.cpp:34-50, OrientedEmitter.cpp:17-23, OmniEmitter.cpp)
+        per_sr = math.pi if emitter == "oriented" else 4.0 * math.pi
+        omni_ext = np.zeros(16, np.float32)
+        omni_ext[15] = 1.0 if emitter == "omni" else 0.0
+        if sh.kind == "point":
+            # PointShape (PointShape.cpp): its position; area 0, so Le = power / pi or power / 4 pi
+            if emitter != "null":
+                power = np.broadcast_to(np.asarray(props.get("power", (1.0, 1.0, 1.0)), np.float64), 3)
+                rec = np.zeros(16, np.float32)
+                rec[0:3] = _xf_points(trans @ sh.local, [(0.0, 0.0, 0.0)])[0]
+                rec[9:12] = (0.0, 1.0, 0.0)
+                rec[13:16] = power / per_sr
+                ext = omni_ext.copy()
+                ext[0] = 3
+                self.b.add_light(rec, ext)
+            return
         mi = self.material_record(self.active)
         if emitter != "null" and self.b.materials[mi][13] != 0:
             raise SceneFileError("a bump-mapped emitter is not supported by the GPU path (its light samples "
@@ -1257,15 +1278,15 @@ class _Flattener:
         if sh.kind == "plane":
             corners = _xf_points(m, [(-0.5, 0, -0.5), (0.5, 0, -0.5), (0.5, 0, 0.5), (-0.5, 0, 0.5)])
             nrm = _xf_normals(m, [(0.0, 1.0, 0.0)])[0]
-            if emitter == "oriented":
+            if emitter != "null":
                 center = _xf_points(m, [(0, 0, 0)])[0]
                 ex = m[:3, :3] @ np.array([1.0, 0.0, 0.0])
                 ez = m[:3, :3] @ np.array([0.0, 0.0, 1.0])
                 area = float(np.linalg.norm(np.cross(ex, ez)))
                 power = np.broadcast_to(np.asarray(props.get("power", (1.0, 1.0, 1.0)), np.float64), 3)
-                rec = S.quad_light(center, ex, ez, power / (area * math.pi))
+                rec = S.quad_light(center, ex, ez, power / (area * per_sr))
                 rec[9:12] = nrm  # emitting side: the transformed +y (inverse transpose)
-                li = self.b.add_light(rec)
+                li = self.b.add_light(rec, omni_ext)
             else:
                 li = -1
             tris = np.array([corners[[0, 3, 2]], corners[[0, 2, 1]]], np.float64)
@@ -1282,7 +1303,7 @@ class _Flattener:
             nrm = _xf_normals(m, [n_obj / np.linalg.norm(n_obj)])[0]
             vi = v[[0, 2, 1]] if np.linalg.det(m[:3, :3]) < 0 else v  # culling follows the object-space winding
             li = -1
-            if emitter == "oriented":
+            if emitter != "null":
                 # Triangle::_getSurfaceArea is the object-space area (Triangle.cpp:356-362)
                 obj_area = 0.5 * float(np.linalg.norm(n_obj))
                 uv = np.asarray(sh.data["uvs"], np.float64).reshape(3, 2)
@@ -1293,8 +1314,8 @@ class _Flattener:
                 rec = np.zeros(16, np.float32)
                 rec[0:3], rec[3:6], rec[6:9], rec[9:12] = v[0], v[1] - v[0], v[2] - v[0], nrm
                 rec[12] = obj_area
-                rec[13:16] = power / (obj_area * math.pi)
-                ext = np.zeros(16, np.float32)
+                rec[13:16] = power / (obj_area * per_sr)
+                ext = omni_ext.copy()
                 ext[0] = 1
                 ext[1:3], ext[3:5], ext[5:7], ext[7] = uv[0], a, b, 1.0 / cross
                 li = self.b.add_light(rec, ext)
@@ -1323,10 +1344,11 @@ class _Flattener:
             inv = np.linalg.inv(m)
             nw = normals @ inv[:3, :3]  # not normalised: interpolated, then normalised per hit
             fuv = sh.data.get("uv")
-            if emitter == "oriented":
+            if emitter != "null":
                 tv = vw[faces]
                 area = 0.5 * float(np.linalg.norm(np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0]), axis=1).sum())
-                self.b.add_mesh_light(sh.data["path"], tv, nw[nfaces], power / (area * math.pi), mi, uv=fuv)
+                li = self.b.add_mesh_light(sh.data["path"], tv, nw[nfaces], power / (area * per_sr), mi, uv=fuv)
+                self.b.light_ext[li][15] = omni_ext[15]
             else:
                 self.b.add(sh.data["path"], vw[faces], nw[nfaces], mi, uv=fuv)
 

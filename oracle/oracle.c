@@ -169,6 +169,7 @@ typedef struct {
   int type;
   double u0, v0, ax, ay, bx, by, inv_ab;
   int64_t first, count;
+  int omni;  /* OmniEmitter (both sides; every point light) */
 } orc_light;
 
 typedef struct {
@@ -744,6 +745,7 @@ static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n
       s->lights[i].inv_ab = x[7];
       s->lights[i].first = first;
       s->lights[i].count = count;
+      s->lights[i].omni = x[15] != 0.0f || s->lights[i].type == 3;
     }
   }
   return s;
@@ -1204,6 +1206,9 @@ static void light_point(const orc_render_ctx *c, const orc_path *ph, int depth, 
     if (sum > 0) { b0 = r1 / sum; b1 = v / sum; b2 = r2 / sum; }
     *pos = vadd(vadd(vmul(tri_vert(s, t, 0), b0), vmul(tri_vert(s, t, 1), b1)), vmul(tri_vert(s, t, 2), b2));
     *nrm = vnorm(vadd(vadd(vmul(tri_nrm(s, t, 0), b0), vmul(tri_nrm(s, t, 1), b1)), vmul(tri_nrm(s, t, 2), b2)));
+  } else if (L->type == 3) {
+    *pos = L->center; /* PointShape: no normal (SurfacePoint.h:130-151: its dot product is 1) */
+    *nrm = V(0, 0, 0);
   } else {
     *pos = vadd(vadd(L->center, vmul(L->ex, u - 0.5)), vmul(L->ez, v - 0.5));
     *nrm = L->normal;
@@ -1221,8 +1226,10 @@ static void direct_light(const orc_render_ctx *c, orc_path *ph, int depth, v3 p,
     if (i == light_self) continue;
     const orc_light *L = &s->lights[i];
     double dir[3] = {0, 0, 0};
-    for (int sy = 0; sy < side; ++sy)
-      for (int sx = 0; sx < side; ++sx) {
+    /* isPoint (area <= EPSILON for a PointShape): one sample, no area factor (:90-130) */
+    const int point = L->type == 3;
+    for (int sy = 0; sy < (point ? 1 : side); ++sy)
+      for (int sx = 0; sx < (point ? 1 : side); ++sx) {
         int m = (i * side + sy) * side + sx; /* flat NEE sample index */
         double u4[4];
         orc_u4(&c->rng, ph->path, (uint32_t)depth, 1u + (uint32_t)(m >> 1), u4);
@@ -1234,19 +1241,20 @@ static void direct_light(const orc_render_ctx *c, orc_path *ph, int depth, v3 p,
         double t = vlen(wo);
         wo = vmul(wo, 1.0 / t);
         double cwo = fabs(vdot(b->ns, wo));
-        double cwi = fabs(vdot(ln, vneg(wo)));
+        double cwi = point ? 1.0 : fabs(vdot(ln, vneg(wo)));
         double fr[3];
         bsdf_eval(b, wo, fr);
         if (cwo > 0 && cwi > 0 && (fr[0] != 0 || fr[1] != 0 || fr[2] != 0)) {
           ph->rays_shadow++;
           /* Scene::intersects(ray, t - EPS) -> ShapeSet/kd intersects(ray, t - 2 EPS) */
           if (!kd_any(s, c->tr, p, wo, t - 2 * ORC_EPS, NULL)) {
-            double le = vdot(ln, vneg(wo)) > 0 ? 1.0 : 0.0;
+            /* OrientedEmitter: the light's normal side only; OmniEmitter: every direction */
+            double le = (L->omni || vdot(ln, vneg(wo)) > 0) ? 1.0 : 0.0;
             for (int k = 0; k < 3; ++k) dir[k] += (fr[k] * L->Le[k] * le * cwo * cwi) / (t * t);
           }
         }
       }
-    for (int k = 0; k < 3; ++k) out[k] += dir[k] * (L->area / c->p.nds);
+    for (int k = 0; k < 3; ++k) out[k] += point ? dir[k] : dir[k] * (L->area / c->p.nds);
   }
 }
 
@@ -1275,7 +1283,7 @@ static void evaluate(const orc_render_ctx *c, orc_path *ph, v3 o, v3 d, int dept
   int li = s->light ? s->light[tri] : -1;
   if (li >= 0) {
     const orc_light *L = &s->lights[li];
-    double le = vdot(ns, vneg(d)) > 0 ? 1.0 : 0.0; /* OrientedEmitter on the hit's normal */
+    double le = (L->omni || vdot(ns, vneg(d)) > 0) ? 1.0 : 0.0; /* OrientedEmitter on the hit's normal */
     if (!c->p.efficient_direct || depth == 0) {
       for (int k = 0; k < 3; ++k) out[k] += L->Le[k] * le;
     } else if (ph->emitted_contribution > ORC_EPS) {

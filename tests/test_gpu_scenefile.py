@@ -1,7 +1,8 @@
 """Milton scene files loaded by milton_gb300.sceneloader render on the GPU like the oracle:
 tests/scenes/box.js (unit-plane light, culled planes, a Phong cube, a dielectric OBJ mesh) and
 tests/scenes/emitters.js (triangle, mesh and plane lights), tests/scenes/spheres.js (analytic
-spheres tessellated by the loader) and tests/scenes/textures.js (image maps)."""
+spheres tessellated by the loader), tests/scenes/textures.js (image maps) and
+tests/scenes/points.js (point lights, omni emitters)."""
 from pathlib import Path
 
 import numpy as np
@@ -14,11 +15,12 @@ pytestmark = pytest.mark.gpu
 HERE = Path(__file__).resolve().parent
 
 
-@pytest.mark.parametrize("name", ["box.js", "emitters.js", "spheres.js", "textures.js"])
+@pytest.mark.parametrize("name", ["box.js", "emitters.js", "spheres.js", "textures.js", "points.js"])
 def test_scene_file_renders_like_the_oracle(cuda, oracle, name):
     # emitters.js: plane, triangle (two uv frames) and mesh lights, 4 light samples per vertex;
     # spheres.js: tessellated spheres (Phong, dielectric, a named sphere and its instance);
-    # textures.js: kd / ks / bump maps from PNG and PPM files, plane, cube and mesh uvs
+    # textures.js: kd / ks / bump maps from PNG and PPM files, plane, cube and mesh uvs;
+    # points.js: omni and oriented point lights, omni plane and mesh emitters
     sf = sceneloader.load(str(HERE / "scenes" / name), tessellate=(32, 17))
     r = sceneloader.path_tracer(sf)
     st = r.settings()

@@ -177,3 +177,29 @@ def test_render_is_thread_count_independent(oracle):
     m1, _, s1 = oracle.render(s, tree, 24, 24, 4, max_depth=5, rr_start=3, threads=1)
     m8, _, s8 = oracle.render(s, tree, 24, 24, 4, max_depth=5, rr_start=3, threads=8)
     assert np.array_equal(m1, m8) and s1 == s8
+
+
+def test_point_light_known_answer(oracle):
+    # an omni point light of power P at height h above a Lambertian floor: the point below it
+    # receives E = (P / 4 pi) / h^2 (DirectIllumination's point branch: one sample, cosine 1 at
+    # the light, no area factor); radiance kd / pi * E
+    kd, P, hgt = 0.6, 10.0, 1.5
+    b = SceneBuilder()
+    fm = b.material(diffuse(kd))
+    h = 50.0
+    b.add("floor", np.array([[[-h, 0, h], [h, 0, h], [h, 0, -h]], [[-h, 0, h], [h, 0, -h], [-h, 0, -h]]],
+                            np.float32), None, fm)
+    rec = np.zeros(16, np.float32)
+    rec[0:3] = (0.0, hgt, 0.0)
+    rec[13:16] = P / (4 * np.pi)
+    ext = np.zeros(16, np.float32)
+    ext[0] = 3
+    b.add_light(rec, ext)
+    cam = camera(eye=(0.0, 0.5, 0.0), look=(0.0, -1.0, 0.0), up=(0, 0, 1), height_angle=0.05, aspect=1.0)
+    s = b.build(cam, name="floor_under_point")
+    tree = oracle.Tree(s.tri_v)
+    mean, _, st = oracle.render(s, tree, 2, 2, 4, max_depth=1, nds=4, seed=3, threads=2)
+    want = kd / np.pi * P / (4 * np.pi) / hgt ** 2
+    assert np.allclose(mean, want, rtol=1e-4), (mean.mean(), want)
+    # one shadow ray per path for the point light, whatever noDirectSamples is
+    assert st["shadow_rays"] == 2 * 2 * 4

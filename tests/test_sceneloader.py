@@ -285,3 +285,23 @@ def test_spheres_tessellate_only_on_request():
     # mesh normals keep the inverse-transpose length (normalised per hit after interpolation)
     n = s.tri_n.reshape(-1, 3).astype(np.float64)
     assert np.allclose(n / np.linalg.norm(n, axis=1, keepdims=True), (v - [2, 1, 0]) / 0.75, atol=1e-5)
+
+
+def test_point_lights_and_omni_emitters():
+    text = _scene('"material" : { "emitter" : { "type" : "omni", "power" : [4, 8, 12] }, '
+                  '"transform" : { "translate" : [1, 2, 3], "point" : { } } }, '
+                  '"material" : { "emitter" : { "type" : "oriented", "power" : 2 }, "point" : { } }, '
+                  '"material" : { "emitter" : { "type" : "omni", "power" : 1 }, '
+                  '"transform" : { "scale" : [2, 1, 2], "plane" : { } } }, '
+                  '"point" : { }')
+    s = L.loads(text).scene
+    # materials in file order: the two points, then the plane; the bare point is no light
+    assert len(s.lights) == 3 and s.ntri == 2
+    assert s.light_ext[2, 0] == 0 and s.light_ext[2, 15] == 1  # omni plane: area 4
+    assert np.allclose(s.lights[2, 13:16], 1 / (4 * 4 * math.pi))
+    p1, p2 = s.lights[0], s.lights[1]
+    assert s.light_ext[0, 0] == 3 and s.light_ext[1, 0] == 3
+    # an omni point: power / 4 pi; an oriented point: power / pi (its stand-in normal dot is 1)
+    assert np.allclose(p1[0:3], (1, 2, 3)) and np.allclose(p1[13:16], np.array([4, 8, 12]) / (4 * math.pi))
+    assert np.allclose(p2[0:3], 0) and np.allclose(p2[13:16], 2 / math.pi)
+    assert np.all(s.tri_light == 2)
