@@ -219,3 +219,27 @@ def test_reconstruction_filters(cuda, kind, support, params):
                                     wave_paths=64), f2)
     pt.render(ds, pt.RenderSettings(W, H, spp, sample_begin=1, max_depth=5, rr_start_depth=3, seed=3), f2)
     assert np.array_equal(f2.mean(), got)
+
+
+def test_point_light_known_answer(cuda):
+    # an omni point light of power P at height h above a Lambertian floor: radiance at the
+    # point below it is kd / pi * (P / 4 pi) / h^2, one shadow ray per path
+    from milton_gb300.scene import SceneBuilder, camera, diffuse
+    kd, P, hgt = 0.6, 10.0, 1.5
+    b = SceneBuilder()
+    fm = b.material(diffuse(kd))
+    h = 50.0
+    b.add("floor", np.array([[[-h, 0, h], [h, 0, h], [h, 0, -h]], [[-h, 0, h], [h, 0, -h], [-h, 0, -h]]],
+                            np.float32), None, fm)
+    rec = np.zeros(16, np.float32)
+    rec[0:3] = (0.0, hgt, 0.0)
+    rec[13:16] = P / (4 * np.pi)
+    ext = np.zeros(16, np.float32)
+    ext[0] = 3
+    b.add_light(rec, ext)
+    s = b.build(camera(eye=(0.0, 0.5, 0.0), look=(0.0, -1.0, 0.0), up=(0, 0, 1), height_angle=0.05, aspect=1.0))
+    st = pt.RenderSettings(4, 4, 16, no_direct_samples=4, max_depth=1, seed=2)
+    mean, paths, _ = gpu_render_paths(cuda, s, st)
+    want = kd / np.pi * P / (4 * np.pi) / hgt ** 2
+    assert np.allclose(mean, want, rtol=1e-4), (mean.mean(), want)
+    assert pt.render_stats()["shadow_rays"] == 4 * 4 * 16
