@@ -94,6 +94,23 @@ MGPU_HD RayPre precompute(const Ray &r) {
   return p;
 }
 
+// Rounded product / difference that the device compiler may not fuse (host code is built with
+// -ffp-contract=off).
+MGPU_HD float mul_nc(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+MGPU_HD float sub_nc(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+
 // Tests one triangle.  On a hit with tmin < t < tbest returns true and fills t, b1, b2.
 // culled: accept only rays arriving on the side that (v1-v0) x (v2-v0) faces, like Milton's
 // back-face culled `Triangle` (det = e1 . (d x e2) > 0 in Triangle.cpp:245-248).
@@ -104,9 +121,12 @@ MGPU_HD bool intersect_tri(const RayPre &p, V3 v0, V3 v1, V3 v2, bool culled, fl
   float Ax = comp(A, p.kx) - p.sx * Akz, Ay = comp(A, p.ky) - p.sy * Akz;
   float Bx = comp(B, p.kx) - p.sx * Bkz, By = comp(B, p.ky) - p.sy * Bkz;
   float Cx = comp(C, p.kx) - p.sx * Ckz, Cy = comp(C, p.ky) - p.sy * Ckz;
-  float U = Cx * By - Cy * Bx;
-  float Vv = Ax * Cy - Ay * Cx;
-  float W = Bx * Ay - By * Ax;
+  // The edge functions must round the same way in the two triangles that share an edge (there
+  // they are exact negatives): products and difference without contraction into an FMA, which
+  // rounds a * b - c * d and d * c - b * a differently and lets rays through shared edges.
+  float U = sub_nc(mul_nc(Cx, By), mul_nc(Cy, Bx));
+  float Vv = sub_nc(mul_nc(Ax, Cy), mul_nc(Ay, Cx));
+  float W = sub_nc(mul_nc(Bx, Ay), mul_nc(By, Ax));
   if (U == 0.0f || Vv == 0.0f || W == 0.0f) {
     // edge case: redo the 2D cross products in double so that shared edges stay watertight
     U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);

@@ -103,3 +103,43 @@ def test_edge_cases(cuda, oracle, plain_dev):
     assert oracle.trace_closest(None, s.tri_v, s.tri_flags, r3)[0][0] > 0.25
     # empty batch is a no-op
     assert pt.trace_closest(ds, cuda.zeros((0, 8), dtype=cuda.float32, device="cuda")).shape == (0, 4)
+
+
+def _scene_of(tris):
+    from milton_gb300.scene import SceneBuilder, camera, diffuse
+    b = SceneBuilder()
+    b.add("t", np.asarray(tris, np.float32), None, b.material(diffuse(0.5)))
+    return b.build(camera(eye=(0, 1, 0), look=(0, -1, 0), up=(0, 0, 1), height_angle=40.0, aspect=1.0))
+
+
+def test_shared_edges_and_vertices_are_watertight(cuda):
+    # rays aimed at points of a shared edge (a large quad split on its diagonal) and at the
+    # shared vertex of a triangle fan must hit one of the triangles: the edge functions are
+    # rounded alike in both triangles (an FMA-contracted edge function let rays through)
+    rng = np.random.default_rng(17)
+    h = 50.0
+    quad = [[[-h, 0, h], [h, 0, h], [h, 0, -h]], [[-h, 0, h], [h, 0, -h], [-h, 0, -h]]]
+    ang = np.linspace(0, 2 * np.pi, 13)[:-1]
+    ring = np.stack([np.cos(ang), 0.3 * np.sin(3 * ang), np.sin(ang)], -1) * 7.0
+    c = np.array([0.31, 0.17, -0.23])
+    fan = [[c, ring[i], ring[(i + 1) % 12]] for i in range(12)]
+    for tris, targets in ((quad, None), (fan, None)):
+        sc = _scene_of(tris)
+        ds = pt.DeviceScene(sc, pt.Accel(sc))
+        n = 1 << 18
+        if tris is quad:
+            s = rng.uniform(-0.999, 0.999, n)
+            tgt = np.stack([-h * s, np.zeros(n), h * s], -1)  # on the diagonal from (-h, 0, h) to (h, 0, -h)
+        else:
+            k = rng.integers(0, 12, n)
+            s = rng.uniform(0.0, 1.0, n)
+            tgt = c + (ring[k] - c) * s[:, None]  # on the spokes, and the centre vertex itself
+            tgt[: n // 8] = c
+        org = tgt + rng.normal(size=(n, 3)) * [3.0, 0.0, 3.0] + np.array([0.0, 0.0, 0.0])
+        org[:, 1] = tgt[:, 1] + rng.uniform(0.5, 20.0, n)
+        d = tgt - org
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        rays = np.concatenate([org, np.zeros((n, 1)), d, np.full((n, 1), np.inf)], 1).astype(np.float32)
+        hits, _ = gpu_trace(cuda, ds, rays)
+        prims = np.ascontiguousarray(hits[:, 1]).view(np.int32)
+        assert (prims < 0).sum() == 0, f"{(prims < 0).sum()} of {n} rays leaked"
