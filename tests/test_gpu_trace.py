@@ -114,14 +114,16 @@ def _scene_of(tris):
 
 def test_shared_edges_and_vertices_are_watertight(cuda):
     # rays aimed at points of a shared edge (a large quad split on its diagonal) and at the
-    # shared vertex of a triangle fan must hit one of the triangles: the edge functions are
-    # rounded alike in both triangles (an FMA-contracted edge function let rays through)
+    # shared vertex and spokes of a planar triangle fan must hit one of the triangles: the edge
+    # functions are rounded alike in both triangles (an FMA-contracted edge function let rays
+    # through).  The fan is planar: around the vertex of a folded fan a grazing ray can pass
+    # legitimately (the FP64 oracle misses those too).
     rng = np.random.default_rng(17)
     h = 50.0
     quad = [[[-h, 0, h], [h, 0, h], [h, 0, -h]], [[-h, 0, h], [h, 0, -h], [-h, 0, -h]]]
-    ang = np.linspace(0, 2 * np.pi, 13)[:-1]
-    ring = np.stack([np.cos(ang), 0.3 * np.sin(3 * ang), np.sin(ang)], -1) * 7.0
+    ang = np.linspace(0, 2 * np.pi, 13)[:-1] + 0.1
     c = np.array([0.31, 0.17, -0.23])
+    ring = c + np.stack([np.cos(ang) * 7.0, np.zeros(12), np.sin(ang) * 5.0], -1)
     fan = [[c, ring[i], ring[(i + 1) % 12]] for i in range(12)]
     for tris, targets in ((quad, None), (fan, None)):
         sc = _scene_of(tris)
@@ -132,7 +134,7 @@ def test_shared_edges_and_vertices_are_watertight(cuda):
             tgt = np.stack([-h * s, np.zeros(n), h * s], -1)  # on the diagonal from (-h, 0, h) to (h, 0, -h)
         else:
             k = rng.integers(0, 12, n)
-            s = rng.uniform(0.0, 1.0, n)
+            s = rng.uniform(0.0, 0.999, n)
             tgt = c + (ring[k] - c) * s[:, None]  # on the spokes, and the centre vertex itself
             tgt[: n // 8] = c
         org = tgt + rng.normal(size=(n, 3)) * [3.0, 0.0, 3.0] + np.array([0.0, 0.0, 0.0])
