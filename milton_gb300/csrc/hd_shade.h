@@ -22,13 +22,15 @@ struct Material {
   int tex_kd, tex_ks, tex_tr, tex_bump;  // 1 + texture index, 0 = none
 };
 
-MGPU_HD Material material_from(const float *m) {
+// ior_index: the path's colour channel (0..2).  A dielectric refracts with that channel's IOR
+// (DielectricBSDF.cpp:79-87): record [8] (all channels when [14] = [15] = 0), [14], [15].
+MGPU_HD Material material_from(const float *m, uint32_t ior_index = 0) {
   Material r;
   r.type = (int)m[0];
   r.kd = v3(m[1], m[2], m[3]);
   r.ks = v3(m[4], m[5], m[6]);
   r.n = m[7];
-  r.ior = m[8];
+  r.ior = (ior_index == 0 || (m[14] == 0.0f && m[15] == 0.0f)) ? m[8] : (ior_index == 1 ? m[14] : m[15]);
   r.transparency = m[9];
   r.kda = (r.kd.x + r.kd.y + r.kd.z) / 3.0f;
   r.ksa = (r.ks.x + r.ks.y + r.ks.z) / 3.0f;

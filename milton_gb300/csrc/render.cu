@@ -152,12 +152,12 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool want) {
   return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
-__device__ __forceinline__ Material load_mat(const JobArgs &J, int i) {
+__device__ __forceinline__ Material load_mat(const JobArgs &J, int i, uint32_t ior_index) {
   float m[16];
   float4 *mm = reinterpret_cast<float4 *>(m);
 #pragma unroll
   for (int k = 0; k < 4; ++k) mm[k] = __ldg(J.mats + 4 * i + k);
-  return material_from(m);
+  return material_from(m, ior_index);
 }
 
 // Image maps at a hit of triangle prim with barycentrics (b0, b1, b2): the uv (Shape::_getUV,
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         ng = normalize(cross(v1 - v0, v2 - v0));
         int mi = __float_as_int(s0.w);
         self = __float_as_int(s1.w);
-        m = load_mat(J, mi);
+        m = load_mat(J, mi, flags & kFlagIorMask);
         if (SURF && (m.tex_kd | m.tex_ks | m.tex_tr | m.tex_bump) != 0) apply_textures(J, prim, b0, b1, b2, m, ns);
         bool spec = is_specular(m);
         if (spec) flags |= kFlagSpecular;

@@ -9,7 +9,8 @@ A `Scene` holds exactly what crosses the C ABI (``mgpu_scene_desc``):
 * ``tri_flags`` (T,)      uint32   bit 0: back-face culled (Milton ``Triangle``,
                                    mlt/src/milton/shapes/Triangle.cpp:245-272); else two-sided
                                    (``MeshTriangle``, MeshTriangle.cpp:142-167)
-* ``materials`` (M, 16)   float32  type, kd[3], ks[3], n, ior, transparency, 0...
+* ``materials`` (M, 16)   float32  type, kd[3], ks[3], n, ior, transparency, texture slots [10..13],
+                                   per-channel IOR [14], [15] (0, 0 = [8] for every channel)
 * ``lights``    (L, 16)   float32  center[3], ex[3], ez[3], normal[3], area, Le[3]
 * ``light_ext`` (L, 16)   float32  type (0 plane, 1 Triangle, 2 Mesh) and its parameters
                                    (include/mgpu.h); all zeros = planes
@@ -68,13 +69,22 @@ def phong(kd, ks, n) -> np.ndarray:
 
 
 def dielectric(ior=1.5, transparency=1.0, ks=1.0) -> np.ndarray:
+    """ior: one value, or three (per colour channel: a path refracts with its channel's, which
+    disperses light as Milton's spectral IOR does)."""
     m = np.zeros(16, np.float32)
     m[0] = MAT_DIELECTRIC
     m[4:7] = np.broadcast_to(np.asarray(ks, np.float32), 3)
     m[7] = 1.0
-    m[8] = ior
+    set_ior(m, ior)
     m[9] = transparency
     return m
+
+
+def set_ior(rec: np.ndarray, ior) -> None:
+    """Material record IOR: [8] for every channel, or [8], [14], [15] per channel."""
+    a = np.broadcast_to(np.asarray(ior, np.float32), 3)
+    rec[8] = a[0]
+    rec[14], rec[15] = (0.0, 0.0) if a[0] == a[1] == a[2] else (a[1], a[2])
 
 
 def quad_light(center, ex, ez, radiance) -> np.ndarray:

@@ -33,7 +33,8 @@ Emitters: a unit plane becomes a parallelogram light, a Triangle a triangle ligh
 frame and object-space area, a mesh one mesh light over its triangles (include/mgpu.h,
 ``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
 element: analytic shapes other than planes, cubes and points (sphere, cylinder, cone, blob),
-emitting cubes, oriented backgrounds, bump-mapped emitters, per-channel IOR or Phong exponents.
+emitting cubes, oriented backgrounds, bump-mapped emitters, per-channel Phong exponents.  A
+per-channel IOR disperses: a path refracts with its colour channel's IOR.
 Emitters are oriented (one-sided, power / (area pi)) or omni (both sides, power / (area 4 pi))
 on planes, triangles and meshes, and point lights (a "point" shape with either emitter: one
 light sample, no area).  A scene's background is taken: an environment map
@@ -1375,7 +1376,10 @@ def material_record(props: dict) -> np.ndarray:
             raise SceneFileError(f"per-channel '{key}' {tuple(a)} is not supported by the GPU path")
         return float(a[0])
 
-    ior = scalar("ior", S.AIR_IOR)
+    ior_v = props.get("ior", S.AIR_IOR)
+    if isinstance(ior_v, str):
+        raise SceneFileError(f"'ior' = '{ior_v}' is not supported by the GPU path")
+    ior = np.broadcast_to(np.asarray(ior_v, np.float64), 3)  # per channel: dispersion
     if kind == "diffuse":
         rec = S.diffuse(spec("kd", 0.5))
     elif kind == "absorbent":
@@ -1394,7 +1398,7 @@ def material_record(props: dict) -> np.ndarray:
         rec = S.dielectric(ior=ior, transparency=scalar("transparency", 1.0), ks=spec("ks", 1.0))
     else:
         raise SceneFileError(f"invalid material (BSDF type): {kind}")
-    rec[8] = ior
+    S.set_ior(rec, ior)
     return rec
 
 

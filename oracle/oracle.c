@@ -146,6 +146,7 @@ enum { MAT_DIFFUSE = 0, MAT_PHONG = 1, MAT_DIELECTRIC = 2 };
 typedef struct {
   int type;
   double kd[3], ks[3], n, ior, transparency;
+  double ior3[3]; /* per-channel IOR (the "ior" spectrum); a path refracts with its channel's */
   int tex[4]; /* 1 + texture index for kd, ks, transparency, bump map; 0 = none */
 } orc_mat;
 
@@ -707,6 +708,15 @@ static orc_tex *textures_from(int ntex, const float *params, const float *const 
   return t;
 }
 
+/* material record [8] = IOR of channel 0 (all channels when [14] = [15] = 0), [14], [15] = the
+ * IOR of channels 1 and 2 */
+static void mat_ior3(orc_mat *m, const float *rec) {
+  const int per = rec[14] != 0.0f || rec[15] != 0.0f;
+  m->ior3[0] = rec[8];
+  m->ior3[1] = per ? rec[14] : rec[8];
+  m->ior3[2] = per ? rec[15] : rec[8];
+}
+
 static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n, const int32_t *mat,
                                     const int32_t *light, const uint32_t *flags, int nmat, const float *mats,
                                     int nlight, const float *lights, const float *light_ext) {
@@ -720,6 +730,7 @@ static orc_scene *scene_from_arrays(int64_t ntri, const float *v, const float *n
     for (int k = 0; k < 3; ++k) { s->mats[i].kd[k] = m[1 + k]; s->mats[i].ks[k] = m[4 + k]; }
     s->mats[i].n = m[7];
     s->mats[i].ior = m[8];
+    mat_ior3(&s->mats[i], m);
     s->mats[i].transparency = m[9];
     for (int k = 0; k < 4; ++k) s->mats[i].tex[k] = (int)m[10 + k];
   }
@@ -1024,7 +1035,7 @@ static int bsdf_sample(const orc_bsdf *b, const double u[3], v3 *wo, double fs[3
   /* dielectric, :56-157 with the caller-set ior index and pdf/eval by lobe */
   v3 N = vdot(b->ns, b->wi) > 0 ? vneg(b->ns) : b->ns;
   unsigned idx = b->ior_index > 0 ? b->ior_index - 1 : 0;
-  double ior = m->ior;
+  double ior = m->ior3[idx]; /* m_ior[index] (DielectricBSDF.cpp:79-87) */
   int ok;
   v3 wt = refract_v(b->wi, b->ns, ORC_AIR, ior, &ok);
   if (ok) {
@@ -1473,6 +1484,7 @@ int orc_bsdf_sample(const float *mat16, const double *ns, const double *wi, int 
   m.type = (int)mat16[0];
   for (int k = 0; k < 3; ++k) { m.kd[k] = mat16[1 + k]; m.ks[k] = mat16[4 + k]; }
   m.n = mat16[7]; m.ior = mat16[8]; m.transparency = mat16[9];
+  mat_ior3(&m, mat16);
   orc_bsdf b = {&m, V(ns[0], ns[1], ns[2]), V(wi[0], wi[1], wi[2]), (unsigned)ior_index + 1};
   v3 wo = V(0, 0, 0);
   double fs[3] = {0, 0, 0};
@@ -1488,6 +1500,7 @@ void orc_bsdf_eval(const float *mat16, const double *ns, const double *wi, const
   m.type = (int)mat16[0];
   for (int k = 0; k < 3; ++k) { m.kd[k] = mat16[1 + k]; m.ks[k] = mat16[4 + k]; }
   m.n = mat16[7]; m.ior = mat16[8]; m.transparency = mat16[9];
+  mat_ior3(&m, mat16);
   orc_bsdf b = {&m, V(ns[0], ns[1], ns[2]), V(wi[0], wi[1], wi[2]), 1};
   bsdf_eval(&b, V(wo[0], wo[1], wo[2]), f_out);
 }

@@ -81,7 +81,7 @@ int hc_trace_kd(const float *v, const uint32_t *flags, int64_t ntri, const float
 
 int hc_bsdf_sample(const float *mat16, const float *ns, const float *wi, int ior_index, const float *u, float *wo_out,
                    float *fs_out) {
-  Material m = material_from(mat16);
+  Material m = material_from(mat16, (uint32_t)ior_index);
   V3 wo = v3(0, 0, 0), fs;
   int ev = bsdf_sample(m, v3(ns[0], ns[1], ns[2]), v3(wi[0], wi[1], wi[2]), (uint32_t)ior_index, u[0], u[1], u[2], wo, fs);
   wo_out[0] = wo.x; wo_out[1] = wo.y; wo_out[2] = wo.z;

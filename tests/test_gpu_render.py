@@ -243,3 +243,19 @@ def test_point_light_known_answer(cuda):
     want = kd / np.pi * P / (4 * np.pi) / hgt ** 2
     assert np.allclose(mean, want, rtol=1e-4), (mean.mean(), want)
     assert pt.render_stats()["shadow_rays"] == 4 * 4 * 16
+
+
+def test_dispersive_dielectric_per_path(cuda, oracle):
+    # a per-channel IOR: every path refracts with its colour channel's index
+    from milton_gb300.scene import dielectric
+    s = scenegen.plain(1)
+    for name, first, count in s.shapes:
+        if name in ("tallBox", "shortBox"):
+            s.materials[s.tri_mat[first]] = dielectric([1.4, 1.55, 1.8], transparency=0.9)
+    st = pt.RenderSettings(48, 48, 16, max_depth=6, rr_start_depth=3, seed=8)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st)
+    mean_o, paths_o, _ = oracle.render(s, oracle.Tree(s.tri_v), 48, 48, 16, max_depth=6, rr_start=3, seed=8,
+                                       per_path=True)
+    agree = _path_agreement(paths_g, paths_o)
+    print(f"dispersive: path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
+    assert agree >= 0.97

@@ -77,7 +77,9 @@ def test_uniforms_match_oracle(oracle, hostcheck):
 
 
 @pytest.mark.parametrize("mat", [diffuse([0.6, 0.5, 0.4]), phong([0.3, 0.2, 0.25], [0.5, 0.6, 0.4], 80.0),
-                                 phong([0.05, 0.05, 0.05], [0.9, 0.9, 0.9], 200.0), dielectric(1.5)])
+                                 phong([0.05, 0.05, 0.05], [0.9, 0.9, 0.9], 200.0), dielectric(1.5),
+                                 dielectric([1.45, 1.6, 1.9], transparency=0.8)],
+                         ids=["diffuse", "phong", "phong-sharp", "dielectric", "dielectric-dispersive"])
 def test_fp32_bsdf_matches_fp64(oracle, hostcheck, mat):
     rng = np.random.default_rng(2)
     agree = 0
@@ -174,3 +176,28 @@ def test_thin_lens_camera_rays(hostcheck, oracle):
         t = (-2.0 - o[2]) / d[2]
         pts.append(o + t * d)
     assert np.ptp(np.array(pts), axis=0).max() < 1e-9
+
+
+def test_dispersion_refracts_each_channel_with_its_ior(oracle, hostcheck):
+    # a path refracts with its colour channel's IOR (DielectricBSDF.cpp:79-87): the refracted
+    # directions of channels 0, 1, 2 bend by their own indices (Snell's law)
+    mat = dielectric([1.3, 1.6, 2.2], transparency=1.0)
+    ns = np.array([0.0, 1.0, 0.0], np.float32)
+    wi = np.array([0.6, -0.8, 0.0], np.float32)
+    sin_i = 0.6
+    for ch, ior in enumerate((1.3, 1.6, 2.2)):
+        for u0 in np.linspace(0.001, 0.5, 20):  # small u: the refraction lobe (probability T (1 - Fr))
+            u = np.array([u0, 0.5, 0.5], np.float32)
+            ev, wo, fs = oracle.bsdf_sample(mat, ns, wi, ch, u)
+            if ev != 4:
+                continue
+            sin_t = np.hypot(wo[0], wo[2])
+            assert abs(sin_t - 1.0003 * sin_i / ior) < 1e-6  # float32 inputs
+            wo32 = np.zeros(3, np.float32)
+            fs32 = np.zeros(3, np.float32)
+            ev32 = hostcheck.hc_bsdf_sample(mat.ctypes.data, ns.ctypes.data, wi.ctypes.data, ch, u.ctypes.data,
+                                            wo32.ctypes.data, fs32.ctypes.data)
+            assert ev32 == 4 and np.allclose(wo32, wo, atol=1e-5)
+            break
+        else:
+            raise AssertionError("no refraction sampled")

@@ -305,3 +305,11 @@ def test_point_lights_and_omni_emitters():
     assert np.allclose(p1[0:3], (1, 2, 3)) and np.allclose(p1[13:16], np.array([4, 8, 12]) / (4 * math.pi))
     assert np.allclose(p2[0:3], 0) and np.allclose(p2[13:16], 2 / math.pi)
     assert np.all(s.tri_light == 2)
+
+
+def test_per_channel_ior_is_dispersion():
+    s = L.loads(_scene('"material" : { "bsdf" : { "type" : "dielectric", "ior" : [1.4, 1.5, 1.6] }, "triangle" : { } }, '
+                       '"material" : { "bsdf" : { "type" : "dielectric", "ior" : 1.5 }, "triangle" : { } }')).scene
+    d, g = s.materials[s.tri_mat[0]], s.materials[s.tri_mat[1]]
+    assert np.allclose([d[8], d[14], d[15]], [1.4, 1.5, 1.6])
+    assert g[8] == np.float32(1.5) and g[14] == 0 and g[15] == 0
