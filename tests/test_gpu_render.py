@@ -259,3 +259,39 @@ def test_dispersive_dielectric_per_path(cuda, oracle):
     agree = _path_agreement(paths_g, paths_o)
     print(f"dispersive: path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
     assert agree >= 0.97
+
+
+@pytest.mark.parametrize("w,h,spp,nds", [(1, 1, 1, 1), (13, 7, 7, 3), (9, 17, 2, 2)])
+def test_ragged_sizes_and_non_square_sample_counts(cuda, oracle, w, h, spp, nds):
+    # image sides that are not multiples of the 8 x 8 slot tiles, sample counts that are not
+    # squares (strata of side floor(sqrt(spp)) reused), several light samples
+    s = scenegen.plain(3)
+    st = pt.RenderSettings(w, h, spp, no_direct_samples=nds, max_depth=5, rr_start_depth=3, seed=21)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st)
+    mean_o, paths_o, _ = oracle.render(s, oracle.Tree(s.tri_v), w, h, spp, nds=nds, max_depth=5, rr_start=3, seed=21,
+                                       per_path=True)
+    assert paths_g.shape == paths_o.shape == (h, w, spp, 3)
+    assert _path_agreement(paths_g, paths_o) >= (0.97 if w * h * spp > 50 else 1.0)
+
+
+def test_scenes_without_geometry_or_lights(cuda):
+    from milton_gb300.scene import SceneBuilder, camera, diffuse, quad_light
+    cam = camera(eye=(0, 0, 3), look=(0, 0, -1), up=(0, 1, 0), height_angle=40.0, aspect=1.0)
+    # a light record but no triangles: every ray misses, the film is black (no background)
+    b = SceneBuilder()
+    b.material(diffuse(0.5))
+    b.add_light(quad_light((0, 1, 0), (1, 0, 0), (0, 0, 1), 5.0))
+    empty = b.build(cam)
+    assert empty.ntri == 0
+    mean, paths, _ = gpu_render_paths(cuda, empty, pt.RenderSettings(8, 8, 4, max_depth=3, seed=1))
+    assert np.all(mean == 0) and np.all(paths == 0)
+    # with a constant background the misses see it
+    empty.background_le = np.array([0.25, 0.5, 1.0], np.float32)
+    mean, _, _ = gpu_render_paths(cuda, empty, pt.RenderSettings(8, 8, 4, max_depth=3, seed=1))
+    assert np.allclose(mean, [0.25, 0.5, 1.0])
+    # geometry without lights: black
+    s = scenegen.plain(0)
+    dark = type(s)(tri_v=s.tri_v, tri_n=s.tri_n, tri_mat=s.tri_mat, tri_light=np.full(s.ntri, -1, np.int32),
+                   tri_flags=s.tri_flags, materials=s.materials, lights=np.zeros((0, 16), np.float32), camera=s.camera)
+    mean, _, _ = gpu_render_paths(cuda, dark, pt.RenderSettings(16, 16, 4, max_depth=5, rr_start_depth=3, seed=1))
+    assert np.all(mean == 0)
