@@ -17,8 +17,9 @@
  *      ticks.
  *   2. Rendering: active jobs get sample passes up to the tick's path budget -- under the fair
  *      policy first one sample each, least recently served first, then the rest of the budget
- *      oldest job first; under the oldest-first policy only the latter -- never past a job's
- *      next checkpoint -- and the passes of all jobs render together in one
+ *      oldest job first; under the oldest-first policy only the latter; under the rotating
+ *      policy whole passes (up to the next checkpoint) to the least recently served jobs first
+ *      -- never past a job's next checkpoint -- and the passes of all jobs render together in one
  *      batch (mgpu_batch_*: jobs of different scenes share waves; passes are grouped by
  *      scene so that a wave touches few trees).
  *   3. Checkpoints: a job's checkpoints are its sample counts c0 = min(spp, max_spp),
@@ -58,11 +59,14 @@ typedef struct {
   mgpu_kd_params kd;     /* kd-tree parameters for every scene (threads 0 = all cores) */
   int32_t policy;        /* MGPU_SERVE_FAIR (0): one sample per active job first, least recently
                             served first, then the rest oldest first; MGPU_SERVE_OLDEST (1): the
-                            whole tick oldest job first (fewer jobs and scenes per wave) */
+                            whole tick oldest job first (fewer jobs and scenes per wave);
+                            MGPU_SERVE_ROTATE (2): whole passes, least recently served job first
+                            (fewer, larger passes per tick: more samples of a pixel in a wave) */
 } mgpu_server_params;
 
 #define MGPU_SERVE_FAIR 0
 #define MGPU_SERVE_OLDEST 1
+#define MGPU_SERVE_ROTATE 2
 
 #define MGPU_JOB_QUEUED 0
 #define MGPU_JOB_ACTIVE 1

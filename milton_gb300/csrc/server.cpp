@@ -304,8 +304,24 @@ void plan(mgpu_server *s, std::vector<Pass> &out) {
       }
     }
   } else if (!act.empty()) {
-    k[0] = 1;  // the oldest job always advances, even when one sample exceeds the tick
-    left -= (int64_t)act[0]->pixels();
+    // the oldest (or least recently served) job always advances, even when one sample exceeds
+    // the tick
+    const size_t first = s->p.policy == MGPU_SERVE_ROTATE ? order[0] : 0;
+    k[first] = 1;
+    left -= (int64_t)act[first]->pixels();
+  }
+  if (s->p.policy == MGPU_SERVE_ROTATE) {
+    // whole passes in least-recently-served order
+    for (size_t i : order) {
+      if (left <= 0) break;
+      const int64_t px = (int64_t)act[i]->pixels();
+      const int64_t room = act[i]->next_ckpt - act[i]->spp_done - k[i];
+      const int64_t more = std::min<int64_t>(room, left / px);
+      if (more > 0) {
+        k[i] += (int32_t)more;
+        left -= more * px;
+      }
+    }
   }
   for (size_t i = 0; i < act.size() && left > 0; ++i) {
     const int64_t px = (int64_t)act[i]->pixels();
@@ -330,7 +346,7 @@ int mgpu_server_create(const mgpu_server_params *params, mgpu_server **out) {
   if (!params || !out) return fail(MGPU_E_INVALID, "mgpu_server_create: null argument");
   if (params->tick_paths < 0 || params->max_active < 0 || params->wave_paths < 0 || params->build_threads < 0)
     return fail(MGPU_E_INVALID, "mgpu_server_create: negative parameter");
-  if (params->policy != MGPU_SERVE_FAIR && params->policy != MGPU_SERVE_OLDEST)
+  if (params->policy != MGPU_SERVE_FAIR && params->policy != MGPU_SERVE_OLDEST && params->policy != MGPU_SERVE_ROTATE)
     return fail(MGPU_E_INVALID, "mgpu_server_create: unknown policy");
   mgpu_server *s = new (std::nothrow) mgpu_server();
   if (!s) return fail(MGPU_E_NOMEM, "mgpu_server_create: out of host memory");

@@ -35,16 +35,17 @@ class ServerSettings:
     use_graph: int = 0
     build_threads: int = 2
     kd: KdSettings = field(default_factory=KdSettings)
-    policy: str = "fair"  # "fair" or "oldest" (include/mgpu_server.h)
+    policy: str = "fair"  # "fair", "oldest" or "rotate" (include/mgpu_server.h)
 
     def to_c(self) -> N.ServerParams:
         p = N.ServerParams()
         p.hbm_budget, p.tick_paths, p.max_active = self.hbm_budget, self.tick_paths, self.max_active
         p.wave_paths, p.use_graph, p.build_threads = self.wave_paths, self.use_graph, self.build_threads
         p.kd = self.kd.to_c()
-        if self.policy not in ("fair", "oldest"):
+        policies = {"fair": 0, "oldest": 1, "rotate": 2}
+        if self.policy not in policies:
             raise ValueError(f"unknown serving policy {self.policy!r}")
-        p.policy = 0 if self.policy == "fair" else 1
+        p.policy = policies[self.policy]
         return p
 
 

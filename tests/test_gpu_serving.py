@@ -51,7 +51,7 @@ def _run(scenes, jobs, settings=None, keys=None):
         return [res[j] for j in jids], srv.stats(), peak
 
 
-@pytest.mark.parametrize("policy", ["fair", "oldest"])
+@pytest.mark.parametrize("policy", ["fair", "oldest", "rotate"])
 def test_same_image_alone_and_in_the_mix(cuda, policy):
     scenes = _scenes()
     mix, st, _ = _run(scenes, JOBS, ServerSettings(tick_paths=20000, policy=policy))
