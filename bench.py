@@ -620,7 +620,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--tick-paths", type=int, default=1 << 26, help="serving: paths per scheduling tick")
     ap.add_argument("--graph", type=int, default=0, help="serving: capture each tick in a CUDA graph")
-    ap.add_argument("--policy", default="fair", choices=["fair", "oldest", "rotate"], help="serving: tick scheduling policy")
+    ap.add_argument("--policy", default="rotate", choices=["fair", "oldest", "rotate"],
+                    help="serving: tick scheduling policy")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)

@@ -35,7 +35,7 @@ class ServerSettings:
     use_graph: int = 0
     build_threads: int = 2
     kd: KdSettings = field(default_factory=KdSettings)
-    policy: str = "fair"  # "fair", "oldest" or "rotate" (include/mgpu_server.h)
+    policy: str = "rotate"  # "rotate" (default), "fair" or "oldest" (include/mgpu_server.h)
 
     def to_c(self) -> N.ServerParams:
         p = N.ServerParams()
