@@ -108,7 +108,13 @@ typedef struct {
  *              background_tex = 1 + index of a colour map read as Milton's latitude-longitude
  *              EnvironmentMap (EnvironmentMap.cpp:40-96: the map's texel at the uv of -d), or 0
  *              for the constant background_le (an omni background: power / 4 pi; zeros = the
- *              default black background)                                                   */
+ *              default black background)
+ *   spheres    nsphere (at most MGPU_MAX_SPHERES) analytic Milton `Sphere`s beside the triangle
+ *              soup, 8 floats each: center[3], radius, then the unit quaternion (x, y, z, w) that
+ *              rotates world directions into the sphere's object frame (for its uvs); primitive
+ *              id ntri + index, material sphere_mat[index]; they do not emit.  Every ray tests
+ *              every sphere (Sphere::getIntersection, Sphere.cpp:17-48), so a scene of many
+ *              spheres is better tessellated.                                               */
 typedef struct mgpu_texture mgpu_texture;
 typedef struct {
   int64_t ntri;
@@ -127,6 +133,9 @@ typedef struct {
   const mgpu_texture *textures;
   int32_t background_tex;
   float background_le[3];
+  int32_t nsphere;
+  const float *spheres;
+  const int32_t *sphere_mat;
 } mgpu_scene_desc;
 
 /* A material's image map (Material::getSample, Material.cpp:285-301, and the bump map of
@@ -156,6 +165,8 @@ struct mgpu_texture {
 
 #define MGPU_TEX_COLOR 0
 #define MGPU_TEX_BUMP 1
+
+#define MGPU_MAX_SPHERES 256
 
 #define MGPU_LIGHT_PLANE 0
 #define MGPU_LIGHT_TRIANGLE 1

@@ -84,23 +84,26 @@ static void register_staging(mgpu_accel *a) {
 
 // Offsets of the arrays in a scene's one device allocation (256-byte aligned each).
 struct SceneLayout {
-  size_t off_pairs, off_refs, off_tris, off_shade, off_mats, off_lights, off_uv, off_texrec, off_texels, off_err,
-      total;
+  size_t off_pairs, off_refs, off_tris, off_shade, off_mats, off_lights, off_uv, off_texrec, off_texels, off_sph,
+      off_err, total;
 };
-// uv_tris: triangles with uploaded uvs (0 or all); ntex textures holding texels texels in all
+// uv_tris: triangles with uploaded uvs (0 or all); ntex textures holding texels texels in all;
+// nsph analytic spheres (2 float4 each, and 3 shading records after the triangles')
 static SceneLayout scene_layout(const mgpu_accel *a, int32_t nmat, int32_t nlight, int64_t uv_tris = 0,
-                                int32_t ntex = 0, uint64_t texels = 0) {
+                                int32_t ntex = 0, uint64_t texels = 0, int32_t nsph = 0) {
   SceneLayout L;
   L.off_pairs = 0;
   L.off_refs = align_up(L.off_pairs + a->dpairs.size() * sizeof(Pair), 256);
   L.off_tris = align_up(L.off_refs + std::max<size_t>(a->ltris.size(), 1) * sizeof(F4), 256);
   L.off_shade = align_up(L.off_tris + std::max<size_t>(a->tris.size(), 1) * sizeof(F4), 256);
-  L.off_mats = align_up(L.off_shade + std::max<size_t>(a->shade.size(), 1) * sizeof(float4), 256);
+  L.off_mats = align_up(L.off_shade + std::max<size_t>(a->shade.size() + 3 * (size_t)std::max(nsph, 0), 1) *
+                                          sizeof(float4), 256);
   L.off_lights = align_up(L.off_mats + (size_t)std::max(nmat, 0) * 16 * sizeof(float), 256);
   L.off_uv = align_up(L.off_lights + std::max<size_t>((size_t)std::max(nlight, 0), 1) * 32 * sizeof(float), 256);
   L.off_texrec = align_up(L.off_uv + (size_t)std::max<int64_t>(uv_tris, 0) * 3 * sizeof(float2), 256);
   L.off_texels = align_up(L.off_texrec + (size_t)std::max(ntex, 0) * 2 * sizeof(float4), 256);
-  L.off_err = align_up(L.off_texels + (size_t)texels * sizeof(float4), 256);
+  L.off_sph = align_up(L.off_texels + (size_t)texels * sizeof(float4), 256);
+  L.off_err = align_up(L.off_sph + (size_t)std::max(nsph, 0) * 2 * sizeof(float4), 256);
   L.total = L.off_err + 256;
   return L;
 }
@@ -385,13 +388,34 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     for (int64_t t = 0; t < T; ++t)
       if (desc->tri_light[t] >= 0 && desc->light_ext[16 * (size_t)desc->tri_light[t]] == 3.0f)
         return fail(MGPU_E_INVALID, "mgpu_scene_create: triangle " + std::to_string(t) + " names a point light");
+  // analytic spheres: records as the traversal reads them, shading records after the triangles'
+  if (desc->nsphere < 0 || desc->nsphere > MGPU_MAX_SPHERES || (desc->nsphere > 0 && (!desc->spheres || !desc->sphere_mat)))
+    return fail(MGPU_E_INVALID, "mgpu_scene_create: bad spheres (at most " + std::to_string(MGPU_MAX_SPHERES) + ")");
+  std::vector<float4> sph((size_t)std::max(desc->nsphere, 0) * 2), sph_shade((size_t)std::max(desc->nsphere, 0) * 3);
+  for (int i = 0; i < desc->nsphere; ++i) {
+    const float *q = desc->spheres + 8 * (size_t)i;
+    bool ok = q[3] > 0.0f;
+    for (int k = 0; k < 8; ++k) ok = ok && std::isfinite(q[k]);
+    if (!ok || desc->sphere_mat[i] < 0 || desc->sphere_mat[i] >= desc->nmat)
+      return fail(MGPU_E_INVALID, "mgpu_scene_create: bad sphere " + std::to_string(i));
+    sph[2 * i] = make_float4(q[0], q[1], q[2], q[3]);
+    sph[2 * i + 1] = make_float4(q[4], q[5], q[6], q[7]);
+    int32_t mat = desc->sphere_mat[i], none = -1;
+    float4 a = make_float4(0, 0, 0, 0), b = a;
+    memcpy(&a.w, &mat, 4);
+    memcpy(&b.w, &none, 4);
+    sph_shade[3 * i] = a;
+    sph_shade[3 * i + 1] = b;
+    sph_shade[3 * i + 2] = make_float4(0, 0, 0, 0);
+  }
   const KdTree &tr = accel->tree;
   mgpu_accel *acc = const_cast<mgpu_accel *>(accel);
   register_staging(acc);
   const std::vector<Pair> &dpairs = accel->dpairs;
   const std::vector<F4> &ltris = accel->ltris, &tris = accel->tris;
   const std::vector<float4> &shade = accel->shade;
-  const SceneLayout L = scene_layout(accel, desc->nmat, desc->nlight, tp.uv ? T : 0, desc->ntex, tp.texels);
+  const SceneLayout L = scene_layout(accel, desc->nmat, desc->nlight, tp.uv ? T : 0, desc->ntex, tp.texels,
+                                     desc->nsphere);
   const size_t off_pairs = L.off_pairs, off_refs = L.off_refs, off_tris = L.off_tris, off_shade = L.off_shade,
                off_mats = L.off_mats, off_lights = L.off_lights, off_err = L.off_err, total = L.total;
   const size_t sz_pairs = dpairs.size() * sizeof(Pair), sz_mats = (size_t)desc->nmat * 16 * sizeof(float);
@@ -417,6 +441,11 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   if (e == cudaSuccess) e = up(off_mats, desc->materials, sz_mats);
   if (e == cudaSuccess && desc->nlight > 0) e = up(off_lights, lrec.data(), lrec.size() * sizeof(float));
   if (e == cudaSuccess && tp.uv) e = up(L.off_uv, desc->tri_uv, (size_t)T * 6 * sizeof(float));
+  if (e == cudaSuccess && desc->nsphere > 0) {
+    e = up(L.off_sph, sph.data(), sph.size() * sizeof(float4));
+    if (e == cudaSuccess)
+      e = up(off_shade + shade.size() * sizeof(float4), sph_shade.data(), sph_shade.size() * sizeof(float4));
+  }
   if (e == cudaSuccess) e = cudaMemsetAsync(base + off_err, 0, 256, st);
   // materials and lights are the caller's pageable arrays: wait for the copies
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -449,6 +478,8 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
   s->view.ntri = T;
   s->view.npairs = tr.pairs.size();
   s->view.nrefs = ltris.size() / 3;
+  s->view.spheres = desc->nsphere > 0 ? (const F4 *)(base + L.off_sph) : nullptr;
+  s->view.nsphere = desc->nsphere;
   s->d_shade = (float4 *)(base + off_shade);
   s->d_mats = (float *)(base + off_mats);
   s->d_lights = (float *)(base + off_lights);
@@ -501,7 +532,8 @@ int mgpu_scene_device_bytes(const mgpu_scene_desc *desc, const mgpu_accel *a, ui
     return fail(MGPU_E_INVALID, "mgpu_scene_device_bytes: bad argument");
   TexPlan tp;
   if (int rc = tex_plan(desc, tp)) return rc;
-  *out = scene_layout(a, desc->nmat, desc->nlight, tp.uv ? desc->ntri : 0, desc->ntex, tp.texels).total;
+  *out = scene_layout(a, desc->nmat, desc->nlight, tp.uv ? desc->ntri : 0, desc->ntex, tp.texels,
+                      std::max(desc->nsphere, 0)).total;
   return MGPU_OK;
 }
 

@@ -62,6 +62,20 @@ MGPU_HD void env_uv(V3 w, float &u, float &v) {
   v = theta / -kPi + 0.5f;
 }
 
+// Rotation of v by the unit quaternion q = (x, y, z, w): v + 2 w (u x v) + 2 u x (u x v), u = q.xyz.
+MGPU_HD V3 quat_rotate(float qx, float qy, float qz, float qw, V3 v) {
+  const V3 u = v3(qx, qy, qz);
+  const V3 t = cross(u, v) * 2.0f;
+  return v + t * qw + cross(u, t);
+}
+
+// Sphere::_getUV (Sphere.cpp:78-85) of an object-space point p of the unit-diameter sphere:
+// u = 1 - atan2(z, x) / 2 pi, v = 1/2 - asin(2 y) / pi.
+MGPU_HD void sphere_uv(V3 p, float &u, float &v) {
+  u = 1.0f - atan2f(p.z, p.x) * (1.0f / (2.0f * kPi));
+  v = 0.5f - asinf(fminf(fmaxf(2.0f * p.y, -1.0f), 1.0f)) * (1.0f / kPi);
+}
+
 // Textured keys replace the constants (Material::getSpectralSampleSet with a file name,
 // Material.cpp:260-283); DielectricBSDF uses the average transparency (DielectricBSDF.cpp:51-52).
 MGPU_HD void tex_apply(Material &m, int slot, float r, float g, float b) {

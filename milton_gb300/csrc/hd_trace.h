@@ -49,6 +49,8 @@ struct SceneView {
   float bmin[3], bmax[3];  // root bounds
   int64_t ntri;
   uint64_t npairs, nrefs;
+  const F4 *spheres;       // 2 per analytic sphere: (center, radius), world-to-object quaternion
+  int32_t nsphere;         // spheres are primitives ntri .. ntri + nsphere - 1
 };
 
 struct Ray {
@@ -241,11 +243,64 @@ MGPU_HD float safe_rcp(float d) {
   return 1.0f / d;
 }
 
-// returns false when the ray misses the scene (no step needed)
-MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32_t ntop, TravState &st) {
+// Ray-sphere test (Sphere::getIntersection, Sphere.cpp:17-48), FP32 with the roots taken as
+// c / q and q / a (q = b' + sign(b') sqrt(a disc)) and the discriminant from the closest approach
+// f = oc - (oc.d / a) d, which avoid the cancellations of the textbook formula (Haines et al.,
+// "Precision Improvements for Ray/Sphere Intersection", Ray Tracing Gems ch. 7): the smallest
+// root in (tmin, tbest) in t; false when there is none.
+MGPU_HD bool sphere_t(V3 o, V3 d, V3 c, float rad, float tmin, float tbest, float &t) {
+  const V3 oc = o - c;
+  const float a = dot(d, d);
+  const float bp = -dot(oc, d);
+  const V3 f = oc + d * (bp / a);
+  const float disc = rad * rad - dot(f, f);
+  if (!(disc >= 0.0f)) return false;
+  const float h = sqrtf(a * disc);
+  const float q = bp + (bp >= 0.0f ? h : -h);
+  const float cc = dot(oc, oc) - rad * rad;
+  float t0 = q != 0.0f ? cc / q : 0.0f, t1 = q / a;
+  if (t0 > t1) { const float x = t0; t0 = t1; t1 = x; }
+  if (t0 > tmin && t0 < tbest) { t = t0; return true; }
+  if (t1 > tmin && t1 < tbest) { t = t1; return true; }
+  return false;
+}
+
+// Closest (or, with any, first) sphere hit in (r.tmin, st.best): updates st.best / best_prim.
+#if defined(__CUDA_ARCH__)
+__device__ __noinline__
+#else
+inline
+#endif
+void spheres_hit(const SceneView &s, const Ray &r, TravState &st, bool any) {
+  for (int i = 0; i < s.nsphere; ++i) {
+#if defined(__CUDA_ARCH__)
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(s.spheres) + 2 * i);
+#else
+    const F4 q = s.spheres[2 * i];
+#endif
+    float t;
+    if (sphere_t(r.o, r.d, v3(q.x, q.y, q.z), q.w, r.tmin, st.best, t)) {
+      st.best = t;
+      st.best_prim = (int32_t)(s.ntri + i);
+      st.bb1 = st.bb2 = 0.0f;
+      if (any) return;
+    }
+  }
+}
+
+// returns false when no traversal step is needed: the ray misses the tree, or (any) a sphere
+// already occludes it; st.best_prim then holds the sphere hit, if any.  SPH: the scene may have
+// analytic spheres (kernels for scenes without them carry no sphere code).
+template <bool SPH = false>
+MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32_t ntop, TravState &st,
+                       bool any = false) {
   st.best = r.tmax;
   st.best_prim = -1;
   st.bb1 = st.bb2 = 0.0f;
+  if (SPH && s.nsphere > 0) {
+    spheres_hit(s, r, st, any);
+    if (any && st.best_prim >= 0) return false;
+  }
   if (s.ntri <= 0) return false;
   {
     V3 inv = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
@@ -341,13 +396,14 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, cons
 }
 
 // ANY = shadow query (returns on the first hit inside (tmin, tmax)).
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool SPH = false>
 MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *top, uint32_t ntop, TraceCounts *cnt) {
   TravState st;
   TravEntry stack[kMaxStack];
   hit.t = INFINITY; hit.prim = -1; hit.b1 = 0.0f; hit.b2 = 0.0f;
-  if (!trav_init(s, r, top, ntop, st)) return false;
-  while (!trav_step<ANY, COUNT>(s, st, stack, top, ntop, cnt)) {
+  if (trav_init<SPH>(s, r, top, ntop, st, ANY)) {
+    while (!trav_step<ANY, COUNT>(s, st, stack, top, ntop, cnt)) {
+    }
   }
   if (st.best_prim < 0) return false;
   hit.t = st.best; hit.prim = st.best_prim; hit.b1 = st.bb1; hit.b2 = st.bb2;
@@ -359,7 +415,7 @@ MGPU_HD bool traverse(const SceneView &s, const Ray &r, Hit &hit, const Pair *to
 //   view(i)                 the scene of the i-th ray (one scene, or a batch job's scene)
 //   load(i, ray)            fills the i-th ray of the batch
 //   store(i, found, state)  consumes the i-th result
-template <bool ANY, bool COUNT, class View, class Load, class Store>
+template <bool ANY, bool COUNT, bool SPH, class View, class Load, class Store>
 __device__ __forceinline__ void grid_trace(View view, const Pair *top, uint32_t ntop, uint32_t n, Load load,
                                            Store store, TraceCounts *cnt, uint32_t &rays_done) {
   TravState st;
@@ -369,8 +425,8 @@ __device__ __forceinline__ void grid_trace(View view, const Pair *top, uint32_t 
     Ray r;
     load(i, r);
     ++rays_done;
-    if (!trav_init(s, r, top, ntop, st)) {
-      store(i, false, st);
+    if (!trav_init<SPH>(s, r, top, ntop, st, ANY)) {
+      store(i, st.best_prim >= 0, st);
       continue;
     }
     while (!trav_step<ANY, COUNT>(s, st, stack, top, ntop, cnt)) {
@@ -383,7 +439,7 @@ __device__ __forceinline__ void grid_trace(View view, const Pair *top, uint32_t 
 // Traversal on GPUs", HPG 2009): every lane owns one ray; after each leaf step, lanes whose
 // ray finished take new rays from a global counter with one warp-aggregated atomicAdd, so a
 // warp never idles behind its slowest ray.  All 32 lanes of every warp must call this.
-template <bool ANY, bool COUNT, class View, class Load, class Store>
+template <bool ANY, bool COUNT, bool SPH, class View, class Load, class Store>
 __device__ __forceinline__ void persistent_trace(View view, const Pair *top, uint32_t ntop, uint32_t n,
                                                  uint32_t *fetch, Load load, Store store, TraceCounts *cnt,
                                                  uint32_t &rays_done) {
@@ -410,8 +466,8 @@ __device__ __forceinline__ void persistent_trace(View view, const Pair *top, uin
           Ray r;
           load(idx, r);
           ++rays_done;
-          if (trav_init(*sv, r, top, ntop, st)) have = true;
-          else store(idx, false, st);
+          if (trav_init<SPH>(*sv, r, top, ntop, st, ANY)) have = true;
+          else store(idx, st.best_prim >= 0, st);
         } else {
           exhausted = true;
         }

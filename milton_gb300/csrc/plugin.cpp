@@ -20,6 +20,8 @@ struct mgpu_renderer {
   std::vector<mgpu_texture> tex;
   int32_t bg_tex = 0;
   float bg_le[3] = {0, 0, 0};
+  std::vector<float> sph;
+  std::vector<int32_t> sph_mat;
   bool has_scene = false, has_n = false, has_light = false, has_flags = false;
   int32_t nmat = 0, nlight = 0;
   float camera[16] = {0, 0, 0, 0, 0, -1, 0, 1, 0, 45, 1, 0, 0, 1, 0, 0};
@@ -66,6 +68,9 @@ struct mgpu_renderer {
     d.textures = tex.empty() ? nullptr : tex.data();
     d.background_tex = bg_tex;
     for (int k = 0; k < 3; ++k) d.background_le[k] = bg_le[k];
+    d.nsphere = (int32_t)sph_mat.size();
+    d.spheres = sph.empty() ? nullptr : sph.data();
+    d.sphere_mat = sph_mat.empty() ? nullptr : sph_mat.data();
     return d;
   }
 };
@@ -135,6 +140,10 @@ int mgpu_renderer_set_scene(mgpu_renderer *r, const mgpu_scene_desc *d) {
   for (int32_t i = 0; i < d->ntex; ++i) r->tex[i].rgb = r->tex_rgb[i].data();
   r->bg_tex = d->background_tex;
   for (int k = 0; k < 3; ++k) r->bg_le[k] = d->background_le[k];
+  if (d->nsphere < 0 || (d->nsphere > 0 && (!d->spheres || !d->sphere_mat)))
+    return bad("mgpu_renderer_set_scene: bad spheres");
+  r->sph.assign(d->spheres, d->spheres + 8 * (size_t)std::max(d->nsphere, 0));
+  r->sph_mat.assign(d->sphere_mat, d->sphere_mat + std::max(d->nsphere, 0));
   r->has_scene = true;
   r->initted = false;
   return MGPU_OK;

@@ -163,10 +163,16 @@ __device__ __forceinline__ Material load_mat(const JobArgs &J, int i, uint32_t i
 // Image maps at a hit of triangle prim with barycentrics (b0, b1, b2): the uv (Shape::_getUV,
 // interpolated from the per-vertex uvs), then each textured key of the material and the bump
 // map (Material::initSurfacePoint, Material.cpp:157-225).
-__device__ __noinline__ void apply_textures(const JobArgs &J, int prim, float b0, float b1, float b2, Material &m,
-                                            V3 &ns) {
+__device__ __noinline__ void apply_textures(const JobArgs &J, int prim, float b0, float b1, float b2, V3 P,
+                                            Material &m, V3 &ns) {
   float u = 0.0f, v = 0.0f;
-  if (J.uv) {
+  if (prim >= J.view.ntri) {
+    // Sphere::_getUV (Sphere.cpp:78-85) of the object-space point: the offset from the centre,
+    // rotated into the sphere's frame, over its diameter
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(J.view.spheres) + 2 * (prim - J.view.ntri));
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(J.view.spheres) + 2 * (prim - J.view.ntri) + 1);
+    sphere_uv(quat_rotate(q.x, q.y, q.z, q.w, (P - v3(c.x, c.y, c.z)) * (0.5f / c.w)), u, v);
+  } else if (J.uv) {
     const float2 a = __ldg(J.uv + 3 * (int64_t)prim), b = __ldg(J.uv + 3 * (int64_t)prim + 1),
                  c = __ldg(J.uv + 3 * (int64_t)prim + 2);
     u = a.x * b0 + b.x * b1 + c.x * b2;
@@ -281,7 +287,7 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
 }
 
 // extend: closest hit for the live queue of bounce b
-template <bool COUNT, bool PERSIST>
+template <bool COUNT, bool PERSIST, bool SPH = false>
 __global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_extend(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
@@ -305,9 +311,9 @@ __global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_extend(RenderArgs a,
                           hit ? st.bb2 : 0.0f);
   };
   if (PERSIST)
-    persistent_trace<false, COUNT>(view_of, nullptr, 0, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
+    persistent_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
   else
-    grid_trace<false, COUNT>(view_of, nullptr, 0, n, load, store, &c, rays);
+    grid_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[0], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[1], (unsigned long long)c.refs);
@@ -327,8 +333,9 @@ __device__ __forceinline__ V3 fold_slots(const RenderArgs &a, int nl, int64_t p,
   return L;
 }
 
-// SURF: the wave has a scene with image maps or a background.  Scenes without them run the
-// variant that has neither branch, whose register allocation (and spilling) is the lighter.
+// SURF: the wave has a scene with image maps, a background or analytic spheres.  Scenes without
+// them run the variant that has none of those branches, whose register allocation (and spilling)
+// is the lighter.
 template <bool SURF>
 __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
@@ -367,19 +374,27 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         int x, y, s;
         pid = path_id(J, p, x, y, s);
         float t = h4.x, b1 = h4.z, b2 = h4.w, b0 = 1.0f - b1 - b2;
-        float4 va = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim);
-        float4 vb = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim + 1);
-        float4 vc = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim + 2);
-        float4 s0 = __ldg(J.shade + 3 * (int64_t)prim), s1 = __ldg(J.shade + 3 * (int64_t)prim + 1),
-               s2 = __ldg(J.shade + 3 * (int64_t)prim + 2);
-        V3 v0 = v3(va.x, va.y, va.z), v1 = v3(vb.x, vb.y, vb.z), v2 = v3(vc.x, vc.y, vc.z);
-        P = v0 * b0 + v1 * b1 + v2 * b2;
-        ns = normalize(v3(s0.x, s0.y, s0.z) * b0 + v3(s1.x, s1.y, s1.z) * b1 + v3(s2.x, s2.y, s2.z) * b2);
-        ng = normalize(cross(v1 - v0, v2 - v0));
+        float4 s0 = __ldg(J.shade + 3 * (int64_t)prim), s1 = __ldg(J.shade + 3 * (int64_t)prim + 1);
+        if (SURF && prim >= J.view.ntri) {
+          // analytic sphere: the hit on the ray, the radial normal (Sphere::_getGeometricNormal)
+          const float4 c = __ldg(reinterpret_cast<const float4 *>(J.view.spheres) + 2 * (prim - J.view.ntri));
+          P = v3(o4.x, o4.y, o4.z) + d * t;
+          ns = normalize(P - v3(c.x, c.y, c.z));
+          ng = ns;
+        } else {
+          float4 va = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim);
+          float4 vb = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim + 1);
+          float4 vc = __ldg(reinterpret_cast<const float4 *>(J.view.tris) + 3 * (int64_t)prim + 2);
+          float4 s2 = __ldg(J.shade + 3 * (int64_t)prim + 2);
+          V3 v0 = v3(va.x, va.y, va.z), v1 = v3(vb.x, vb.y, vb.z), v2 = v3(vc.x, vc.y, vc.z);
+          P = v0 * b0 + v1 * b1 + v2 * b2;
+          ns = normalize(v3(s0.x, s0.y, s0.z) * b0 + v3(s1.x, s1.y, s1.z) * b1 + v3(s2.x, s2.y, s2.z) * b2);
+          ng = normalize(cross(v1 - v0, v2 - v0));
+        }
         int mi = __float_as_int(s0.w);
         self = __float_as_int(s1.w);
         m = load_mat(J, mi, flags & kFlagIorMask);
-        if (SURF && (m.tex_kd | m.tex_ks | m.tex_tr | m.tex_bump) != 0) apply_textures(J, prim, b0, b1, b2, m, ns);
+        if (SURF && (m.tex_kd | m.tex_ks | m.tex_tr | m.tex_bump) != 0) apply_textures(J, prim, b0, b1, b2, P, m, ns);
         bool spec = is_specular(m);
         if (spec) flags |= kFlagSpecular;
         if (self >= 0) {
@@ -511,7 +526,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
 }
 
 // shadow: any-hit query per queued light sample; an occluded sample's slot is zeroed
-template <bool COUNT, bool PERSIST>
+template <bool COUNT, bool PERSIST, bool SPH = false>
 __global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_shadow(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrNee + b];
   const float4 *so = a.so, *sd = a.sd;
@@ -536,9 +551,9 @@ __global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_shadow(RenderArgs a,
     if (hit) slots[__float_as_uint(so[i].w)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   };
   if (PERSIST)
-    persistent_trace<true, COUNT>(view_of, nullptr, 0, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
+    persistent_trace<true, COUNT, SPH>(view_of, nullptr, 0, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
   else
-    grid_trace<true, COUNT>(view_of, nullptr, 0, n, load, store, &c, rays);
+    grid_trace<true, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
   if (COUNT && rays) {
     atomicAdd(&a.tcount[4], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[5], (unsigned long long)c.refs);
@@ -1145,8 +1160,10 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   }
 
   const bool persist = g_tune.persistent.load() != 0;
-  auto kext = persist ? k_extend<COUNT, true> : k_extend<COUNT, false>;
-  auto kshw = persist ? k_shadow<COUNT, true> : k_shadow<COUNT, false>;
+  bool sph = false;  // a job's scene has analytic spheres: the traversal kernels that test them
+  for (const Job &j : jobs) sph = sph || j.scene->view.nsphere > 0;
+  auto kext = sph ? k_extend<COUNT, false, true> : persist ? k_extend<COUNT, true> : k_extend<COUNT, false>;
+  auto kshw = sph ? k_shadow<COUNT, false, true> : persist ? k_shadow<COUNT, true> : k_shadow<COUNT, false>;
   const int g_gen = grid_for((const void *)k_generate, 0);
   const int g_ext = grid_for((const void *)kext, 0);
   const int g_sha = grid_for((const void *)k_shade<true>, 0);
@@ -1202,10 +1219,10 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
     a.tcount = w->tcount;
     a.max_b = wv.max_b;
     const int max_b = wv.max_b;
-    bool surf = false;  // a chunk's scene has image maps or a background
+    bool surf = false;  // a chunk's scene has image maps, a background or analytic spheres
     for (const JobArgs &c : wv.chunks)
       surf = surf || c.texrec != nullptr || c.bg_tex != 0 || c.bg_le[0] != 0.0f || c.bg_le[1] != 0.0f ||
-             c.bg_le[2] != 0.0f;
+             c.bg_le[2] != 0.0f || c.view.nsphere > 0;
     err = cudaMemsetAsync(w->counters, 0, kNumCounters * sizeof(uint32_t), st);
     int m = pf.begin(kProfGenerate, st);
     k_generate<<<g_gen, kBlock, 0, st>>>(a);

@@ -39,6 +39,8 @@ struct SrvScene {
   std::vector<mgpu_texture> tex;
   int32_t bg_tex = 0;
   float bg_le[3] = {0, 0, 0};
+  std::vector<float> sph;
+  std::vector<int32_t> sph_mat;
   int32_t nmat = 0, nlight = 0;
   // written by a build thread, read under the server mutex
   int state = kIdle;
@@ -69,6 +71,9 @@ struct SrvScene {
     d.textures = tex.empty() ? nullptr : tex.data();
     d.background_tex = bg_tex;
     for (int k = 0; k < 3; ++k) d.background_le[k] = bg_le[k];
+    d.nsphere = (int32_t)sph_mat.size();
+    d.spheres = sph.empty() ? nullptr : sph.data();
+    d.sphere_mat = sph_mat.empty() ? nullptr : sph_mat.data();
     return d;
   }
 };
@@ -425,6 +430,12 @@ int mgpu_server_add_scene(mgpu_server *s, const mgpu_scene_desc *d, int32_t *sce
     for (int32_t i = 0; i < d->ntex; ++i) sc->tex[i].rgb = sc->tex_rgb[i].data();
     sc->bg_tex = d->background_tex;
     for (int k = 0; k < 3; ++k) sc->bg_le[k] = d->background_le[k];
+    if (d->nsphere < 0 || (d->nsphere > 0 && (!d->spheres || !d->sphere_mat)))
+      return fail(MGPU_E_INVALID, "mgpu_server_add_scene: bad spheres");
+    if (d->nsphere > 0) {
+      sc->sph.assign(d->spheres, d->spheres + 8 * (size_t)d->nsphere);
+      sc->sph_mat.assign(d->sphere_mat, d->sphere_mat + d->nsphere);
+    }
   } catch (...) {
     return fail(MGPU_E_NOMEM, "mgpu_server_add_scene: out of host memory");
   }

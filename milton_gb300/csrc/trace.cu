@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(SceneView s, uint32_t nto
     if (COUNT) counts[i] = make_uint4(c.nodes, c.refs, c.tris, c.max_stack);
   };
   auto view = [&](uint32_t) -> const SceneView & { return s; };
-  persistent_trace<ANY, COUNT>(view, top, ntop, n, fetch, load, store, &c, done);
+  persistent_trace<ANY, COUNT, true>(view, top, ntop, n, fetch, load, store, &c, done);
 }
 
 template <bool ANY, bool COUNT>

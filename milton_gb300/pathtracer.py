@@ -57,6 +57,9 @@ def _desc(scene: Scene) -> N.SceneDesc:
         texs[i] = N.Texture(w, h, N.ptr(t.rgb), t.kind, f, support, p1, p2, t.repeat_u, t.repeat_v,
                             t.bump_intensity)
     d.textures = texs
+    d.nsphere = len(scene.spheres)
+    d.spheres = N.ptr(scene.spheres) if len(scene.spheres) else None
+    d.sphere_mat = N.ptr(scene.sphere_mat) if len(scene.spheres) else None
     d.background_tex = int(scene.background_tex)
     for k in range(3):
         d.background_le[k] = float(scene.background_le[k])

@@ -19,6 +19,9 @@ A `Scene` holds exactly what crosses the C ABI (``mgpu_scene_desc``):
 * ``tri_uv``    (T, 3, 2) float32  per-vertex uvs, or None (every uv is (0, 0))
 * ``textures``  list of `Texture`: image maps named by the material texture slots
                                    [10] kd, [11] ks, [12] transparency, [13] bump (1 + index)
+* ``spheres``   (S, 8)    float32  analytic spheres beside the soup: center[3], radius, world-to-object
+                                   rotation quaternion (x, y, z, w); primitive ids ntri + index
+* ``sphere_mat`` (S,)     int32    their material indices
 * ``background_tex`` int           1 + index of the environment map (latitude-longitude), or 0
 * ``background_le``  (3,) float32  constant background radiance when background_tex is 0
 
@@ -134,6 +137,25 @@ TEX_BUMP = 1
 FILTERS = {"box": 1, "triangle": 2, "gaussian": 3, "mitchell": 4, "lanczosSinc": 5}
 
 
+def quat_from_matrix(R) -> np.ndarray:
+    """Unit quaternion (x, y, z, w) of a 3 x 3 rotation matrix (Shepperd's method)."""
+    R = np.asarray(R, np.float64)
+    tr = np.trace(R)
+    if tr > 0:
+        s = 2.0 * np.sqrt(tr + 1.0)
+        q = [(R[2, 1] - R[1, 2]) / s, (R[0, 2] - R[2, 0]) / s, (R[1, 0] - R[0, 1]) / s, 0.25 * s]
+    else:
+        i = int(np.argmax(np.diag(R)))
+        j, k = (i + 1) % 3, (i + 2) % 3
+        s = 2.0 * np.sqrt(1.0 + R[i, i] - R[j, j] - R[k, k])
+        q = [0.0, 0.0, 0.0, (R[k, j] - R[j, k]) / s]
+        q[i] = 0.25 * s
+        q[j] = (R[j, i] + R[i, j]) / s
+        q[k] = (R[k, i] + R[i, k]) / s
+    q = np.asarray(q)
+    return (q / np.linalg.norm(q)).astype(np.float32)
+
+
 @dataclass
 class Texture:
     """A material's image map (include/mgpu.h, mgpu_texture): rgb (H, W, 3) linear values, row 0
@@ -178,6 +200,8 @@ class Scene:
     textures: list = field(default_factory=list)
     background_tex: int = 0
     background_le: np.ndarray = field(default_factory=lambda: np.zeros(3, np.float32))
+    spheres: np.ndarray = field(default_factory=lambda: np.zeros((0, 8), np.float32))
+    sphere_mat: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
 
     def __post_init__(self):
         self.tri_v = np.ascontiguousarray(self.tri_v, np.float32).reshape(-1, 3, 3)
@@ -211,6 +235,12 @@ class Scene:
             if self.tri_uv.shape[0] != T:
                 raise ValueError(f"tri_uv has {self.tri_uv.shape[0]} rows, expected {T}")
         self.background_le = np.ascontiguousarray(np.broadcast_to(np.asarray(self.background_le, np.float32), 3))
+        self.spheres = np.ascontiguousarray(self.spheres, np.float32).reshape(-1, 8)
+        self.sphere_mat = np.ascontiguousarray(self.sphere_mat, np.int32).reshape(-1)
+        if len(self.sphere_mat) != len(self.spheres):
+            raise ValueError("sphere_mat needs one entry per sphere")
+        if len(self.spheres) and (self.sphere_mat.min() < 0 or self.sphere_mat.max() >= len(self.materials)):
+            raise ValueError("sphere material index out of range")
         if not 0 <= self.background_tex <= len(self.textures):
             raise ValueError("background texture out of range")
         slots = self.materials[:, 10:14] if len(self.materials) else np.zeros((0, 4), np.float32)
@@ -222,7 +252,8 @@ class Scene:
         return int(self.tri_v.shape[0])
 
     def nbytes(self) -> int:
-        extra = (0 if self.tri_uv is None else self.tri_uv.nbytes) + sum(t.rgb.nbytes for t in self.textures)
+        extra = (0 if self.tri_uv is None else self.tri_uv.nbytes) + sum(t.rgb.nbytes for t in self.textures) + \
+            self.spheres.nbytes + self.sphere_mat.nbytes
         return extra + sum(a.nbytes for a in (self.tri_v, self.tri_n, self.tri_mat, self.tri_light, self.tri_flags,
                                               self.materials, self.lights, self.light_ext))
 
@@ -236,6 +267,8 @@ class SceneBuilder:
         self.textures: list[Texture] = []
         self.bg_tex = 0
         self.bg_le = np.zeros(3, np.float32)
+        self.spheres: list[np.ndarray] = []
+        self.sphere_mat: list[int] = []
         self.materials: list[np.ndarray] = []
         self.lights: list[np.ndarray] = []
         self.light_ext: list[np.ndarray] = []
@@ -245,6 +278,18 @@ class SceneBuilder:
     def material(self, rec: np.ndarray) -> int:
         self.materials.append(np.asarray(rec, np.float32))
         return len(self.materials) - 1
+
+    def add_sphere(self, center, radius: float, mat: int, rotation=None) -> int:
+        """An analytic sphere (Milton's Sphere: its centre, radius and object frame, given by the
+        3 x 3 rotation from object to world, identity by default).  Returns its index among the
+        spheres (its primitive id is the triangle count plus this index)."""
+        rec = np.zeros(8, np.float32)
+        rec[0:3] = center
+        rec[3] = radius
+        rec[4:8] = quat_from_matrix(np.eye(3) if rotation is None else np.asarray(rotation, np.float64).T)
+        self.spheres.append(rec)
+        self.sphere_mat.append(int(mat))
+        return len(self.spheres) - 1
 
     def background(self, tex: int = 0, le=(0.0, 0.0, 0.0)) -> None:
         """The scene's background: an environment map (tex = a value from texture()) or the
@@ -349,6 +394,8 @@ class SceneBuilder:
                                      for u, v in zip(self.uv, self.v)])
         return Scene(
             tri_uv=tri_uv, textures=list(self.textures), background_tex=self.bg_tex, background_le=self.bg_le,
+            spheres=np.stack(self.spheres) if self.spheres else np.zeros((0, 8), np.float32),
+            sphere_mat=np.asarray(self.sphere_mat, np.int32),
             tri_v=cat(self.v, (0, 3, 3), np.float32), tri_n=cat(self.n, (0, 3, 3), np.float32),
             tri_mat=cat(self.mat, (0,), np.int32), tri_light=cat(self.light, (0,), np.int32),
             tri_flags=cat(self.flags, (0,), np.uint32),

@@ -44,9 +44,10 @@ its bumpMap become textures (PNG, PPM / PGM) with the material's filter, repeatU
 bumpIntensity, and every triangle carries the uvs of Shape::_getUV for the shape it came from
 (Plane, Triangle, Cube -- from the world position, as the reference does -- and Mesh: the first
 vertex's texture coordinate for the whole triangle).  An image that fails to load leaves the
-key at 0.7 or the normal unbumped, as the reference's Material does.  Spheres are taken when the caller passes tessellate=(nu, nv): each becomes an
-nu x nv UV sphere with radial normals under Milton's T(position) S(2 radius) (:596-611), an
-approximation of the analytic surface.  Instances of named shapes are copied (their geometry
+key at 0.7 or the normal unbumped, as the reference's Material does.  Spheres are analytic:
+centre, radius and frame of Milton's T(position) S(2 radius) (:596-611) under the graph's
+transform, which must then be a similarity; with tessellate=(nu, nv) they become nu x nv UV
+spheres with radial normals instead (an approximation, for many or distorted spheres).  Instances of named shapes are copied (their geometry
 under the instance's transform chain, with the material active at the instance).  A thin-lens
 camera keeps its aperture, f-stop and focal distance; its autofocus is resolved against the
 resident scene (pathtracer.resolve_autofocus).  A "cube" becomes the 12 triangles of Milton's
@@ -782,12 +783,11 @@ class _Loader:
             return self.shape_set(v)
         elif t in ("cube", "point"):
             pass
-        elif t == "sphere" and self.tessellate:
+        elif t == "sphere":
             req.update(position="point3", radius="real_t")
-        elif t in ("sphere", "cylinder", "cone", "blob", "dynamic"):
-            raise SceneFileError(f"shape '{t}' is not a triangle shape; the GPU path renders planes, cubes, "
-                                 "triangles, meshes and points" + (" (spheres with tessellate=(nu, nv))"
-                                                                   if t == "sphere" else ""))
+        elif t in ("cylinder", "cone", "blob", "dynamic"):
+            raise SceneFileError(f"shape '{t}' is not supported by the GPU path (planes, cubes, triangles, "
+                                 "meshes, spheres and points are)")
         else:
             raise SceneFileError("invalid shape type")
         props = {}
@@ -816,6 +816,13 @@ class _Loader:
                 local = local @ _trans(pos)
             if "radius" in props:
                 local = local @ _scale([2.0 * props["radius"]] * 3)
+            if not self.tessellate:
+                node = _Node("shape", _Shape("sphere", {}, local))
+                self.name_node(props, node)
+                self.begin(node)
+                self.visit(v, {"material": self.material, "spatialAccel": None}, strict=False)
+                self.end()
+                return
             tris, nrm, uv = _unit_sphere(*self.tessellate)
             node = _Node("shape", _Shape("mesh", {"v": tris.reshape(-1, 3).astype(np.float64),
                                                   "f": np.arange(tris.shape[0] * 3).reshape(-1, 3),
@@ -1258,6 +1265,21 @@ class _Flattener:
         per_sr = math.pi if emitter == "oriented" else 4.0 * math.pi
         omni_ext = np.zeros(16, np.float32)
         omni_ext[15] = 1.0 if emitter == "omni" else 0.0
+        if sh.kind == "sphere":
+            # an analytic sphere beside the soup: the object frame of T R S must be a similarity
+            # (a uniformly scaled rotation) for the centre / radius / rotation record
+            if emitter != "null":
+                raise SceneFileError("an emitting sphere is not supported by the GPU path")
+            msph = trans @ sh.local
+            A = msph[:3, :3]
+            k = float(np.linalg.norm(A[:, 0]))
+            if k <= 0 or not np.allclose(A.T @ A, k * k * np.eye(3), rtol=1e-6, atol=1e-9 * k * k) or \
+                    np.linalg.det(A) <= 0:
+                raise SceneFileError("a sphere under a non-uniform scale or a reflection is not supported by the "
+                                     "GPU path as an analytic sphere (load with tessellate=(nu, nv))")
+            mi = self.material_record(self.active)
+            self.b.add_sphere(msph[:3, 3], 0.5 * k, mi, rotation=A / k)
+            return
         if sh.kind == "point":
             # PointShape (PointShape.cpp): its position; area 0, so Le = power / pi or power / 4 pi
             if emitter != "null":
@@ -1483,8 +1505,8 @@ def _unit_sphere(nu: int, nv: int):
 
 def loads(text: str, base_dir: str = ".", source: str = "<string>", tessellate=None) -> SceneFile:
     """Parses already-read scene text (see read_scene_text for how a file becomes text).
-    tessellate=(nu, nv) turns analytic spheres into UV spheres of that resolution (an
-    approximation of Milton's Sphere; without it they are refused)."""
+    tessellate=(nu, nv) turns spheres into UV spheres of that resolution (an approximation of
+    Milton's Sphere; without it they are analytic spheres)."""
     ld = _Loader(base_dir, tessellate)
     ld.root_obj(parse_text(text))
     fl = _Flattener(ld.named, base_dir)

@@ -39,6 +39,7 @@
  *                          its application at one texel), M/filters/{Box,Triangle,Gaussian,Mitchell,
  *                          LanczosSinc}Filter.cpp (evaluate), M/shapes/Triangle.cpp:23-39 (uv),
  *                          M/common/image/Rgba.inl:32-45 (byte / 255, luminance)
+ *   spheres                M/shapes/Sphere.cpp:17-85 (intersection in object space, uv, normal)
  *   background             M/core/Scene.cpp:116-118, M/renderers/renderers/PathTracer.cpp:39-42,
  *                          M/materials/emitters/EnvironmentMap.cpp:40-96, OmniEmitter.cpp
  *   constants              M/common/arch.h:120-137 (EPSILON 1e-7, double), M/common/utilities.h:240 (EQ),
@@ -189,6 +190,9 @@ typedef struct {
   orc_tex *tex;
   int bg_tex;          /* background: 1 + colour map (environment map) or 0 */
   double bg_le[3];     /* constant background radiance when bg_tex == 0 */
+  int nsph;            /* analytic spheres: primitive ids ntri .. ntri + nsph - 1 */
+  const float *sph;    /* 8 floats each: center, radius, world-to-object quaternion */
+  const int32_t *sph_mat;
 } orc_scene;
 
 static inline v3 tri_vert(const orc_scene *s, int64_t t, int k) {
@@ -1092,11 +1096,65 @@ static v3 shading_normal(const orc_scene *s, int64_t tri, v3 p) {
   return vnorm(n);
 }
 
+/* Analytic spheres: Milton's Sphere (Sphere.cpp), a sphere of radius 1/2 under T(center)
+ * R^T S(2 radius); rays are taken to its object space, where the quadratic is solved
+ * (getIntersection / intersects, Sphere.cpp:17-75, INTERSECT_TOLERANCE = EPSILON).          */
+static v3 qrot(const float *q, v3 v) { /* rotation by the unit quaternion (x, y, z, w) */
+  v3 u = V(q[0], q[1], q[2]);
+  v3 t = vmul(vcross(u, v), 2.0);
+  return vadd(vadd(v, vmul(t, q[3])), vcross(u, t));
+}
+
+static void sphere_obj(const float *sp, v3 o, v3 d, v3 *P, v3 *D) {
+  double k = 1.0 / (2.0 * sp[3]);
+  *P = vmul(qrot(sp + 4, vsub(o, V(sp[0], sp[1], sp[2]))), k);
+  *D = vmul(qrot(sp + 4, d), k);
+}
+
+static double sphere_closest(const float *sp, v3 o, v3 d) {
+  v3 P, D;
+  sphere_obj(sp, o, d, &P, &D);
+  double A = 2 * vdot(D, D), B = -2 * vdot(P, D), C = vdot(P, P) - 0.25;
+  double disc = B * B - 2 * A * C;
+  if (disc < 0) return ORC_INF;
+  disc = sqrt(disc);
+  double F = 1 / A, t = (B - disc) * F;
+  if (t > ORC_EPS) return t;
+  t = (B + disc) * F;
+  return t > ORC_EPS ? t : ORC_INF;
+}
+
+static int sphere_any(const float *sp, v3 o, v3 d, double tmax) {
+  v3 P, D;
+  sphere_obj(sp, o, d, &P, &D);
+  double A = 2 * vdot(D, D), B = -2 * vdot(P, D), C = vdot(P, P) - 0.25;
+  double disc = B * B - 2 * A * C;
+  if (disc < 0) return 0;
+  disc = sqrt(disc);
+  double F = 1 / A, t = (B + disc) * F;
+  if (t < tmax && t > ORC_EPS) return 1;
+  t = (B - disc) * F;
+  return t < tmax && t > ORC_EPS;
+}
+
+/* closest hit among the triangles (kd-tree) and the spheres: t, and the primitive in *prim */
+static double scene_closest(const orc_scene *s, const orc_tree *tr, v3 o, v3 d, int64_t *prim);
+static int scene_any(const orc_scene *s, const orc_tree *tr, v3 o, v3 d, double tmax);
+
 /* uv at a hit (Triangle::_getUV, Triangle.cpp:23-39: area-ratio barycentrics of the hit point
  * weighting the three vertex uvs; the other shapes' _getUV are affine over each of their
  * triangles, which the per-vertex uvs encode) */
 static void hit_uv(const orc_scene *s, int64_t tri, v3 p, double *u, double *v) {
   *u = *v = 0.0;
+  if (tri >= s->ntri) { /* Sphere::_getUV of the object-space point (Sphere.cpp:78-85) */
+    const float *sp = s->sph + 8 * (tri - s->ntri);
+    v3 P, D;
+    sphere_obj(sp, p, V(0, 0, 1), &P, &D);
+    *u = 1 - atan2(P.z, P.x) * (1 / (2 * ORC_PI));
+    double y2 = 2 * P.y;
+    *v = 0.5 - asin(y2 > 1 ? 1 : (y2 < -1 ? -1 : y2)) * (1 / ORC_PI);
+    return;
+  }
   if (!s->uv) return;
   v3 a = tri_vert(s, tri, 0), b = tri_vert(s, tri, 1), c = tri_vert(s, tri, 2);
   double A = 1.0 / vlen(vcross(vsub(b, a), vsub(c, a)));
@@ -1258,7 +1316,7 @@ static void direct_light(const orc_render_ctx *c, orc_path *ph, int depth, v3 p,
         if (cwo > 0 && cwi > 0 && (fr[0] != 0 || fr[1] != 0 || fr[2] != 0)) {
           ph->rays_shadow++;
           /* Scene::intersects(ray, t - EPS) -> ShapeSet/kd intersects(ray, t - 2 EPS) */
-          if (!kd_any(s, c->tr, p, wo, t - 2 * ORC_EPS, NULL)) {
+          if (!scene_any(s, c->tr, p, wo, t - 2 * ORC_EPS)) {
             /* OrientedEmitter: the light's normal side only; OmniEmitter: every direction */
             double le = (L->omni || vdot(ln, vneg(wo)) > 0) ? 1.0 : 0.0;
             for (int k = 0; k < 3; ++k) dir[k] += (fr[k] * L->Le[k] * le * cwo * cwi) / (t * t);
@@ -1269,20 +1327,42 @@ static void direct_light(const orc_render_ctx *c, orc_path *ph, int depth, v3 p,
   }
 }
 
+static double scene_closest(const orc_scene *s, const orc_tree *tr, v3 o, v3 d, int64_t *prim) {
+  double t = kd_closest(s, tr, o, d, prim, NULL);
+  for (int i = 0; i < s->nsph; ++i) {
+    double ts = sphere_closest(s->sph + 8 * i, o, d);
+    if (ts < t) {
+      t = ts;
+      *prim = s->ntri + i;
+    }
+  }
+  return t;
+}
+
+static int scene_any(const orc_scene *s, const orc_tree *tr, v3 o, v3 d, double tmax) {
+  for (int i = 0; i < s->nsph; ++i)
+    if (sphere_any(s->sph + 8 * i, o, d, tmax)) return 1;
+  return kd_any(s, tr, o, d, tmax, NULL);
+}
+
 static void evaluate(const orc_render_ctx *c, orc_path *ph, v3 o, v3 d, int depth, double out[3]) {
   const orc_scene *s = c->s;
   out[0] = out[1] = out[2] = 0;
   if (depth >= ORC_HARD_DEPTH_CAP) { ph->truncated++; return; }
   int64_t tri;
   ph->rays_ext++;
-  double t = kd_closest(s, c->tr, o, d, &tri, NULL);
+  double t = scene_closest(s, c->tr, o, d, &tri);
   if (!(t > ORC_EPS && t < ORC_INF)) { /* PathTracer.cpp:39-42: a miss adds the background */
     background(s, d, out);
     return;
   }
   v3 p = vadd(o, vmul(d, t));
-  v3 ns = shading_normal(s, tri, p);
-  const orc_mat *m = &s->mats[s->mat[tri]];
+  const int on_sphere = tri >= s->ntri;
+  /* a sphere's normal is radial (Sphere::_getGeometricNormal with a similarity transform) */
+  v3 ns = on_sphere ? vnorm(vsub(p, V(s->sph[8 * (tri - s->ntri)], s->sph[8 * (tri - s->ntri) + 1],
+                                          s->sph[8 * (tri - s->ntri) + 2])))
+                    : shading_normal(s, tri, p);
+  const orc_mat *m = &s->mats[on_sphere ? s->sph_mat[tri - s->ntri] : s->mat[tri]];
   orc_mat mt;
   if (m->tex[0] || m->tex[1] || m->tex[2] || m->tex[3]) {
     mt = *m;
@@ -1291,7 +1371,7 @@ static void evaluate(const orc_render_ctx *c, orc_path *ph, v3 o, v3 d, int dept
   }
   orc_bsdf b = {m, ns, d, ph->ior_index + 1};
   if (is_specular(m)) ph->specular = 1;
-  int li = s->light ? s->light[tri] : -1;
+  int li = (s->light && !on_sphere) ? s->light[tri] : -1;
   if (li >= 0) {
     const orc_light *L = &s->lights[li];
     double le = (L->omni || vdot(ns, vneg(d)) > 0) ? 1.0 : 0.0; /* OrientedEmitter on the hit's normal */
@@ -1408,9 +1488,9 @@ static void *render_thread(void *arg) {
 int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat, const int32_t *light,
                const uint32_t *flags, int nmat, const float *mats, int nlight, const float *lights,
                const float *light_ext, const float *tri_uv, int ntex, const float *tex_params,
-               const float *const *tex_rgb, const float *bg, const orc_tree *tr, const float *camera,
-               const int32_t *ip, uint64_t seed, uint32_t stream, double *film_sum, double *path_out,
-               uint64_t *stats_out) {
+               const float *const *tex_rgb, const float *bg, int nsph, const float *sph, const int32_t *sph_mat,
+               const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed, uint32_t stream,
+               double *film_sum, double *path_out, uint64_t *stats_out) {
   orc_scene *s = scene_from_arrays(ntri, v, n, mat, light, flags, nmat, mats, nlight, lights, light_ext);
   s->uv = tri_uv;
   s->ntex = ntex;
@@ -1420,6 +1500,9 @@ int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat,
     s->bg_tex = (int)bg[0];
     for (int k = 0; k < 3; ++k) s->bg_le[k] = bg[1 + k];
   }
+  s->nsph = nsph;
+  s->sph = sph;
+  s->sph_mat = sph_mat;
   orc_render_ctx c;
   c.s = s;
   c.tr = tr;
@@ -1524,6 +1607,11 @@ void orc_texture_lookup(const float *params, const float *rgb, double u, double 
   }
   free(t->wts);
   free(t);
+}
+
+/* Sphere::getIntersection of one sphere record (8 floats) for the ray (o, d) (tests) */
+double orc_sphere_closest(const float *sp, const double *o, const double *d) {
+  return sphere_closest(sp, V(o[0], o[1], o[2]), V(d[0], d[1], d[2]));
 }
 
 /* background radiance of a ray with direction d (tests): params / rgb describe the environment

@@ -33,8 +33,10 @@ def load() -> C.CDLL:
     lib.orc_trace_closest.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, vp]
     lib.orc_trace_any.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp]
     lib.orc_render.restype = C.c_int
-    lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp, vp,
-                               vp, vp, u64, u32, vp, vp, vp]
+    lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp,
+                               C.c_int, vp, vp, vp, vp, vp, u64, u32, vp, vp, vp]
+    lib.orc_sphere_closest.restype = C.c_double
+    lib.orc_sphere_closest.argtypes = [vp, vp, vp]
     lib.orc_background.argtypes = [vp, vp, vp, vp, vp]
     lib.orc_texture_lookup.argtypes = [vp, vp, C.c_double, C.c_double, vp, vp]
     lib.orc_philox4x32_10.argtypes = [vp, vp, vp]
@@ -141,13 +143,15 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
     uv = None if uv is None else np.ascontiguousarray(uv, np.float32)
     textures = list(getattr(scene, "textures", []))
     tparams, trgb = texture_params(textures)
+    sph = np.ascontiguousarray(getattr(scene, "spheres", np.zeros((0, 8))), np.float32).reshape(-1, 8)
+    sph_mat = np.ascontiguousarray(getattr(scene, "sphere_mat", np.zeros(0)), np.int32)
     bg = np.zeros(4, np.float32)
     bg[0] = getattr(scene, "background_tex", 0)
     bg[1:4] = getattr(scene, "background_le", (0.0, 0.0, 0.0))
     lib.orc_render(scene.ntri, _p(scene.tri_v), _p(scene.tri_n), _p(scene.tri_mat), _p(scene.tri_light),
                    _p(scene.tri_flags), len(scene.materials), _p(scene.materials), len(scene.lights), _p(lights),
-                   _p(ext), _p(uv), len(textures), _p(tparams), C.cast(trgb, C.c_void_p), _p(bg), tree.h, _p(cam),
-                   _p(ip), seed, stream, _p(film), _p(paths), _p(st))
+                   _p(ext), _p(uv), len(textures), _p(tparams), C.cast(trgb, C.c_void_p), _p(bg), len(sph), _p(sph),
+                   _p(sph_mat), tree.h, _p(cam), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
     mean = film[r0:r1] / max(sample_count, 1)
     if per_path:
         paths = paths.reshape(height, width, sample_count, 3)[r0:r1]
@@ -187,12 +191,21 @@ def background(direction, tex=None, le=(0.0, 0.0, 0.0)) -> np.ndarray:
     out = np.zeros(3, np.float64)
     d = np.ascontiguousarray(direction, np.float64)
     if tex is None:
-        lib.orc_background(None, None, _p(np.ascontiguousarray(le, np.float64)), _p(d), _p(out))
+        le = np.ascontiguousarray(le, np.float64)
+        lib.orc_background(None, None, _p(le), _p(d), _p(out))
     else:
         params, _ = texture_params([tex])
         rgb = np.ascontiguousarray(tex.rgb, np.float32)
         lib.orc_background(_p(params), rgb.ctypes.data, None, _p(d), _p(out))
     return out
+
+
+def sphere_closest(sphere8, o, d) -> float:
+    """Milton's Sphere::getIntersection for one sphere record (center, radius, quaternion)."""
+    sp = np.ascontiguousarray(sphere8, np.float32)
+    o = np.ascontiguousarray(o, np.float64)
+    d = np.ascontiguousarray(d, np.float64)
+    return float(load().orc_sphere_closest(_p(sp), _p(o), _p(d)))
 
 
 def philox(ctr, key) -> np.ndarray:

@@ -54,6 +54,8 @@ int hc_trace_kd(const float *v, const uint32_t *flags, int64_t ntri, const float
   s.ntri = ntri;
   s.npairs = t.pairs.size();
   s.nrefs = ltris.size() / 3;
+  s.spheres = nullptr;
+  s.nsphere = 0;
   const Pair *top = use_top ? dpairs.data() : nullptr;
   uint32_t ntop = use_top ? t.top_pairs : 0;
   for (int64_t i = 0; i < n; ++i) {

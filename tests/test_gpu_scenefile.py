@@ -15,13 +15,14 @@ pytestmark = pytest.mark.gpu
 HERE = Path(__file__).resolve().parent
 
 
-@pytest.mark.parametrize("name", ["box.js", "emitters.js", "spheres.js", "textures.js", "points.js"])
-def test_scene_file_renders_like_the_oracle(cuda, oracle, name):
+@pytest.mark.parametrize("name,tess", [("box.js", None), ("emitters.js", None), ("spheres.js", (32, 17)),
+                                       ("spheres.js", None), ("textures.js", None), ("points.js", None)])
+def test_scene_file_renders_like_the_oracle(cuda, oracle, name, tess):
     # emitters.js: plane, triangle (two uv frames) and mesh lights, 4 light samples per vertex;
     # spheres.js: tessellated spheres (Phong, dielectric, a named sphere and its instance);
     # textures.js: kd / ks / bump maps from PNG and PPM files, plane, cube and mesh uvs;
     # points.js: omni and oriented point lights, omni plane and mesh emitters
-    sf = sceneloader.load(str(HERE / "scenes" / name), tessellate=(32, 17))
+    sf = sceneloader.load(str(HERE / "scenes" / name), tessellate=tess)  # spheres.js: analytic or tessellated
     r = sceneloader.path_tracer(sf)
     st = r.settings()
     mean_g, paths_g, _ = gpu_render_paths(cuda, sf.scene, st)

@@ -145,3 +145,52 @@ def test_shared_edges_and_vertices_are_watertight(cuda):
         hits, _ = gpu_trace(cuda, ds, rays)
         prims = np.ascontiguousarray(hits[:, 1]).view(np.int32)
         assert (prims < 0).sum() == 0, f"{(prims < 0).sum()} of {n} rays leaked"
+
+
+def test_analytic_spheres_closest_and_any(cuda, oracle):
+    # rays against a floor and analytic spheres (one rotated, one inside another's reach): the
+    # closest hit and the occlusion query through the C ABI against the oracle's restatement of
+    # Sphere::getIntersection / intersects
+    from milton_gb300.scene import SceneBuilder, camera, diffuse
+    rng = np.random.default_rng(23)
+    b = SceneBuilder()
+    m = b.material(diffuse(0.5))
+    h = 6.0
+    b.add("floor", np.array([[[-h, 0, h], [h, 0, h], [h, 0, -h]], [[-h, 0, h], [h, 0, -h], [-h, 0, -h]]],
+                            np.float32), None, m)
+    spheres = [((0.0, 1.0, 0.0), 1.0), ((2.0, 0.5, 1.0), 0.5), ((-1.5, 0.8, -1.0), 0.8), ((0.5, 2.6, 0.2), 0.3)]
+    ang = 0.7
+    rot = np.array([[np.cos(ang), 0, np.sin(ang)], [0, 1, 0], [-np.sin(ang), 0, np.cos(ang)]])
+    for k, (c, r) in enumerate(spheres):
+        b.add_sphere(c, r, m, rotation=rot if k == 1 else None)
+    s = b.build(camera(eye=(0, 2, 6), look=(0, -0.3, -1), up=(0, 1, 0), height_angle=40, aspect=1))
+    ds = pt.DeviceScene(s, pt.Accel(s))
+    n = 20000
+    o = rng.uniform([-4, 0.1, -4], [4, 4, 4], (n, 3))
+    tgt = np.array([c for c, _ in spheres])[rng.integers(0, 4, n)] + rng.normal(size=(n, 3)) * 0.7
+    d = tgt - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, np.zeros((n, 1)), d, np.full((n, 1), np.inf)], 1).astype(np.float32)
+    hits, _ = gpu_trace(cuda, ds, rays)
+    prims = np.ascontiguousarray(hits[:, 1]).view(np.int32)
+    # oracle: triangles through its kd traversal, spheres by Sphere::getIntersection
+    t_tri, p_tri, _, _ = oracle.trace_closest(oracle.Tree(s.tri_v), s.tri_v, s.tri_flags, rays)
+    t_ref, p_ref = np.asarray(t_tri, np.float64).copy(), np.asarray(p_tri).copy()
+    for k in range(len(spheres)):
+        ts = np.array([oracle.sphere_closest(s.spheres[k], rays[i, :3].astype(np.float64),
+                                             rays[i, 4:7].astype(np.float64)) for i in range(n)])
+        closer = ts < t_ref
+        t_ref[closer], p_ref[closer] = ts[closer], s.ntri + k
+    same = prims == p_ref
+    t_ok = np.where(np.isfinite(t_ref), np.abs(hits[:, 0] - t_ref) <= 1e-4 * np.maximum(1, t_ref), ~np.isfinite(hits[:, 0]))
+    # grazing rays (within FP32 of a tangent or of another surface) may differ
+    assert same.mean() >= 0.999 and t_ok[same].mean() >= 0.999, (same.mean(), t_ok[same].mean())
+    assert (prims >= s.ntri).sum() > n // 4  # the spheres are hit
+    # occlusion within the hit distance: occluded exactly when the closest hit is nearer
+    seg = rays.copy()
+    seg[:, 7] = np.where(np.isfinite(t_ref), t_ref * 0.5, 3.0)
+    occ = gpu_any(cuda, ds, seg)
+    assert (occ == 0).mean() >= 0.999  # nothing lies closer than half the closest hit
+    seg[:, 7] = np.where(np.isfinite(t_ref), t_ref * 1.01, 3.0)
+    occ = gpu_any(cuda, ds, seg)
+    assert (occ[np.isfinite(t_ref)] == 1).mean() >= 0.999

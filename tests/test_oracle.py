@@ -203,3 +203,19 @@ def test_point_light_known_answer(oracle):
     assert np.allclose(mean, want, rtol=1e-4), (mean.mean(), want)
     # one shadow ray per path for the point light, whatever noDirectSamples is
     assert st["shadow_rays"] == 2 * 2 * 4
+
+
+def test_sphere_intersection_known_answers(oracle):
+    # Sphere::getIntersection: unit-diameter sphere under T(c) R S(2r); the nearest root beyond
+    # EPSILON, else the far one (a ray from inside), else none
+    sp = np.array([1.0, 2.0, -3.0, 0.5, 0.0, 0.0, 0.0, 1.0], np.float32)
+    assert np.isclose(oracle.sphere_closest(sp, [1, 2, 0], [0, 0, -1]), 2.5)
+    assert np.isclose(oracle.sphere_closest(sp, [1, 2, -3], [0, 1, 0]), 0.5)
+    assert np.isinf(oracle.sphere_closest(sp, [1, 2.6, 0], [0, 0, -1]))
+    assert np.isinf(oracle.sphere_closest(sp, [1, 2, -4], [0, 0, -1]))  # sphere behind
+    # a grazing ray at distance 0.4 from the centre: chord half-length 0.3
+    assert np.isclose(oracle.sphere_closest(sp, [1, 2.4, 0], [0, 0, -1]), 3.0 - 0.3)
+    # a rotation does not move the surface
+    q = np.array([0.2, 0.4, -0.1, 0.8]); q /= np.linalg.norm(q)
+    sp2 = sp.copy(); sp2[4:8] = q
+    assert np.isclose(oracle.sphere_closest(sp2, [1, 2.4, 0], [0, 0, -1]), 2.7)

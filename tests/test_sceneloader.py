@@ -160,7 +160,9 @@ def test_camera_defaults_and_output_size():
 
 
 @pytest.mark.parametrize("body,extra,msg", [
-    ('"sphere" : { "radius" : 1 }', "", "not a triangle shape"),
+    ('"transform" : { "scale" : [1, 2, 1], "sphere" : { "radius" : 1 } }', "", "non-uniform scale"),
+    ('"material" : { "emitter" : { "type" : "omni" }, "sphere" : { } }', "", "emitting sphere"),
+    ('"cylinder" : { }', "", "not supported"),
     ('"material" : { "emitter" : { "type" : "oriented", "power" : 1 }, "cube" : { } }', "", "emitting cube"),
     ('"transform" : { "translate" : [0, 0, 0], "name" : "x", "plane" : { } }', "", "unknown key"),
     ('"triangle" : { }', '"renderer" : { "type" : "pathTracer" }, "renderer" : { "type" : "pathTracer" },',
@@ -271,11 +273,22 @@ def test_instances_copy_named_shapes():
         L.loads(_scene('"triangle" : { "name" : "a" }, "plane" : { "name" : "a" }'))
 
 
-def test_spheres_tessellate_only_on_request():
+def test_spheres_analytic_or_tessellated():
+    body = ('"transform" : { "translate" : [0, 1, 0], "rotate" : [0, 0, 0, 0, 1, 0, 90], '
+            '"sphere" : { "position" : [2, 0, 0], "radius" : 0.75 } }')
+    a = L.loads(_scene(body)).scene
+    # analytic: T(0, 1, 0) R_y(90) T(2, 0, 0) S(1.5): centre R (2, 0, 0) + (0, 1, 0) = (0, 1, -2)
+    assert a.ntri == 0 and len(a.spheres) == 1
+    assert np.allclose(a.spheres[0, :3], (0, 1, -2), atol=1e-6) and np.isclose(a.spheres[0, 3], 0.75)
+    # the record rotates world directions into the object frame: R^T (0, 0, -1) = (1, 0, 0)
+    from milton_gb300 import scene as Sc
+    q = a.spheres[0, 4:8].astype(np.float64)
+    u, w = q[:3], q[3]
+    v = np.array([0.0, 0.0, -1.0])
+    t = 2 * np.cross(u, v)
+    assert np.allclose(v + w * t + np.cross(u, t), (1, 0, 0), atol=1e-6)
     body = ('"transform" : { "translate" : [0, 1, 0], '
             '"sphere" : { "position" : [2, 0, 0], "radius" : 0.75 } }')
-    with pytest.raises(L.SceneFileError, match="not a triangle shape"):
-        L.loads(_scene(body))
     s = L.loads(_scene(body), tessellate=(16, 9)).scene
     assert s.ntri == 16 * 9 * 2 - 2 * 16
     # graph transform after the sphere's own T(position) S(2 radius) on a unit-diameter sphere
