@@ -219,3 +219,21 @@ def test_sphere_intersection_known_answers(oracle):
     q = np.array([0.2, 0.4, -0.1, 0.8]); q /= np.linalg.norm(q)
     sp2 = sp.copy(); sp2[4:8] = q
     assert np.isclose(oracle.sphere_closest(sp2, [1, 2.4, 0], [0, 0, -1]), 2.7)
+
+
+def test_oracle_matches_its_golden_fixtures(oracle):
+    # regression pins of the oracle's own outputs (tests/golden/make_golden.py); FP64 libm may
+    # differ in the last bits between hosts, hence the tolerance
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_golden as G
+    here = Path(__file__).resolve().parent / "golden"
+    for name, fn in (("oracle_plain.npz", G.plain_case), ("oracle_textured.npz", G.textured_case)):
+        want = np.load(here / name)
+        got = fn()
+        for k in want.files:
+            if want[k].dtype.kind == "f":
+                assert np.allclose(got[k], want[k], rtol=1e-9, atol=1e-12), (name, k)
+            else:
+                assert np.array_equal(got[k], want[k]), (name, k)
