@@ -93,6 +93,12 @@ typedef struct {
  *                                   more uniforms r1, r2, normal = interpolated vertex normals
  *                                   (Mesh::getPosition / getPoint, Mesh.cpp:436-448,
  *                                   MeshTriangle::getPosition, MeshTriangle.cpp:299-333)
+ *              MGPU_LIGHT_SPHERE    [1..4] the object-to-world quaternion, [5] the radius: a Milton
+ *                                   `Sphere` emitter at center, sampled as Sphere::getPosition does
+ *                                   (Sphere.cpp:114-121: x = clamp(tan((1 - u) / 2 pi)), y =
+ *                                   clamp(sin((1/2 - v) / pi) / 2), z = sqrt(1 - x^2 - y^2) in object
+ *                                   space, a patch off the sphere's surface), normal = the object
+ *                                   point's direction, area = pi (its object-space area, :131-134)
  *              MGPU_LIGHT_POINT     nothing more: a Milton `PointShape` at center, area 0, one
  *                                   light sample, no normal (cosine 1) and no triangles
  *                                   (DirectIllumination.cpp:90-130)
@@ -112,7 +118,7 @@ typedef struct {
  *   spheres    nsphere (at most MGPU_MAX_SPHERES) analytic Milton `Sphere`s beside the triangle
  *              soup, 8 floats each: center[3], radius, then the unit quaternion (x, y, z, w) that
  *              rotates world directions into the sphere's object frame (for its uvs); primitive
- *              id ntri + index, material sphere_mat[index]; they do not emit.  Every ray tests
+ *              id ntri + index, material sphere_mat[index], light sphere_light[index].  Every ray tests
  *              every sphere (Sphere::getIntersection, Sphere.cpp:17-48), so a scene of many
  *              spheres is better tessellated.                                               */
 typedef struct mgpu_texture mgpu_texture;
@@ -136,6 +142,7 @@ typedef struct {
   int32_t nsphere;
   const float *spheres;
   const int32_t *sphere_mat;
+  const int32_t *sphere_light;  /* NULL or nsphere light indices (-1 = not an emitter) */
 } mgpu_scene_desc;
 
 /* A material's image map (Material::getSample, Material.cpp:285-301, and the bump map of
@@ -172,6 +179,7 @@ struct mgpu_texture {
 #define MGPU_LIGHT_TRIANGLE 1
 #define MGPU_LIGHT_MESH 2
 #define MGPU_LIGHT_POINT 3
+#define MGPU_LIGHT_SPHERE 4
 
 /* Render parameters.  Defaults mirror Milton's PathTracer/DirectIllumination keys:
  * noDirectSamples 1, efficientDirect 1, no maximum depth, Russian roulette from depth 2

@@ -43,7 +43,8 @@ class SceneDesc(C.Structure):
                 ("materials", C.c_void_p), ("nlight", C.c_int32), ("lights", C.c_void_p),
                 ("light_ext", C.c_void_p), ("tri_uv", C.c_void_p), ("ntex", C.c_int32),
                 ("textures", C.POINTER(Texture)), ("background_tex", C.c_int32), ("background_le", C.c_float * 3),
-                ("nsphere", C.c_int32), ("spheres", C.c_void_p), ("sphere_mat", C.c_void_p)]
+                ("nsphere", C.c_int32), ("spheres", C.c_void_p), ("sphere_mat", C.c_void_p),
+                ("sphere_light", C.c_void_p)]
 
 
 class RenderParams(C.Structure):

@@ -371,7 +371,7 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
     if (!desc->light_ext) continue;
     const float *x = desc->light_ext + 16 * (size_t)i;
     memcpy(&lrec[32 * (size_t)i + 16], x, 16 * sizeof(float));
-    if (!(x[0] == 0.0f || x[0] == 1.0f || x[0] == 2.0f || x[0] == 3.0f))
+    if (!(x[0] == 0.0f || x[0] == 1.0f || x[0] == 2.0f || x[0] == 3.0f || x[0] == 4.0f))
       return fail(MGPU_E_INVALID, "mgpu_scene_create: unknown light type at light " + std::to_string(i));
     if (x[0] == 2.0f) {
       uint32_t first, count;
@@ -400,10 +400,12 @@ int mgpu_scene_create(const mgpu_scene_desc *desc, const mgpu_accel *accel, void
       return fail(MGPU_E_INVALID, "mgpu_scene_create: bad sphere " + std::to_string(i));
     sph[2 * i] = make_float4(q[0], q[1], q[2], q[3]);
     sph[2 * i + 1] = make_float4(q[4], q[5], q[6], q[7]);
-    int32_t mat = desc->sphere_mat[i], none = -1;
+    int32_t mat = desc->sphere_mat[i], li = desc->sphere_light ? desc->sphere_light[i] : -1;
+    if (li < -1 || li >= desc->nlight)
+      return fail(MGPU_E_INVALID, "mgpu_scene_create: light index out of range at sphere " + std::to_string(i));
     float4 a = make_float4(0, 0, 0, 0), b = a;
     memcpy(&a.w, &mat, 4);
-    memcpy(&b.w, &none, 4);
+    memcpy(&b.w, &li, 4);
     sph_shade[3 * i] = a;
     sph_shade[3 * i + 1] = b;
     sph_shade[3 * i + 2] = make_float4(0, 0, 0, 0);

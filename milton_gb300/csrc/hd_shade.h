@@ -62,13 +62,6 @@ MGPU_HD void env_uv(V3 w, float &u, float &v) {
   v = theta / -kPi + 0.5f;
 }
 
-// Rotation of v by the unit quaternion q = (x, y, z, w): v + 2 w (u x v) + 2 u x (u x v), u = q.xyz.
-MGPU_HD V3 quat_rotate(float qx, float qy, float qz, float qw, V3 v) {
-  const V3 u = v3(qx, qy, qz);
-  const V3 t = cross(u, v) * 2.0f;
-  return v + t * qw + cross(u, t);
-}
-
 // Sphere::_getUV (Sphere.cpp:78-85) of an object-space point p of the unit-diameter sphere:
 // u = 1 - atan2(z, x) / 2 pi, v = 1/2 - asin(2 y) / pi.
 MGPU_HD void sphere_uv(V3 p, float &u, float &v) {
@@ -92,10 +85,18 @@ MGPU_HD void tex_apply(Material &m, int slot, float r, float g, float b) {
 
 MGPU_HD bool is_specular(const Material &m) { return m.type == 2; }
 
+// Rotation of v by the unit quaternion q = (x, y, z, w): v + 2 w (u x v) + 2 u x (u x v), u = q.xyz.
+MGPU_HD V3 quat_rotate(float qx, float qy, float qz, float qw, V3 v) {
+  const V3 u = v3(qx, qy, qz);
+  const V3 t = cross(u, v) * 2.0f;
+  return v + t * qw + cross(u, t);
+}
+
 // Light: a Milton `Plane` under a transform (type 0), a standalone `Triangle` (type 1), a `Mesh`
-// (type 2) or a `PointShape` (type 3, area 0).  Record: 16 floats (center / v1, ex, ez, normal,
+// (type 2), a `PointShape` (type 3, area 0) or a `Sphere` (type 4: quaternion in the uv-frame
+// slots u0, v0, ax, ay, radius in bx).  Record: 16 floats (center / v1, ex, ez, normal,
 // area, Le) + 16 extension floats (type, triangle uv frame, mesh triangle run, [15] omni).
-constexpr int kLightPlane = 0, kLightTriangle = 1, kLightMesh = 2, kLightPoint = 3;
+constexpr int kLightPlane = 0, kLightTriangle = 1, kLightMesh = 2, kLightPoint = 3, kLightSphere = 4;
 constexpr uint32_t kMeshLightBlock = 0x4000u;  // RNG block of a mesh light sample's extra pair
 
 struct Light {
@@ -156,6 +157,17 @@ MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, V
     p = a * b0 + b * b1 + c * b2;
     n = normalize(nrm(t, 0) * b0 + nrm(t, 1) * b1 + nrm(t, 2) * b2);
     g = normalize(cross(b - a, c - a));
+  } else if (L.type == kLightSphere) {
+    // Sphere::getPosition (Sphere.cpp:114-121) in object space, under T(center) R S(2 radius);
+    // the normal is the object point's direction (Sphere::_getGeometricNormal).  The point lies
+    // off the sphere, as in the reference, so there is no surface to move the shadow ray off.
+    const float x = fminf(fmaxf(tanf((1.0f - u) / (2.0f * kPi)), -0.5f), 0.5f);
+    const float y = fminf(fmaxf(sinf((0.5f - v) / kPi) * 0.5f, -0.5f), 0.5f);
+    const V3 po = v3(x, y, sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y)));
+    const V3 pw = quat_rotate(L.u0, L.v0, L.ax, L.ay, po);  // uv-frame slots hold the quaternion
+    p = L.center + pw * (2.0f * L.bx);
+    n = normalize(pw);
+    g = v3(0.0f, 0.0f, 0.0f);
   } else if (L.type == kLightPoint) {
     // PointShape: the point itself, no normal (SurfacePoint's stand-in dot product is 1) and no
     // surface to move the shadow ray's end off

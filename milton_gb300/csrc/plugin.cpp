@@ -21,7 +21,7 @@ struct mgpu_renderer {
   int32_t bg_tex = 0;
   float bg_le[3] = {0, 0, 0};
   std::vector<float> sph;
-  std::vector<int32_t> sph_mat;
+  std::vector<int32_t> sph_mat, sph_light;
   bool has_scene = false, has_n = false, has_light = false, has_flags = false;
   int32_t nmat = 0, nlight = 0;
   float camera[16] = {0, 0, 0, 0, 0, -1, 0, 1, 0, 45, 1, 0, 0, 1, 0, 0};
@@ -71,6 +71,7 @@ struct mgpu_renderer {
     d.nsphere = (int32_t)sph_mat.size();
     d.spheres = sph.empty() ? nullptr : sph.data();
     d.sphere_mat = sph_mat.empty() ? nullptr : sph_mat.data();
+    d.sphere_light = sph_light.empty() ? nullptr : sph_light.data();
     return d;
   }
 };
@@ -144,6 +145,8 @@ int mgpu_renderer_set_scene(mgpu_renderer *r, const mgpu_scene_desc *d) {
     return bad("mgpu_renderer_set_scene: bad spheres");
   r->sph.assign(d->spheres, d->spheres + 8 * (size_t)std::max(d->nsphere, 0));
   r->sph_mat.assign(d->sphere_mat, d->sphere_mat + std::max(d->nsphere, 0));
+  if (d->sphere_light) r->sph_light.assign(d->sphere_light, d->sphere_light + std::max(d->nsphere, 0));
+  else r->sph_light.clear();
   r->has_scene = true;
   r->initted = false;
   return MGPU_OK;

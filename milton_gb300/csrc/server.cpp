@@ -40,7 +40,7 @@ struct SrvScene {
   int32_t bg_tex = 0;
   float bg_le[3] = {0, 0, 0};
   std::vector<float> sph;
-  std::vector<int32_t> sph_mat;
+  std::vector<int32_t> sph_mat, sph_light;
   int32_t nmat = 0, nlight = 0;
   // written by a build thread, read under the server mutex
   int state = kIdle;
@@ -74,6 +74,7 @@ struct SrvScene {
     d.nsphere = (int32_t)sph_mat.size();
     d.spheres = sph.empty() ? nullptr : sph.data();
     d.sphere_mat = sph_mat.empty() ? nullptr : sph_mat.data();
+    d.sphere_light = sph_light.empty() ? nullptr : sph_light.data();
     return d;
   }
 };
@@ -435,6 +436,7 @@ int mgpu_server_add_scene(mgpu_server *s, const mgpu_scene_desc *d, int32_t *sce
     if (d->nsphere > 0) {
       sc->sph.assign(d->spheres, d->spheres + 8 * (size_t)d->nsphere);
       sc->sph_mat.assign(d->sphere_mat, d->sphere_mat + d->nsphere);
+      if (d->sphere_light) sc->sph_light.assign(d->sphere_light, d->sphere_light + d->nsphere);
     }
   } catch (...) {
     return fail(MGPU_E_NOMEM, "mgpu_server_add_scene: out of host memory");

@@ -60,6 +60,7 @@ def _desc(scene: Scene) -> N.SceneDesc:
     d.nsphere = len(scene.spheres)
     d.spheres = N.ptr(scene.spheres) if len(scene.spheres) else None
     d.sphere_mat = N.ptr(scene.sphere_mat) if len(scene.spheres) else None
+    d.sphere_light = N.ptr(scene.sphere_light) if len(scene.spheres) else None
     d.background_tex = int(scene.background_tex)
     for k in range(3):
         d.background_le[k] = float(scene.background_le[k])

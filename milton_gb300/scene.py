@@ -22,6 +22,7 @@ A `Scene` holds exactly what crosses the C ABI (``mgpu_scene_desc``):
 * ``spheres``   (S, 8)    float32  analytic spheres beside the soup: center[3], radius, world-to-object
                                    rotation quaternion (x, y, z, w); primitive ids ntri + index
 * ``sphere_mat`` (S,)     int32    their material indices
+* ``sphere_light`` (S,)   int32    their light indices (-1 = not an emitter)
 * ``background_tex`` int           1 + index of the environment map (latitude-longitude), or 0
 * ``background_le``  (3,) float32  constant background radiance when background_tex is 0
 
@@ -202,6 +203,7 @@ class Scene:
     background_le: np.ndarray = field(default_factory=lambda: np.zeros(3, np.float32))
     spheres: np.ndarray = field(default_factory=lambda: np.zeros((0, 8), np.float32))
     sphere_mat: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    sphere_light: np.ndarray | None = None
 
     def __post_init__(self):
         self.tri_v = np.ascontiguousarray(self.tri_v, np.float32).reshape(-1, 3, 3)
@@ -239,6 +241,11 @@ class Scene:
         self.sphere_mat = np.ascontiguousarray(self.sphere_mat, np.int32).reshape(-1)
         if len(self.sphere_mat) != len(self.spheres):
             raise ValueError("sphere_mat needs one entry per sphere")
+        if self.sphere_light is None:
+            self.sphere_light = np.full(len(self.spheres), -1, np.int32)
+        self.sphere_light = np.ascontiguousarray(self.sphere_light, np.int32).reshape(-1)
+        if len(self.sphere_light) != len(self.spheres):
+            raise ValueError("sphere_light needs one entry per sphere")
         if len(self.spheres) and (self.sphere_mat.min() < 0 or self.sphere_mat.max() >= len(self.materials)):
             raise ValueError("sphere material index out of range")
         if not 0 <= self.background_tex <= len(self.textures):
@@ -269,6 +276,7 @@ class SceneBuilder:
         self.bg_le = np.zeros(3, np.float32)
         self.spheres: list[np.ndarray] = []
         self.sphere_mat: list[int] = []
+        self.sphere_light: list[int] = []
         self.materials: list[np.ndarray] = []
         self.lights: list[np.ndarray] = []
         self.light_ext: list[np.ndarray] = []
@@ -279,16 +287,32 @@ class SceneBuilder:
         self.materials.append(np.asarray(rec, np.float32))
         return len(self.materials) - 1
 
-    def add_sphere(self, center, radius: float, mat: int, rotation=None) -> int:
+    def add_sphere(self, center, radius: float, mat: int, rotation=None, radiance=None, omni: bool = False) -> int:
         """An analytic sphere (Milton's Sphere: its centre, radius and object frame, given by the
-        3 x 3 rotation from object to world, identity by default).  Returns its index among the
-        spheres (its primitive id is the triangle count plus this index)."""
+        3 x 3 rotation from object to world, identity by default).  radiance: an emitting sphere
+        of that Le (a light of type 4, area pi).  Returns its index among the spheres (its
+        primitive id is the triangle count plus this index)."""
+        R = np.eye(3) if rotation is None else np.asarray(rotation, np.float64)
         rec = np.zeros(8, np.float32)
         rec[0:3] = center
         rec[3] = radius
-        rec[4:8] = quat_from_matrix(np.eye(3) if rotation is None else np.asarray(rotation, np.float64).T)
+        rec[4:8] = quat_from_matrix(R.T)
+        li = -1
+        if radiance is not None:
+            lrec = np.zeros(16, np.float32)
+            lrec[0:3] = center
+            lrec[9:12] = (0.0, 0.0, 1.0)
+            lrec[12] = np.pi  # Sphere::_getSurfaceArea: the object-space area
+            lrec[13:16] = np.broadcast_to(np.asarray(radiance, np.float64), 3)
+            ext = np.zeros(16, np.float32)
+            ext[0] = 4
+            ext[1:5] = quat_from_matrix(R)
+            ext[5] = radius
+            ext[15] = 1.0 if omni else 0.0
+            li = self.add_light(lrec, ext)
         self.spheres.append(rec)
         self.sphere_mat.append(int(mat))
+        self.sphere_light.append(li)
         return len(self.spheres) - 1
 
     def background(self, tex: int = 0, le=(0.0, 0.0, 0.0)) -> None:
@@ -395,7 +419,7 @@ class SceneBuilder:
         return Scene(
             tri_uv=tri_uv, textures=list(self.textures), background_tex=self.bg_tex, background_le=self.bg_le,
             spheres=np.stack(self.spheres) if self.spheres else np.zeros((0, 8), np.float32),
-            sphere_mat=np.asarray(self.sphere_mat, np.int32),
+            sphere_mat=np.asarray(self.sphere_mat, np.int32), sphere_light=np.asarray(self.sphere_light, np.int32),
             tri_v=cat(self.v, (0, 3, 3), np.float32), tri_n=cat(self.n, (0, 3, 3), np.float32),
             tri_mat=cat(self.mat, (0,), np.int32), tri_light=cat(self.light, (0,), np.int32),
             tri_flags=cat(self.flags, (0,), np.uint32),

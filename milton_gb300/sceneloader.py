@@ -1268,8 +1268,6 @@ class _Flattener:
         if sh.kind == "sphere":
             # an analytic sphere beside the soup: the object frame of T R S must be a similarity
             # (a uniformly scaled rotation) for the centre / radius / rotation record
-            if emitter != "null":
-                raise SceneFileError("an emitting sphere is not supported by the GPU path")
             msph = trans @ sh.local
             A = msph[:3, :3]
             k = float(np.linalg.norm(A[:, 0]))
@@ -1278,7 +1276,14 @@ class _Flattener:
                 raise SceneFileError("a sphere under a non-uniform scale or a reflection is not supported by the "
                                      "GPU path as an analytic sphere (load with tessellate=(nu, nv))")
             mi = self.material_record(self.active)
-            self.b.add_sphere(msph[:3, 3], 0.5 * k, mi, rotation=A / k)
+            if emitter != "null" and self.b.materials[mi][13] != 0:
+                raise SceneFileError("a bump-mapped emitter is not supported by the GPU path")
+            radiance = None
+            if emitter != "null":
+                # Sphere::_getSurfaceArea is pi whatever the transform (Sphere.cpp:131-134)
+                power = np.broadcast_to(np.asarray(props.get("power", (1.0, 1.0, 1.0)), np.float64), 3)
+                radiance = power / (math.pi * per_sr)
+            self.b.add_sphere(msph[:3, 3], 0.5 * k, mi, rotation=A / k, radiance=radiance, omni=emitter == "omni")
             return
         if sh.kind == "point":
             # PointShape (PointShape.cpp): its position; area 0, so Le = power / pi or power / 4 pi

@@ -193,6 +193,7 @@ typedef struct {
   int nsph;            /* analytic spheres: primitive ids ntri .. ntri + nsph - 1 */
   const float *sph;    /* 8 floats each: center, radius, world-to-object quaternion */
   const int32_t *sph_mat;
+  const int32_t *sph_light; /* or NULL */
 } orc_scene;
 
 static inline v3 tri_vert(const orc_scene *s, int64_t t, int k) {
@@ -1275,6 +1276,18 @@ static void light_point(const orc_render_ctx *c, const orc_path *ph, int depth, 
     if (sum > 0) { b0 = r1 / sum; b1 = v / sum; b2 = r2 / sum; }
     *pos = vadd(vadd(vmul(tri_vert(s, t, 0), b0), vmul(tri_vert(s, t, 1), b1)), vmul(tri_vert(s, t, 2), b2));
     *nrm = vnorm(vadd(vadd(vmul(tri_nrm(s, t, 0), b0), vmul(tri_nrm(s, t, 1), b1)), vmul(tri_nrm(s, t, 2), b2)));
+  } else if (L->type == 4) {
+    /* Sphere::getPosition (Sphere.cpp:114-121) in object space under T(center) R S(2 radius),
+     * normal = the object point's direction (Sphere::_getGeometricNormal); the quaternion
+     * (object to world) sits in the uv-frame slots, the radius in bx */
+    double x = tan((1.0 - u) / (2 * ORC_PI)), y = sin((0.5 - v) / ORC_PI) * 0.5;
+    x = x < -0.5 ? -0.5 : (x > 0.5 ? 0.5 : x);
+    y = y < -0.5 ? -0.5 : (y > 0.5 ? 0.5 : y);
+    double zz = 1 - x * x - y * y;
+    float q[4] = {(float)L->u0, (float)L->v0, (float)L->ax, (float)L->ay};
+    v3 pw = qrot(q, V(x, y, sqrt(zz > 0 ? zz : 0)));
+    *pos = vadd(L->center, vmul(pw, 2 * L->bx));
+    *nrm = vnorm(pw);
   } else if (L->type == 3) {
     *pos = L->center; /* PointShape: no normal (SurfacePoint.h:130-151: its dot product is 1) */
     *nrm = V(0, 0, 0);
@@ -1371,7 +1384,7 @@ static void evaluate(const orc_render_ctx *c, orc_path *ph, v3 o, v3 d, int dept
   }
   orc_bsdf b = {m, ns, d, ph->ior_index + 1};
   if (is_specular(m)) ph->specular = 1;
-  int li = (s->light && !on_sphere) ? s->light[tri] : -1;
+  int li = on_sphere ? (s->sph_light ? s->sph_light[tri - s->ntri] : -1) : (s->light ? s->light[tri] : -1);
   if (li >= 0) {
     const orc_light *L = &s->lights[li];
     double le = (L->omni || vdot(ns, vneg(d)) > 0) ? 1.0 : 0.0; /* OrientedEmitter on the hit's normal */
@@ -1489,7 +1502,7 @@ int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat,
                const uint32_t *flags, int nmat, const float *mats, int nlight, const float *lights,
                const float *light_ext, const float *tri_uv, int ntex, const float *tex_params,
                const float *const *tex_rgb, const float *bg, int nsph, const float *sph, const int32_t *sph_mat,
-               const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed, uint32_t stream,
+               const int32_t *sph_light, const orc_tree *tr, const float *camera, const int32_t *ip, uint64_t seed, uint32_t stream,
                double *film_sum, double *path_out, uint64_t *stats_out) {
   orc_scene *s = scene_from_arrays(ntri, v, n, mat, light, flags, nmat, mats, nlight, lights, light_ext);
   s->uv = tri_uv;
@@ -1503,6 +1516,7 @@ int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat,
   s->nsph = nsph;
   s->sph = sph;
   s->sph_mat = sph_mat;
+  s->sph_light = sph_light;
   orc_render_ctx c;
   c.s = s;
   c.tr = tr;

@@ -34,7 +34,7 @@ def load() -> C.CDLL:
     lib.orc_trace_any.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp]
     lib.orc_render.restype = C.c_int
     lib.orc_render.argtypes = [i64, vp, vp, vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_int, vp, vp, vp,
-                               C.c_int, vp, vp, vp, vp, vp, u64, u32, vp, vp, vp]
+                               C.c_int, vp, vp, vp, vp, vp, vp, u64, u32, vp, vp, vp]
     lib.orc_sphere_closest.restype = C.c_double
     lib.orc_sphere_closest.argtypes = [vp, vp, vp]
     lib.orc_background.argtypes = [vp, vp, vp, vp, vp]
@@ -145,13 +145,15 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
     tparams, trgb = texture_params(textures)
     sph = np.ascontiguousarray(getattr(scene, "spheres", np.zeros((0, 8))), np.float32).reshape(-1, 8)
     sph_mat = np.ascontiguousarray(getattr(scene, "sphere_mat", np.zeros(0)), np.int32)
+    sph_light = getattr(scene, "sphere_light", None)
+    sph_light = None if sph_light is None else np.ascontiguousarray(sph_light, np.int32)
     bg = np.zeros(4, np.float32)
     bg[0] = getattr(scene, "background_tex", 0)
     bg[1:4] = getattr(scene, "background_le", (0.0, 0.0, 0.0))
     lib.orc_render(scene.ntri, _p(scene.tri_v), _p(scene.tri_n), _p(scene.tri_mat), _p(scene.tri_light),
                    _p(scene.tri_flags), len(scene.materials), _p(scene.materials), len(scene.lights), _p(lights),
                    _p(ext), _p(uv), len(textures), _p(tparams), C.cast(trgb, C.c_void_p), _p(bg), len(sph), _p(sph),
-                   _p(sph_mat), tree.h, _p(cam), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
+                   _p(sph_mat), _p(sph_light), tree.h, _p(cam), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
     mean = film[r0:r1] / max(sample_count, 1)
     if per_path:
         paths = paths.reshape(height, width, sample_count, 3)[r0:r1]

@@ -295,3 +295,30 @@ def test_scenes_without_geometry_or_lights(cuda):
                    tri_flags=s.tri_flags, materials=s.materials, lights=np.zeros((0, 16), np.float32), camera=s.camera)
     mean, _, _ = gpu_render_paths(cuda, dark, pt.RenderSettings(16, 16, 4, max_depth=5, rr_start_depth=3, seed=1))
     assert np.all(mean == 0)
+
+
+def test_emitting_and_plain_spheres_per_path(cuda, oracle):
+    # analytic spheres in the plain box: a glass one, a Phong one, and an emitting one whose light
+    # samples follow Sphere::getPosition (a patch off its surface, area pi) and whose surface
+    # emits at hits
+    from milton_gb300.scene import SceneBuilder, camera, dielectric, diffuse, phong
+    s0 = scenegen.plain(4)
+    b = SceneBuilder()
+    for name, first, count in s0.shapes:
+        if name == "light":
+            continue
+        mi = b.material(s0.materials[s0.tri_mat[first]])
+        b.add(name, s0.tri_v[first:first + count], s0.tri_n[first:first + count], mi)
+    b.add_sphere((-0.4, 0.35, 0.3), 0.3, b.material(dielectric(1.5)))
+    b.add_sphere((0.45, 0.25, -0.2), 0.25, b.material(phong(0.3, 0.4, 40.0)))
+    rot = np.array([[0, 0, 1], [0, 1, 0], [-1, 0, 0]], np.float64)  # object +z toward world -x
+    b.add_sphere((0.2, 1.5, 0.0), 0.15, b.material(diffuse(0.5)), rotation=rot, radiance=[20.0, 18.0, 15.0])
+    s = b.build(s0.camera)
+    assert len(s.lights) == 1 and s.light_ext[0, 0] == 4 and s.sphere_light.tolist() == [-1, -1, 0]
+    st = pt.RenderSettings(40, 40, 16, no_direct_samples=2, max_depth=5, rr_start_depth=3, seed=13)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st)
+    mean_o, paths_o, _ = oracle.render(s, oracle.Tree(s.tri_v), 40, 40, 16, nds=2, max_depth=5, rr_start=3,
+                                       seed=13, per_path=True)
+    agree = _path_agreement(paths_g, paths_o)
+    print(f"spheres: path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
+    assert agree >= 0.97 and mean_g.mean() > 0.01

@@ -161,7 +161,6 @@ def test_camera_defaults_and_output_size():
 
 @pytest.mark.parametrize("body,extra,msg", [
     ('"transform" : { "scale" : [1, 2, 1], "sphere" : { "radius" : 1 } }', "", "non-uniform scale"),
-    ('"material" : { "emitter" : { "type" : "omni" }, "sphere" : { } }', "", "emitting sphere"),
     ('"cylinder" : { }', "", "not supported"),
     ('"material" : { "emitter" : { "type" : "oriented", "power" : 1 }, "cube" : { } }', "", "emitting cube"),
     ('"transform" : { "translate" : [0, 0, 0], "name" : "x", "plane" : { } }', "", "unknown key"),
@@ -326,3 +325,13 @@ def test_per_channel_ior_is_dispersion():
     d, g = s.materials[s.tri_mat[0]], s.materials[s.tri_mat[1]]
     assert np.allclose([d[8], d[14], d[15]], [1.4, 1.5, 1.6])
     assert g[8] == np.float32(1.5) and g[14] == 0 and g[15] == 0
+
+
+def test_emitting_sphere_light_record():
+    s = L.loads(_scene('"material" : { "emitter" : { "type" : "oriented", "power" : [3, 6, 9] }, '
+                       '"transform" : { "translate" : [1, 2, 3], "sphere" : { "radius" : 0.5 } } }')).scene
+    assert len(s.spheres) == 1 and len(s.lights) == 1 and s.sphere_light.tolist() == [0]
+    assert s.light_ext[0, 0] == 4 and np.isclose(s.light_ext[0, 5], 0.5) and np.isclose(s.lights[0, 12], math.pi)
+    # Le = power / (area pi) with the object-space area pi (Sphere::_getSurfaceArea)
+    assert np.allclose(s.lights[0, 13:16], np.array([3, 6, 9]) / math.pi ** 2)
+    assert np.allclose(s.lights[0, 0:3], (1, 2, 3))
