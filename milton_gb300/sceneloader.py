@@ -31,13 +31,13 @@ which material are kept as the reference has them:
 
 Emitters: a unit plane becomes a parallelogram light, a Triangle a triangle light with its uv
 frame and object-space area, a mesh one mesh light over its triangles (include/mgpu.h,
-``light_ext``).  What the GPU path cannot render is refused with a SceneFileError naming the
-element: analytic shapes other than planes, cubes and points (sphere, cylinder, cone, blob),
+``light_ext``), a sphere a sphere light sampled as Sphere::getPosition does.  What the GPU path
+cannot render is refused with a SceneFileError naming the element: cylinders, cones and blobs,
 emitting cubes, oriented backgrounds, bump-mapped emitters, per-channel Phong exponents.  A
 per-channel IOR disperses: a path refracts with its colour channel's IOR.
 Emitters are oriented (one-sided, power / (area pi)) or omni (both sides, power / (area 4 pi))
-on planes, triangles and meshes, and point lights (a "point" shape with either emitter: one
-light sample, no area).  A scene's background is taken: an environment map
+on planes, triangles, meshes and spheres, and point lights (a "point" shape with either emitter:
+one light sample, no area).  A scene's background is taken: an environment map
 (latitude-longitude image: PNG, PPM / PGM or Radiance HDR) or an omni background's constant
 radiance, added where a ray leaves the scene.  Image maps are taken: a material's kd / ks / transparency given as a file name and
 its bumpMap become textures (PNG, PPM / PGM) with the material's filter, repeatU / repeatV and
@@ -1353,7 +1353,7 @@ class _Flattener:
             return
         if emitter != "null" and sh.kind != "mesh":
             raise SceneFileError(f"an emitting {sh.kind} is not supported by the GPU path (emitters must be "
-                                 "planes, triangles or meshes)")
+                                 "planes, triangles, meshes, spheres or points)")
         if sh.kind == "cube":
             tris, nrms, uvs = [], [], []
             for n_obj, q in _CUBE_FACES:
