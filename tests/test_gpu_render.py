@@ -322,3 +322,25 @@ def test_emitting_and_plain_spheres_per_path(cuda, oracle):
     agree = _path_agreement(paths_g, paths_o)
     print(f"spheres: path agreement {agree:.5f}, mean {mean_g.mean():.5f} / {mean_o.mean():.5f}")
     assert agree >= 0.97 and mean_g.mean() > 0.01
+
+
+def test_large_frame_and_many_passes(cuda, oracle):
+    # a 4096 x 4096 frame (16.8 M paths in one call: several waves when the wave is capped) and a
+    # tiny one with 1024 passes: a band of rows and every pixel match the oracle's paths
+    s = scenegen.plain(5)
+    ds = pt.DeviceScene(s, pt.Accel(s))
+    f = pt.Film(4096, 4096)
+    st = pt.RenderSettings(4096, 4096, 1, max_depth=5, rr_start_depth=3, seed=17, wave_paths=1 << 22)
+    pt.render(ds, st, f)
+    img = f.mean()
+    mean_o, _, _ = oracle.render(s, oracle.Tree(s.tri_v), 4096, 4096, 1, max_depth=5, rr_start=3, seed=17,
+                                 rows=(2048, 2052))
+    band = img[2048:2052]
+    close = np.abs(band - mean_o) <= 1e-4 + 2e-3 * np.maximum(np.abs(band), np.abs(mean_o))
+    assert np.all(close, axis=-1).mean() >= 0.98
+    st = pt.RenderSettings(3, 2, 1024, max_depth=5, rr_start_depth=3, seed=19)
+    mean_g, paths_g, _ = gpu_render_paths(cuda, s, st)
+    mean_o, paths_o, _ = oracle.render(s, oracle.Tree(s.tri_v), 3, 2, 1024, max_depth=5, rr_start=3, seed=19,
+                                       per_path=True)
+    assert _path_agreement(paths_g, paths_o) >= 0.98
+    assert np.allclose(mean_g, mean_o, rtol=2e-3, atol=1e-4)
