@@ -78,3 +78,37 @@ def test_batch_progressive_and_unlimited_depth(cuda, scenes):
     b.add(ds, st, f_b)
     b.render()
     assert np.array_equal(f_b.raw(), f_solo.raw())
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_batch_mixing_image_maps_spheres_and_plain_scenes(cuda, use_graph):
+    # waves that mix scenes with image maps and a background, scenes with analytic spheres and
+    # plain ones run the kernel variants that carry those branches; every film still equals its
+    # own render
+    from milton_gb300.scene import SceneBuilder, dielectric, diffuse
+    tex = scenegen.textured(6)
+    tex.background_le = np.array([0.2, 0.3, 0.4], np.float32)
+    s0 = scenegen.plain(7)
+    b = SceneBuilder()
+    for name, first, count in s0.shapes:
+        b.add(name, s0.tri_v[first:first + count], s0.tri_n[first:first + count],
+              b.material(s0.materials[s0.tri_mat[first]]),
+              light=int(s0.tri_light[first]) if s0.tri_light[first] >= 0 else -1)
+    for rec, ext in zip(s0.lights, s0.light_ext):
+        b.add_light(rec, ext)
+    b.add_sphere((0.0, 0.4, 0.0), 0.35, b.material(dielectric(1.5)))
+    b.add_sphere((0.5, 1.2, -0.4), 0.1, b.material(diffuse(0.2)), radiance=5.0)
+    sph = b.build(s0.camera)
+    plain = scenegen.plain(8)
+    reqs = []
+    for k, (s, (w, h, spp)) in enumerate(zip((tex, sph, plain, tex), ((40, 32, 8), (48, 40, 8), (32, 32, 4), (24, 24, 16)))):
+        ds = pt.DeviceScene(s, pt.Accel(s))
+        reqs.append((ds, pt.RenderSettings(w, h, spp, max_depth=5, rr_start_depth=3, seed=50 + k, stream_id=k)))
+    want = _solo(reqs)
+    batch = pt.Batch(wave_paths=12000, use_graph=use_graph)
+    films = [pt.Film(st.width, st.height) for _, st in reqs]
+    for (ds, st), f in zip(reqs, films):
+        batch.add(ds, st, f)
+    batch.render()
+    for f, w in zip(films, want):
+        assert np.array_equal(f.raw(), w)
