@@ -165,3 +165,30 @@ def test_replay_reports_latency(cuda):
         for v in infos.values():
             assert v["t_arrival"] <= v["t_admit"] <= v["t_done"]
         assert srv.stats()["film_bytes"] == 0  # every film released
+
+
+def test_served_textured_and_sphere_scenes_equal_plain_renders(cuda):
+    # the service owns copies of image maps, uvs, backgrounds and spheres: served images of such
+    # scenes equal their plain renders with the same sample counts
+    from milton_gb300.scene import SceneBuilder, dielectric
+    tex = scenegen.textured(9)
+    tex.background_le = np.array([0.1, 0.2, 0.3], np.float32)
+    b = SceneBuilder()
+    s0 = scenegen.plain(9)
+    for name, first, count in s0.shapes:
+        b.add(name, s0.tri_v[first:first + count], s0.tri_n[first:first + count],
+              b.material(s0.materials[s0.tri_mat[first]]),
+              light=int(s0.tri_light[first]) if s0.tri_light[first] >= 0 else -1)
+    for rec, ext in zip(s0.lights, s0.light_ext):
+        b.add_light(rec, ext)
+    b.add_sphere((0.1, 0.4, 0.2), 0.3, b.material(dielectric([1.4, 1.5, 1.7])))
+    sph = b.build(s0.camera)
+    scenes = [tex, sph]
+    jobs = [(0, 32, 4, 16, 0.0), (1, 40, 4, 16, 0.0), (0, 24, 1, 4, 0.0)]
+    served, _, _ = _run(scenes, jobs)
+    for k, ((si, side, spp, mx, _), (info, img)) in enumerate(zip(jobs, served)):
+        st = _settings(k, side, spp)
+        st.sample_count = info["spp_done"]
+        f = pt.Film(side, side)
+        pt.render(pt.DeviceScene(scenes[si], pt.Accel(scenes[si])), st, f)
+        assert info["spp_done"] == mx and np.array_equal(f.mean(), img)
