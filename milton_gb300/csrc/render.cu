@@ -39,7 +39,8 @@ constexpr int kCtrFetchExt = 2 * (kHardCap + 8);   // work counters of the persi
 constexpr int kCtrFetchSh = 3 * (kHardCap + 8);    // ... and of the persistent shadow kernel
 constexpr int kCtrTrunc = 4 * (kHardCap + 8);
 constexpr int kNumCounters = kCtrTrunc + 8;
-constexpr int kBins = 4096;             // queue binning keys
+constexpr int kBinBits = 13;           // queue binning keys: 2^13 bins
+constexpr int kBins = 1 << kBinBits;
 constexpr double kAutoWaveBytes = 40e9;  // workspace budget of an automatic wave
 #ifndef MGPU_TRAV_MIN_BLOCKS
 #define MGPU_TRAV_MIN_BLOCKS 12
@@ -211,10 +212,10 @@ __device__ __forceinline__ Light load_light(const JobArgs &J, int i) {
   return light_from(l, l + 16);
 }
 
-// Binning keys (kBins = 4096).  Ray coherence: rays of one warp should start close together
+// Binning keys (kBins = 8192).  Ray coherence: rays of one warp should start close together
 // and head the same way, so that they visit the same nodes.  Keys combine the direction
 // octant (extension rays) or the light index (shadow rays) with the Morton code of the
-// origin's cell in a 16x16x16 grid over the scene bounds.
+// origin's cell in a 16x16x16 grid over the scene bounds (the top bits of it that fit).
 __device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> every third bit
   return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
 }
@@ -234,7 +235,7 @@ __device__ __forceinline__ uint32_t morton12(const SceneView &s, V3 p) {
 
 __device__ __forceinline__ uint32_t ext_key(const JobArgs &J, V3 o, V3 d) {
   uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-  return (oct << 9) | (morton12(J.view, o) >> 3);
+  return (oct << (kBinBits - 3)) | (morton12(J.view, o) >> (15 - kBinBits));
 }
 
 __device__ __forceinline__ uint32_t sh_key(const JobArgs &J, int light, V3 o) {
@@ -1010,7 +1011,7 @@ static JobArgs job_args(const Job &j) {
   while (nlp < std::min(sc->nlight, 16)) nlp <<= 1;
   int lb = 0;
   while ((1 << lb) < nlp) ++lb;
-  J.sh_cell_bits = 12 - lb;  // light index in the top bits, origin cell below
+  J.sh_cell_bits = std::min(12, kBinBits - lb);  // light index in the top bits, origin cell below
   return J;
 }
 
