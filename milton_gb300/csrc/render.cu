@@ -39,8 +39,9 @@ constexpr int kCtrFetchExt = 2 * (kHardCap + 8);   // work counters of the persi
 constexpr int kCtrFetchSh = 3 * (kHardCap + 8);    // ... and of the persistent shadow kernel
 constexpr int kCtrTrunc = 4 * (kHardCap + 8);
 constexpr int kNumCounters = kCtrTrunc + 8;
-constexpr int kBinBits = 13;           // queue binning keys: 2^13 bins
+constexpr int kBinBits = 14;           // queue binning keys: 2^14 bins
 constexpr int kBins = 1 << kBinBits;
+constexpr int kBinSmem = kBins * 4;    // dynamic shared memory of a sorting block
 constexpr double kAutoWaveBytes = 40e9;  // workspace budget of an automatic wave
 #ifndef MGPU_TRAV_MIN_BLOCKS
 #define MGPU_TRAV_MIN_BLOCKS 12
@@ -212,34 +213,38 @@ __device__ __forceinline__ Light load_light(const JobArgs &J, int i) {
   return light_from(l, l + 16);
 }
 
-// Binning keys (kBins = 8192).  Ray coherence: rays of one warp should start close together
+// Binning keys (kBins = 16384).  Ray coherence: rays of one warp should start close together
 // and head the same way, so that they visit the same nodes.  Keys combine the direction
 // octant (extension rays) or the light index (shadow rays) with the Morton code of the
-// origin's cell in a 16x16x16 grid over the scene bounds (the top bits of it that fit).
+// origin's cell in a 32x32x32 grid over the scene bounds (the top bits of it that fit).
 __device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> every third bit
   return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
 }
 
-__device__ __forceinline__ uint32_t morton12(const SceneView &s, V3 p) {
+__device__ __forceinline__ uint32_t spread5(uint32_t v) {  // 5 bits -> every third bit
+  return spread4(v & 15u) | ((v & 16u) << 8);
+}
+
+__device__ __forceinline__ uint32_t morton15(const SceneView &s, V3 p) {
   uint32_t c[3];
   const float pp[3] = {p.x, p.y, p.z};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     float ext = s.bmax[k] - s.bmin[k];
     float f = ext > 0.0f ? (pp[k] - s.bmin[k]) / ext : 0.0f;
-    int q = (int)(f * 16.0f);
-    c[k] = (uint32_t)min(max(q, 0), 15);
+    int q = (int)(f * 32.0f);
+    c[k] = (uint32_t)min(max(q, 0), 31);
   }
-  return (spread4(c[0]) << 2) | (spread4(c[1]) << 1) | spread4(c[2]);
+  return (spread5(c[0]) << 2) | (spread5(c[1]) << 1) | spread5(c[2]);
 }
 
 __device__ __forceinline__ uint32_t ext_key(const JobArgs &J, V3 o, V3 d) {
   uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-  return (oct << (kBinBits - 3)) | (morton12(J.view, o) >> (15 - kBinBits));
+  return (oct << (kBinBits - 3)) | (morton15(J.view, o) >> (18 - kBinBits));
 }
 
 __device__ __forceinline__ uint32_t sh_key(const JobArgs &J, int light, V3 o) {
-  uint32_t cell = morton12(J.view, o) >> (12 - J.sh_cell_bits);
+  uint32_t cell = morton15(J.view, o) >> (15 - J.sh_cell_bits);
   return (((uint32_t)light << J.sh_cell_bits) | cell) & (kBins - 1);
 }
 
@@ -568,7 +573,7 @@ __global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_shadow(RenderArgs a,
 // range reservations (one global atomic per block chunk and non-empty bin)
 __global__ void __launch_bounds__(256) k_bin_hist(const uint32_t *__restrict__ keys, const uint32_t *count,
                                                  uint32_t *__restrict__ hist) {
-  __shared__ uint32_t h[kBins];
+  extern __shared__ uint32_t h[];  // kBins
   for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
   __syncthreads();
   const uint32_t n = *count;
@@ -607,9 +612,9 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const uint32_t *__restrict_
                                                     const float4 *__restrict__ in1, const float4 *__restrict__ in2,
                                                     float4 *__restrict__ out0, float4 *__restrict__ out1,
                                                     float4 *__restrict__ out2) {
-  constexpr int kPer = 16;                 // entries per thread per chunk
+  constexpr int kPer = 32;                 // entries per thread per chunk
   constexpr int kChunk = 256 * kPer;
-  __shared__ uint32_t h[kBins];
+  extern __shared__ uint32_t h[];  // kBins
   const uint32_t n = *count;
   for (uint32_t c0 = blockIdx.x * kChunk; c0 < n; c0 += gridDim.x * kChunk) {
     for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
@@ -1011,7 +1016,7 @@ static JobArgs job_args(const Job &j) {
   while (nlp < std::min(sc->nlight, 16)) nlp <<= 1;
   int lb = 0;
   while ((1 << lb) < nlp) ++lb;
-  J.sh_cell_bits = std::min(12, kBinBits - lb);  // light index in the top bits, origin cell below
+  J.sh_cell_bits = std::min(15, kBinBits - lb);  // light index in the top bits, origin cell below
   return J;
 }
 
@@ -1171,6 +1176,19 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   const int g_shw = grid_for((const void *)kshw, 0);
   const int g_acc = grid_for((const void *)k_accumulate, 0);
   const int g_bin = device_sm_count() * 4;
+  {
+    // the sorting blocks hold kBins counters in shared memory, above the 48 KB default
+    static std::once_flag once;
+    static cudaError_t smem_rc = cudaSuccess;
+    std::call_once(once, [] {
+      const void *kerns[] = {(const void *)k_bin_hist, (const void *)k_bin_scatter<2>, (const void *)k_bin_scatter<3>};
+      for (const void *kf : kerns) {
+        cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, kBinSmem);
+        if (e != cudaSuccess && smem_rc == cudaSuccess) smem_rc = e;
+      }
+    });
+    MGPU_CUDA(smem_rc);
+  }
   const int bin_ext = g_tune.bin_extension.load(), bin_sh = g_tune.bin_shadow.load();
   const int64_t bin_min = g_tune.bin_min_paths.load();
 
@@ -1246,18 +1264,18 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
           m = pf.begin(kProfBin, st);
           if (a.bin_sh) {
             cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st);
-            k_bin_hist<<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->hist);
+            k_bin_hist<<<g_bin, 256, kBinSmem, st>>>(w->skey, a.counters + kCtrNee + b, w->hist);
             k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
-            k_bin_scatter<2><<<g_bin, 256, 0, st>>>(w->skey, a.counters + kCtrNee + b, w->cursor, w->so_u, w->sd_u,
+            k_bin_scatter<2><<<g_bin, 256, kBinSmem, st>>>(w->skey, a.counters + kCtrNee + b, w->cursor, w->so_u, w->sd_u,
                                                     nullptr, w->so, w->sd, nullptr);
             launches += 3;
           }
           if (a.bin_ext && b + 1 < max_b) {
             const int nx = (b + 1) & 1;
             cudaMemsetAsync(w->hist, 0, kBins * sizeof(uint32_t), st);
-            k_bin_hist<<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->hist);
+            k_bin_hist<<<g_bin, 256, kBinSmem, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->hist);
             k_bin_scan<<<1, 1024, 0, st>>>(w->hist, w->cursor);
-            k_bin_scatter<3><<<g_bin, 256, 0, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->cursor, w->qo_u,
+            k_bin_scatter<3><<<g_bin, 256, kBinSmem, st>>>(w->qkey, a.counters + kCtrRay + b + 1, w->cursor, w->qo_u,
                                                     w->qd_u, w->qt_u, w->qo[nx], w->qd[nx], w->qt[nx]);
             launches += 3;
           }
