@@ -15,8 +15,10 @@ Printed JSON line (rank 0):
               HBM copy bandwidth
   cpu_baseline  the FP64 oracle (port of Milton's PathTracer) on a bounded pixel subset
 
-`--impl reference` times the CPU implementation of the path (the oracle port; Milton itself
-does not build here) on the same workload and prints its own line.
+`--impl reference` times the CPU implementation of the path -- the FP64 oracle port of Milton's
+PathTracer (Milton's renderer needs Boost, Qt 4 and OpenGL and does not build here; its kd-tree and
+triangle code do, and pin the oracle's intersections) -- on the same bounded sample of the same
+workload as the cpu_baseline leg, with every host thread, and prints its own line.
 
 Other workloads (`--workload`): plain (the CPU-runnable 256 x 256 x 16 spp frame, same line
 format, CPU baseline over the whole frame), batched (64 scenes rendered one by one and as one
@@ -43,12 +45,14 @@ SEED = 0
 # The frame workloads: mid (the benchmark line) and plain (the CPU-runnable configuration).
 CONFIGS = {
     "mid": dict(scene="mid", width=1024, height=1024, spp=64, max_depth=8, rr_start=3,
-                cpu_rows=(496, 528), ref_rows=8,  # bounded CPU samples: 32 / 8 rows of the frame
+                cpu_rows=(496, 528),  # the bounded CPU sample: 32 rows of the frame, every pass
+                hispp_rows=(508, 512), hispp_spp=1024,  # the FP64 high-spp image of the parity check
                 workload=("mid: 1,000,010 triangles (400 seeded UV spheres x 2,500 tris on a 20x20 ground quad), "
                           "60/30/10% Lambertian/modified-Phong/dielectric(IOR 1.5), 4 quad lights, SAH kd-tree "
                           "(Milton defaults), 1024x1024 px, 64 spp, max depth 8, RR from depth 3, fp32")),
     "plain": dict(scene="plain", width=256, height=256, spp=16, max_depth=5, rr_start=3,
-                  cpu_rows=(0, 256), ref_rows=64,  # the whole frame / a quarter of it per step
+                  cpu_rows=(0, 256),  # the whole frame
+                  hispp_rows=(120, 136), hispp_spp=1024,
                   workload=("plain: closed box of 5 quads + 2 rotated boxes (34 triangles), one 0.25-area quad "
                             "light of radiance 15, Lambertian albedos U[0.2, 0.8], 256x256 px, 16 spp, max depth 5, "
                             "RR from depth 3, 40 degree pinhole, fp32")),
@@ -135,20 +139,40 @@ def _dist():
     return ws, rank, local
 
 
-def _cpu_sample(scene, rows, sample_count, seed, threads=None):
-    """Times the oracle (FP64 restatement of Milton's PathTracer) on a bounded pixel subset."""
+L2_NOTE = "a 256 MiB buffer (larger than the 129 MB L2) is written before every step"
+# The CPU sample (cpu_baseline leg and the reference arm) uses its own seed, independent of the
+# GPU frame's, so that its image also serves the z-test on per-pixel means.
+CPU_SEED = SEED + 1
+HISPP_SEED = SEED + 2
+
+
+def _config(ws: int) -> dict:
+    """The workload description, identical in both arms' lines."""
+    return {"workload": WORKLOAD, "l2": L2_NOTE,
+            "parallelism": f"replicas x{ws} (independent sample streams, no collective in the step)"}
+
+
+def _cpu_sample_text(threads: int) -> str:
+    return (f"rows {CPU_ROWS[0]}-{CPU_ROWS[1] - 1} of the {CFG['scene']} frame ({CPU_ROWS[1] - CPU_ROWS[0]} x {W_IMG} "
+            f"px x {SPP} spp = {W_IMG * (CPU_ROWS[1] - CPU_ROWS[0]) * SPP} paths), FP64 oracle port of Milton's "
+            f"PathTracer, {threads} threads, work handed out in 32-pixel spans")
+
+
+def _cpu_sample(scene, tree=None, threads=None, per_path=False):
+    """Times the oracle (FP64 restatement of Milton's PathTracer) on the bounded pixel subset
+    CPU_ROWS, every sample pass, seed CPU_SEED."""
     from oracle import pyoracle
     t0 = time.perf_counter()
-    tree = pyoracle.Tree(scene.tri_v)
+    tree = tree or pyoracle.Tree(scene.tri_v)
     build_s = time.perf_counter() - t0
     threads = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
-    mean, _, st = pyoracle.render(scene, tree, W_IMG, H_IMG, SPP, sample_count=sample_count, max_depth=MAX_DEPTH,
-                                  rr_start=RR_START, seed=seed, rows=rows, threads=threads)
+    mean, paths, st = pyoracle.render(scene, tree, W_IMG, H_IMG, SPP, max_depth=MAX_DEPTH, rr_start=RR_START,
+                                      seed=CPU_SEED, rows=CPU_ROWS, threads=threads, per_path=per_path)
     dt = time.perf_counter() - t0
-    paths = W_IMG * (rows[1] - rows[0]) * sample_count
-    return dict(mpaths=paths / dt / 1e6, seconds=dt, paths=paths, threads=threads, build_s=build_s, mean=mean,
-                stats=st, tree=tree)
+    n = W_IMG * (CPU_ROWS[1] - CPU_ROWS[0]) * SPP
+    return dict(mpaths=n / dt / 1e6, seconds=dt, paths=n, threads=threads, build_s=build_s, mean=mean,
+                per_path=paths, stats=st, tree=tree)
 
 
 def run_reference(args):
@@ -159,29 +183,84 @@ def run_reference(args):
     from oracle import pyoracle
     tree = pyoracle.Tree(scene.tri_v)
     threads = os.cpu_count() or 1
-    rows_per_step = CFG["ref_rows"]
     times = []
-    paths_per_step = W_IMG * rows_per_step * SPP
+    paths_per_step = 0
     for k in range(args.warmup + args.steps):
-        r0 = (H_IMG // 4 + rows_per_step * k) % (H_IMG - rows_per_step + 1)
-        t0 = time.perf_counter()
-        pyoracle.render(scene, tree, W_IMG, H_IMG, SPP, max_depth=MAX_DEPTH, rr_start=RR_START, seed=SEED,
-                        rows=(r0, r0 + rows_per_step), threads=threads)
-        dt = time.perf_counter() - t0
+        r = _cpu_sample(scene, tree=tree, threads=threads)
+        paths_per_step = r["paths"]
         if k >= args.warmup:
-            times.append(dt)
+            times.append(r["seconds"])
     total = sum(times)
     value = paths_per_step * len(times) / total / 1e6
-    sample = (f"each step: {rows_per_step} rows x {W_IMG} px x {SPP} spp = {paths_per_step} paths of the "
-              f"{CFG['scene']} frame (rows advance per step), FP64 oracle port, {threads} threads")
+    sample = "each step: " + _cpu_sample_text(threads)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": sample},
+            "config": _config(ws),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def _luminance(x):
+    return x.mean(axis=-1)
+
+
+def _frame_parity(scene, dscene, film, img, cpu, pt, torch):
+    """Parity of the benchmark frame against the FP64 oracle (rank 0, after the timed region):
+      path_agreement   per-path radiance, GPU vs oracle with the same seed and counter RNG, on
+                       the CPU rows at 4 samples per pixel (within 1e-4 + 2e-3 relative)
+      z                per-pixel mean luminance of the GPU frame (seed SEED) against the oracle's
+                       (seed CPU_SEED, independent) on the CPU rows: z = difference / standard
+                       error; z_frac = fraction of pixels with |z| > 4
+      rmse_*_vs_fp64_hispp  RMSE of the GPU frame and of the oracle image, both at the frame's
+                       spp, against an FP64 oracle image at hispp_spp of the hispp rows"""
+    import numpy as np
+    from oracle import pyoracle
+    r0, r1 = CPU_ROWS
+    # same-sample per-path agreement
+    ns = 4
+    out = torch.zeros((W_IMG * H_IMG * ns, 4), dtype=torch.float32, device="cuda")
+    pf = pt.Film(W_IMG, H_IMG)
+    pt.render(dscene, pt.RenderSettings(W_IMG, H_IMG, SPP, sample_count=ns, max_depth=MAX_DEPTH,
+                                        rr_start_depth=RR_START, seed=SEED), pf, path_out=out)
+    torch.cuda.synchronize()
+    pg = out.cpu().numpy().reshape(H_IMG, W_IMG, ns, 4)[r0:r1, ..., :3].astype(np.float64)
+    pf.close()
+    _, po, _ = pyoracle.render(scene, cpu["tree"], W_IMG, H_IMG, SPP, sample_count=ns, max_depth=MAX_DEPTH,
+                               rr_start=RR_START, seed=SEED, rows=CPU_ROWS, per_path=True)
+    close = np.abs(pg - po) <= 1e-4 + 2e-3 * np.maximum(np.abs(pg), np.abs(po))
+    agree = float(np.all(close, axis=-1).mean())
+    # z-test on per-pixel mean luminance, independent seeds
+    raw = film.raw()[:, r0:r1].astype(np.float64)  # [0]: sum rgb, count; [1]: compensation rgb, sum of lum^2
+    n_g = raw[0, ..., 3]
+    m_g = _luminance(img[r0:r1])
+    v_g = np.maximum(raw[1, ..., 3] / n_g - m_g ** 2, 0.0) * n_g / (n_g - 1)
+    lo = _luminance(cpu["per_path"])  # (rows, W, spp)
+    n_o = lo.shape[-1]
+    m_o = lo.mean(-1)
+    v_o = lo.var(-1, ddof=1)
+    se = np.sqrt(v_g / n_g + v_o / n_o)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        z = np.where(se > 0, (m_g - m_o) / se, 0.0)
+    z_frac = float((np.abs(z) > 4).mean())
+    # FP64 high-spp image of a few rows
+    h0, h1 = CFG["hispp_rows"]
+    t0 = time.perf_counter()
+    hi, _, _ = pyoracle.render(scene, cpu["tree"], W_IMG, H_IMG, CFG["hispp_spp"], max_depth=MAX_DEPTH,
+                               rr_start=RR_START, seed=HISPP_SEED, rows=(h0, h1))
+    hi_s = time.perf_counter() - t0
+    rmse_g = float(np.sqrt(((img[h0:h1] - hi) ** 2).mean()))
+    rmse_o = float(np.sqrt(((cpu["mean"][h0 - r0:h1 - r0] - hi) ** 2).mean()))
+    return {"path_agreement": agree, "path_agreement_sample": f"rows {r0}-{r1 - 1}, first {ns} of {SPP} passes, "
+                                                             f"same seed ({W_IMG * (r1 - r0) * ns} paths)",
+            "z_frac": z_frac, "z_abs_mean": float(np.abs(z).mean()), "z_sample": f"rows {r0}-{r1 - 1}, {SPP} spp, "
+                                                                               "GPU seed vs an independent oracle seed",
+            "rmse_gpu_vs_fp64_hispp": rmse_g, "rmse_oracle_vs_fp64_hispp": rmse_o,
+            "rmse_gpu_over_oracle": rmse_g / rmse_o if rmse_o > 0 else None,
+            "hispp": f"FP64 oracle, rows {h0}-{h1 - 1}, {CFG['hispp_spp']} spp, {hi_s:.1f} s",
+            "image_mean_gpu": float(img[h0:h1].mean()), "image_mean_fp64_hispp": float(hi.mean())}
 
 
 def run_ours(args):
@@ -290,6 +369,22 @@ def run_ours(args):
         e2e_s = float(t.item())
     e2e_value = paths_per_step * ws * args.steps / e2e_s / 1e6
 
+    # once through the renderer object a Milton host drives (Renderer::init: kd build and upload;
+    # render; the finalized output read back), so the host kd build is inside the time
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ptr = pt.PathTracer(props={"noSuperSamples": SPP, "maxDepth": MAX_DEPTH, "rrStartDepth": RR_START,
+                               "seed": SEED})
+    ptr.set_scene(scene)
+    ptr.set_output(W_IMG, H_IMG)
+    ptr.init()
+    ptr.render(stream=stream)
+    ptr.output()
+    init_s = time.perf_counter() - t0
+    e2e_init = {"value": paths_per_step / init_s / 1e6, "unit": UNIT, "seconds": round(init_s, 3),
+                "what": "one frame through PathTracer init (host kd build + upload) + render + output read"}
+    del ptr
+
     # roofline of the dominant kernel
     peaks = _peaks()
     ext_ms, ext_n = prof["extend"]
@@ -315,14 +410,14 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene generator, no external assets)",
-        "config": {"workload": WORKLOAD, "paths_per_step": paths_per_step,
-                   "l2": "a 256 MiB buffer (larger than the 129 MB L2) is written before every step",
-                   "wave_paths": "automatic (up to 2^26 paths per wave, workspace within 40 GB)",
-                   "parallelism": f"replicas x{ws} (independent sample streams, no collective in the step)",
-                   "kd_build_s": round(build_s, 3), "kd_nodes": kst["node_pairs"], "kd_refs": kst["refs"],
-                   "rays_per_path": (stats["extension_rays"] + stats["shadow_rays"]) / paths_per_step,
-                   "mrays_per_s": value * (stats["extension_rays"] + stats["shadow_rays"]) / paths_per_step},
+        "config": _config(ws),
+        "details": {"paths_per_step": paths_per_step,
+                    "wave_paths": "automatic (up to 2^26 paths per wave, workspace within 40 GB)",
+                    "kd_build_s": round(build_s, 3), "kd_nodes": kst["node_pairs"], "kd_refs": kst["refs"],
+                    "rays_per_path": (stats["extension_rays"] + stats["shadow_rays"]) / paths_per_step,
+                    "mrays_per_s": value * (stats["extension_rays"] + stats["shadow_rays"]) / paths_per_step},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e_with_init": e2e_init,
         "gpu_launches": int(launches),
         "kernels_ms": {k: round(v[0], 3) for k, v in prof.items()},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -332,18 +427,10 @@ def run_ours(args):
         "clocks": clk,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu = _cpu_sample(scene, CPU_ROWS, SPP, SEED)
-        gpu_rows = img[CPU_ROWS[0]:CPU_ROWS[1]]
-        rmse = float(np.sqrt(((gpu_rows - cpu["mean"]) ** 2).mean()))
-        out["cpu_baseline"] = {
-            "value": cpu["mpaths"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
-            "sample": (f"rows {CPU_ROWS[0]}-{CPU_ROWS[1] - 1} of the {CFG['scene']} frame "
-                       f"({CPU_ROWS[1] - CPU_ROWS[0]} x {W_IMG} px x {SPP} spp = {cpu['paths']} paths), FP64 oracle, "
-                       "same seed"), "seconds": round(cpu["seconds"], 2)}
-        out["parity"] = {"rmse_vs_fp64_same_samples": rmse, "oracle_rows_mean": float(cpu["mean"].mean()),
-                         "gpu_rows_mean": float(gpu_rows.mean()),
-                         "note": "same seed and counter RNG: paths agree unless FP32 and FP64 take "
-                                 "different discrete decisions"}
+        cpu = _cpu_sample(scene, per_path=True)
+        out["cpu_baseline"] = {"value": cpu["mpaths"], "unit": UNIT, "cores": cpu["threads"], "kind": "port",
+                               "sample": _cpu_sample_text(cpu["threads"]), "seconds": round(cpu["seconds"], 2)}
+        out["parity"] = _frame_parity(scene, dscene, film, img, cpu, pt, torch)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:

@@ -1,8 +1,9 @@
 """Build the oracle (test infrastructure): oracle/oracle.c -> oracle/_build/liborc.so.
 
-Compiled with gcc at -O2 and -ffp-contract=off so that the FP64 restatement rounds the
-same way on x86-64 and aarch64 (the kd-tree comparison against the product builder is
-bit-exact).
+Compiled with gcc at -O3 (the reference's OPT level, mlt/src/.make/defines.mk:144-148) and
+-ffp-contract=off so that the FP64 restatement rounds the same way on x86-64 and aarch64 (the
+kd-tree comparison against the product builder is bit-exact); no -march=native, so the one
+build runs on both hosts.
 """
 from __future__ import annotations
 
@@ -20,7 +21,7 @@ def build(force: bool = False) -> Path:
     if not force and OUT.exists() and OUT.stat().st_mtime >= SRC.stat().st_mtime:
         return OUT
     tmp = OUT.with_suffix(".so.tmp")
-    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", str(SRC), "-o", str(tmp),
+    cmd = ["gcc", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", str(SRC), "-o", str(tmp),
            "-lm", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -1429,23 +1429,27 @@ static void evaluate(const orc_render_ctx *c, orc_path *ph, v3 o, v3 d, int dept
   }
 }
 
+/* Work is handed out in spans of ORC_SPAN pixels of one row (not whole rows), so that a sample
+ * of a few rows still keeps every host thread busy. */
+#define ORC_SPAN 32
+
 typedef struct {
   const orc_render_ctx *c;
   int row_begin, row_end;
-  int *next_row;      /* shared work counter (rows handed out one at a time) */
+  int64_t *next_span; /* shared work counter: spans of ORC_SPAN pixels, row-major from row_begin */
   pthread_mutex_t *lock;
   double *film;       /* width*height*3 sums */
-  double *path_out;   /* optional per-path radiance: (pixel * sample_count + s) * 3 */
+  double *path_out;   /* optional per-path radiance: (pixel - row_begin * width) * sample_count + s, 3 each */
   uint64_t stats[4];
 } orc_job;
 
-static void render_row(orc_job *j, int y) {
+static void render_span(orc_job *j, int y, int x0, int x1) {
   const orc_render_ctx *c = j->c;
   int W = c->p.width, H = c->p.height;
   int side = (int)sqrt((double)c->p.spp);
   if (side < 1) side = 1;
   int s2 = side * side;
-  for (int x = 0; x < W; ++x) {
+  for (int x = x0; x < x1; ++x) {
     uint64_t pix = (uint64_t)y * W + x;
     double acc[3] = {0, 0, 0};
     for (int si = 0; si < c->p.sample_count; ++si) {
@@ -1468,7 +1472,8 @@ static void render_row(orc_job *j, int y) {
       evaluate(c, &ph, o, d, 0, L);
       for (int k3 = 0; k3 < 3; ++k3) acc[k3] += L[k3];
       if (j->path_out) {
-        double *po = j->path_out + (pix * (uint64_t)c->p.sample_count + (uint64_t)si) * 3;
+        uint64_t band_pix = pix - (uint64_t)j->row_begin * (uint64_t)W;
+        double *po = j->path_out + (band_pix * (uint64_t)c->p.sample_count + (uint64_t)si) * 3;
         po[0] = L[0]; po[1] = L[1]; po[2] = L[2];
       }
       j->stats[0] += ph.rays_ext;
@@ -1482,12 +1487,17 @@ static void render_row(orc_job *j, int y) {
 
 static void *render_thread(void *arg) {
   orc_job *j = (orc_job *)arg;
+  const int W = j->c->p.width;
+  const int64_t per_row = (W + ORC_SPAN - 1) / ORC_SPAN;
+  const int64_t total = per_row * (int64_t)(j->row_end - j->row_begin);
   for (;;) {
     pthread_mutex_lock(j->lock);
-    int y = (*j->next_row)++;
+    int64_t k = (*j->next_span)++;
     pthread_mutex_unlock(j->lock);
-    if (y >= j->row_end) break;
-    render_row(j, y);
+    if (k >= total) break;
+    int y = j->row_begin + (int)(k / per_row);
+    int x0 = (int)(k % per_row) * ORC_SPAN;
+    render_span(j, y, x0, x0 + ORC_SPAN < W ? x0 + ORC_SPAN : W);
   }
   return NULL;
 }
@@ -1535,10 +1545,10 @@ int orc_render(int64_t ntri, const float *v, const float *n, const int32_t *mat,
   pthread_t *th = (pthread_t *)calloc(nth, sizeof(pthread_t));
   pthread_mutex_t lock;
   pthread_mutex_init(&lock, NULL);
-  int next = row0;
+  int64_t next = 0;
   for (int t = 0; t < nth; ++t) {
     jobs[t].c = &c; jobs[t].film = film_sum; jobs[t].path_out = path_out;
-    jobs[t].row_begin = row0; jobs[t].row_end = row1; jobs[t].next_row = &next; jobs[t].lock = &lock;
+    jobs[t].row_begin = row0; jobs[t].row_end = row1; jobs[t].next_span = &next; jobs[t].lock = &lock;
   }
   for (int t = 1; t < nth; ++t) pthread_create(&th[t], NULL, render_thread, &jobs[t]);
   render_thread(&jobs[0]);

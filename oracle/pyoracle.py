@@ -132,7 +132,8 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
     ip = np.array([width, height, spp, nds, max_depth, rr_start, efficient_direct, sample_begin, sample_count, r0, r1,
                    threads], np.int32)
     film = np.zeros((height, width, 3), np.float64)
-    paths = np.zeros((height * width * sample_count, 3), np.float64) if per_path else None
+    # per-path radiance of the rendered rows only: ((y - r0) * width + x) * sample_count + s
+    paths = np.zeros(((r1 - r0) * width * sample_count, 3), np.float64) if per_path else None
     st = np.zeros(4, np.uint64)
     lights = scene.lights if len(scene.lights) else np.zeros((1, 16), np.float32)
     cam = np.zeros(16, np.float32)
@@ -156,7 +157,7 @@ def render(scene, tree: Tree, width, height, spp, sample_begin=0, sample_count=N
                    _p(sph_mat), _p(sph_light), tree.h, _p(cam), _p(ip), seed, stream, _p(film), _p(paths), _p(st))
     mean = film[r0:r1] / max(sample_count, 1)
     if per_path:
-        paths = paths.reshape(height, width, sample_count, 3)[r0:r1]
+        paths = paths.reshape(r1 - r0, width, sample_count, 3)
     stats = dict(extension_rays=int(st[0]), shadow_rays=int(st[1]), zero_pdf=int(st[2]), truncated=int(st[3]))
     return mean, paths, stats
 
