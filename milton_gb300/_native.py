@@ -1,4 +1,4 @@
-"""ctypes binding of libmgpu.so (include/mgpu.h, include/mgpu_server.h, include/milton_plugin.h).
+"""ctypes binding of libmgpu.so (include/mgpu.h, include/mgpu_server.h, include/mgpu_renderer.h).
 
 There is no fallback: if the in-tree library is missing, importing this module raises.
 """
@@ -137,9 +137,8 @@ SIGNATURES = [
     ("mgpu_server_read", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("mgpu_server_release", C.c_int, [C.c_void_p, C.c_int64]),
     ("mgpu_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
-    ("plugin_type", C.c_int, []),
-    ("plugin_new", C.c_void_p, []),
-    ("plugin_delete", None, [C.c_void_p]),
+    ("mgpu_renderer_create", C.c_int, [C.POINTER(C.c_void_p)]),
+    ("mgpu_renderer_destroy", C.c_int, [C.c_void_p]),
     ("mgpu_renderer_set_value", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     ("mgpu_renderer_get_value", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_size_t]),
     ("mgpu_renderer_set_scene", C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),

@@ -1,4 +1,5 @@
-"""Build libmgpu.so in-tree (milton_gb300/lib/) for sm_103a.
+"""Build libmgpu.so in-tree (milton_gb300/lib/) for sm_103a, and beside it libmgpu_milton.so,
+Milton's dynamic renderer plugin (milton_plugin/gpu_path_tracer.cpp, linked against libmgpu.so).
 
 Each translation unit is compiled in parallel: .cu files with nvcc
 (-gencode arch=compute_103a,code=sm_103a), .cpp files with g++, then linked with nvcc
@@ -19,6 +20,8 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 OUT_DIR = PKG / "lib"
 LIB = OUT_DIR / "libmgpu.so"
+PLUGIN_SRC = PKG / "milton_plugin" / "gpu_path_tracer.cpp"
+PLUGIN = OUT_DIR / "libmgpu_milton.so"
 BUILD_DIR = PKG / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -76,7 +79,21 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | No
         tmp = LIB.with_suffix(".so.tmp")
         _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lpthread"])
         os.replace(tmp, LIB)
+    build_plugin()
     return LIB
+
+
+def build_plugin() -> Path:
+    """libmgpu_milton.so: the plugin's Milton base-class members stay undefined here and resolve
+    against the host (Milton's library, or the stand-in host of the tests) when it is loaded."""
+    deps = [PLUGIN_SRC, LIB, *(PKG / "milton_plugin").glob("*.h"), INCLUDE / "mgpu.h"]
+    if PLUGIN.exists() and PLUGIN.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
+        return PLUGIN
+    tmp = PLUGIN.with_suffix(".so.tmp")
+    _run(["g++", *HOST_FLAGS, "-shared", "-o", str(tmp), str(PLUGIN_SRC), f"-L{OUT_DIR}", "-lmgpu",
+          "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, PLUGIN)
+    return PLUGIN
 
 
 if __name__ == "__main__":

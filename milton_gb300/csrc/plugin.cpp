@@ -1,4 +1,6 @@
-// plugin.cpp -- Milton dynamic-plugin entry points and the GPU PathTracer object behind them.
+// plugin.cpp -- the renderer object of the C ABI (include/mgpu_renderer.h): Milton's PathTracer
+// keys, scene, camera and output behind plain C calls, for hosts that speak C.  Milton itself
+// loads the C++ plugin libmgpu_milton.so (milton_gb300/milton_plugin/gpu_path_tracer.cpp).
 #include <stdlib.h>
 #include <string.h>
 
@@ -7,7 +9,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/milton_plugin.h"
+#include "../../include/mgpu_renderer.h"
 
 struct mgpu_renderer {
   std::map<std::string, std::string> props;  // PropertyMap (text values)
@@ -76,19 +78,25 @@ struct mgpu_renderer {
   }
 };
 
-static int bad(const char *msg);
+// errors go through the library's thread-local message
+namespace mgpu {
+int fail(int code, const std::string &msg);
+}
+static int bad(const char *msg) { return mgpu::fail(MGPU_E_INVALID, msg); }
 
 extern "C" {
 
-MILTON_PLUGIN_TYPE plugin_type(void) { return MILTON_PLUGIN_TYPE_RENDERER; }
-
-void *plugin_new(void) {
-  mgpu_renderer *r = new (std::nothrow) mgpu_renderer();
-  if (!r) bad("plugin_new: out of host memory");
-  return r;
+int mgpu_renderer_create(mgpu_renderer **out) {
+  if (!out) return bad("mgpu_renderer_create: null argument");
+  *out = new (std::nothrow) mgpu_renderer();
+  if (!*out) return mgpu::fail(MGPU_E_NOMEM, "mgpu_renderer_create: out of host memory");
+  return MGPU_OK;
 }
 
-void plugin_delete(void *plugin) { delete static_cast<mgpu_renderer *>(plugin); }
+int mgpu_renderer_destroy(mgpu_renderer *r) {
+  delete r;
+  return MGPU_OK;
+}
 
 int mgpu_renderer_set_value(mgpu_renderer *r, const char *key, const char *value) {
   if (!r || !key || !value) return bad("mgpu_renderer_set_value: null argument");
@@ -232,8 +240,3 @@ int mgpu_renderer_get_output(mgpu_renderer *r, double *rgb) {
 
 }  // extern "C"
 
-// errors go through the library's thread-local message
-namespace mgpu {
-int fail(int code, const std::string &msg);
-}
-static int bad(const char *msg) { return mgpu::fail(MGPU_E_INVALID, msg); }

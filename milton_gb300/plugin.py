@@ -1,10 +1,13 @@
-"""Milton's `"renderer": {"type": "dynamic", "path": ...}` plugin loading, for hosts that speak
-the C interface (MiltonJSONSceneLoader::_parse_dynamic_plugin,
-mlt/src/milton/loaders/MiltonJSONSceneLoader.cpp:1770-1813): dlopen, resolve plugin_type and
-plugin_new, check the type, instantiate; the same error cases raise PluginError."""
+"""The GPU PathTracer as a renderer object for Python hosts (include/mgpu_renderer.h): Milton's
+PropertyMap keys, setScene / setCamera / setOutput, Renderer::init, Renderer::render and the
+finalized output (mlt/src/milton/renderers/Renderer.h:52-62, PointSampleRenderer.h:61-95).
+
+Milton itself loads the C++ plugin milton_gb300/lib/libmgpu_milton.so (`PLUGIN_PATH`), a
+milton::PointSampleRenderer built from milton_gb300/milton_plugin/gpu_path_tracer.cpp."""
 from __future__ import annotations
 
 import ctypes as C
+from pathlib import Path
 
 import numpy as np
 
@@ -12,24 +15,28 @@ from . import _native as N
 from .pathtracer import _desc
 from .scene import Scene
 
-MILTON_PLUGIN_TYPE_RENDERER = 0
+PLUGIN_PATH = Path(__file__).resolve().parent / "lib" / "libmgpu_milton.so"
 
 
-class PluginError(RuntimeError):
-    pass
+class RendererObject:
+    """One mgpu_renderer: a GPU PathTracer driven through mgpu_renderer_*."""
 
-
-class DynamicRenderer:
-    """The renderer object behind plugin_new(), driven through mgpu_renderer_*."""
-
-    def __init__(self, lib: C.CDLL, handle: int):
-        self.lib, self.handle = lib, handle
+    def __init__(self):
+        self.lib = N.load()
+        h = C.c_void_p()
+        N.check(self.lib.mgpu_renderer_create(C.byref(h)))
+        self.handle = h.value
         self.width = self.height = 0
 
     def __setitem__(self, key: str, value) -> None:
         if isinstance(value, bool):
             value = "true" if value else "false"
         N.check(self.lib.mgpu_renderer_set_value(self.handle, key.encode(), str(value).encode()))
+
+    def __getitem__(self, key: str) -> str:
+        buf = C.create_string_buffer(256)
+        N.check(self.lib.mgpu_renderer_get_value(self.handle, key.encode(), buf, 256))
+        return buf.value.decode()
 
     def set_scene(self, scene: Scene) -> None:
         d = _desc(scene)
@@ -55,7 +62,7 @@ class DynamicRenderer:
 
     def close(self) -> None:
         if self.handle:
-            self.lib.plugin_delete(self.handle)
+            self.lib.mgpu_renderer_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
@@ -63,27 +70,3 @@ class DynamicRenderer:
             self.close()
         except Exception:
             pass
-
-
-def load_dynamic_renderer(path: str) -> DynamicRenderer:
-    try:
-        lib = C.CDLL(path, mode=C.RTLD_LOCAL)
-    except OSError as e:
-        raise PluginError(f"{path}: plugin failed to load: {e}") from None
-    for sym in ("plugin_type", "plugin_new"):
-        if not hasattr(lib, sym):
-            raise PluginError(f"{path}: invalid plugin; could not find {sym} symbol")
-    lib.plugin_type.restype = C.c_int
-    lib.plugin_new.restype = C.c_void_p
-    kind = lib.plugin_type()
-    if kind != MILTON_PLUGIN_TYPE_RENDERER:
-        raise PluginError(f"{path}: dynamic plugin expected type '{MILTON_PLUGIN_TYPE_RENDERER}' but found type '{kind}'")
-    # the entry points behind the handle are libmgpu's; bind them with the shared signatures
-    for name, res, args in N.SIGNATURES:
-        if hasattr(lib, name):
-            fn = getattr(lib, name)
-            fn.restype, fn.argtypes = res, args
-    handle = lib.plugin_new()
-    if not handle:
-        raise PluginError(f"{path}: invalid plugin; plugin_new returned NULL")
-    return DynamicRenderer(lib, handle)

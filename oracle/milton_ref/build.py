@@ -52,6 +52,9 @@ SOURCES = [
     "cameras/Camera.cpp",
 ]
 
+# this directory's own sources linked in: the query driver and the statics Milton's host keeps
+OWN = ["host_statics.cpp", "driver.cpp"]
+
 FLAGS = ["-std=gnu++17", "-O3", "-DNDEBUG", "-DPOSIX", "-fno-pie", "-w"]
 
 
@@ -78,6 +81,17 @@ def _includes(m: Path) -> list[str]:
     return [f"-I{d}" for d in dirs]
 
 
+def include_flags() -> list[str]:
+    """-I flags (stand-ins first) for compiling other test sources against Milton's headers."""
+    return _includes(milton_dir())
+
+
+def objects(with_driver: bool = False) -> list[Path]:
+    """The compiled reference objects (and host_statics), after build()."""
+    names = [rel.replace("/", "_") + ".o" for rel in SOURCES + OWN if with_driver or rel != "driver.cpp"]
+    return [OBJ_DIR / n for n in names]
+
+
 def _run(cmd: list[str]) -> None:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -92,8 +106,8 @@ def build(force: bool = False) -> Path | None:
     inc = _includes(m)
     shim_mtime = max(p.stat().st_mtime for p in (HERE / "shim").rglob("*") if p.is_file())
     jobs, objs = [], []
-    for rel in SOURCES + ["driver.cpp"]:
-        src = HERE / rel if rel == "driver.cpp" else m / rel
+    for rel in SOURCES + OWN:
+        src = HERE / rel if rel in OWN else m / rel
         obj = OBJ_DIR / (rel.replace("/", "_") + ".o")
         objs.append(obj)
         if force or not obj.exists() or obj.stat().st_mtime < max(src.stat().st_mtime, shim_mtime):

@@ -48,14 +48,6 @@
 
 using namespace milton;
 
-// Static state of ResourceManager (its .cpp needs the plugin loader, which this oracle does
-// not use) and the image loader (no image maps on the intersection path).
-ImagePtrMap ResourceManager::s_imagePtrMap;
-PropertyMap ResourceManager::s_propertyMap;
-QMutex ResourceManager::s_mutex;
-Log ResourceManager::log;
-Image *Image::load(const std::string &) { return NULL; }
-
 namespace {
 
 struct Reader {

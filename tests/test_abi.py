@@ -1,18 +1,19 @@
-"""The C-ABI library loads and exports every entry point include/*.h declares (no GPU calls)."""
+"""The C-ABI library loads and exports every entry point include/*.h declares, and the Milton
+plugin library exports the three entry points Milton resolves (no GPU calls)."""
 import ctypes as C
 import re
+import subprocess
 from pathlib import Path
 
-import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 DECL = re.compile(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:mgpu|plugin)_\w+)\s*\(", re.M)
 
 
-def declared():
+def declared(headers=("mgpu.h", "mgpu_server.h", "mgpu_renderer.h")):
     names = set()
-    for h in (ROOT / "include").glob("*.h"):
-        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+    for h in headers:
+        text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / h).read_text(), flags=re.S)
         for m in DECL.finditer(text):
             if "typedef" not in text[max(0, m.start() - 40):m.start()]:
                 names.add(m.group(1))
@@ -22,8 +23,9 @@ def declared():
 def test_headers_declare_the_boundary():
     names = declared()
     for must in ("mgpu_accel_build", "mgpu_scene_create", "mgpu_trace_closest", "mgpu_trace_any", "mgpu_render",
-                 "mgpu_film_read", "mgpu_last_error", "plugin_type", "plugin_new", "plugin_delete"):
+                 "mgpu_film_read", "mgpu_last_error", "mgpu_renderer_create", "mgpu_renderer_init"):
         assert must in names
+    assert declared(("milton_plugin.h",)) == ["plugin_delete", "plugin_new", "plugin_type"]
 
 
 def test_library_exports_every_declared_symbol():
@@ -33,14 +35,29 @@ def test_library_exports_every_declared_symbol():
     for name in declared():
         assert hasattr(lib, name), f"{name} not exported"
         assert name in bound, f"{name} has no ctypes signature"
+    # the Milton plugin entry points live in the plugin library only
+    for name in ("plugin_type", "plugin_new", "plugin_delete"):
+        assert not hasattr(lib, name), f"libmgpu.so must not export {name}"
 
 
-def test_plugin_abi_and_errors_without_gpu():
+def _dynamic_symbols(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(path)], capture_output=True, text=True, check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if line.strip()}
+
+
+def test_plugin_library_exports_the_milton_entry_points():
+    from milton_gb300.plugin import PLUGIN_PATH
+    syms = _dynamic_symbols(PLUGIN_PATH)
+    for name in declared(("milton_plugin.h",)):
+        assert name in syms, f"{name} not exported by {PLUGIN_PATH.name}"
+
+
+def test_renderer_object_and_errors_without_gpu():
     from milton_gb300 import _native
     lib = _native.load()
-    assert lib.plugin_type() == 0  # MILTON_PLUGIN_TYPE_RENDERER
-    r = lib.plugin_new()
-    assert r
+    h = C.c_void_p()
+    assert lib.mgpu_renderer_create(C.byref(h)) == 0 and h.value
+    r = h.value
     # PropertyMap round trip and Renderer::init preconditions (host-only paths)
     assert lib.mgpu_renderer_set_value(r, b"noSuperSamples", b"16") == 0
     buf = C.create_string_buffer(32)
@@ -48,18 +65,10 @@ def test_plugin_abi_and_errors_without_gpu():
     assert lib.mgpu_renderer_init(r) == -1
     assert b"no scene" in lib.mgpu_last_error()
     assert lib.mgpu_renderer_render(r) == -1
-    lib.plugin_delete(r)
+    assert lib.mgpu_renderer_destroy(r) == 0
+    assert lib.mgpu_renderer_create(None) == -1
     # argument validation happens before any device work
     assert lib.mgpu_accel_build(None, None, None) == -1
     assert lib.mgpu_trace_closest(None, None, None, 1, None) == -1
     assert lib.mgpu_render(None, None, None, None) == -1
     assert lib.mgpu_version() == 1
-
-
-def test_dynamic_loader_mirrors_milton(tmp_path):
-    from milton_gb300.plugin import load_dynamic_renderer, PluginError
-    r = load_dynamic_renderer(str(ROOT / "milton_gb300" / "lib" / "libmgpu.so"))
-    assert r.handle
-    r.close()
-    with pytest.raises(PluginError, match="failed to load"):
-        load_dynamic_renderer(str(tmp_path / "missing.so"))

@@ -123,15 +123,14 @@ def test_tuning_knobs_do_not_change_the_image(cuda):
 
 
 @pytest.mark.parametrize("kind", ["plain", "textured"])
-def test_renderer_plugin_object(cuda, kind):
-    # the Milton plugin object owns copies of every scene array (image maps, uvs and a
-    # background included) and renders what mgpu_render renders
-    from milton_gb300.plugin import load_dynamic_renderer
-    from milton_gb300._native import LIB_PATH
+def test_renderer_object(cuda, kind):
+    # the C renderer object (include/mgpu_renderer.h) owns copies of every scene array (image
+    # maps, uvs and a background included) and renders what mgpu_render renders
+    from milton_gb300.plugin import RendererObject
     s = scenegen.plain(0) if kind == "plain" else scenegen.textured(4)
     if kind == "textured":
         s.background_le = np.array([0.3, 0.2, 0.1], np.float32)
-    r = load_dynamic_renderer(str(LIB_PATH))
+    r = RendererObject()
     r.set_scene(s)
     r.set_output(32, 32)
     for k, v in dict(noSuperSamples=4, maxDepth=5, rrStartDepth=3, seed=9).items():
