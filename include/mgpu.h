@@ -298,18 +298,28 @@ int mgpu_render(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_
  * a plugin host whose device allocator is its own -- so this entry point renders with the same
  * estimator, random numbers and film as mgpu_render but never calls cudaMalloc, cudaFree or any
  * allocating routine.  Its scratch (path state, ray queues, light-sample slots) is one fixed
- * 32 MiB device array compiled into libmgpu.so; every GPU that loads the library holds it until
- * the process exits.  The caller still provides the inputs and outputs: a scene from
- * mgpu_scene_create and a film from mgpu_film_create, made beforehand.
+ * 32 MiB device array compiled into libmgpu.so; every GPU that loads the library's rendering
+ * module holds it until the process exits.  The caller still provides the inputs and outputs: a
+ * scene from mgpu_scene_create and a film from mgpu_film_create, made beforehand.
  *   - The scratch bounds the wave: with 4 light samples per vertex it holds about 65 000
  *     paths in flight (wave_paths 0 picks the most that fit), so large frames render slower
  *     than with mgpu_render.  A wave_paths above that capacity is rejected with
  *     MGPU_E_INVALID and a message naming the capacity; nothing is rendered.
- *   - The first call on a device looks up the array's device address with
- *     cudaGetSymbolAddress; make that first call before any stream capture.
+ *   - The array comes into existence when the rendering module is loaded on a device.  Under
+ *     CUDA's lazy module loading (the default) that is the first render call of any kind on
+ *     that device, so the first mgpu_render_noalloc call there may itself take the 32 MiB: a
+ *     host that fixes its device-memory budget makes one render call per device at start-up,
+ *     before fixing it.  That first call also looks up the array's device address with
+ *     cudaGetSymbolAddress; make it before any stream capture.
+ *   - The looked-up address stays valid for the life of the process's context on the device:
+ *     after cudaDeviceReset every object of this library on that device is invalid, and this
+ *     entry point must not be called there again.
  *   - All calls share the one array and it keeps the last call's contents; each call clears
  *     what must start at zero itself.  Calls whose work overlaps on the GPU (other streams,
- *     other host threads) race on the array: serialise them.                                */
+ *     other host threads) race on the array: serialise them.
+ *   - mgpu_render_stats_get and mgpu_render_wave_queues read their numbers from the array
+ *     after a call of this entry point, so they report the most recent mgpu_render_noalloc
+ *     call on that device, whichever host thread made it.                                  */
 int mgpu_render_noalloc(const mgpu_scene *scene, const mgpu_render_params *params, mgpu_film *film, void *stream);
 /* Batched rendering: render requests of different scenes, resolutions and sample counts share
  * waves, so scenes too small to fill the GPU alone render together; each request's film gets

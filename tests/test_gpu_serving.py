@@ -73,6 +73,54 @@ def test_same_image_alone_and_in_the_mix(cuda, policy):
     assert stopped_early >= 1  # some error target was met before the cap
 
 
+def test_jobs_admitted_while_others_render_match_alone(cuda):
+    """Continuous batching: jobs are submitted between ticks while earlier jobs are on the GPU
+    (active, part of their samples done); each still finishes with the image and sample count it
+    gets alone."""
+    scenes = _scenes()
+    # (ticks to run before submitting the next group, jobs of the group)
+    schedule = [(0, [0, 1]), (2, [2, 3]), (1, [4]), (3, [5, 6])]
+    with Server(ServerSettings(tick_paths=20000, policy="rotate")) as srv:
+        ids = [srv.add_scene(s) for s in scenes]
+        jids = {}
+        res = {}
+        overlapped = 0
+
+        def harvest():
+            for k, j in jids.items():
+                if k not in res:
+                    info = srv.job(j)
+                    if info["state"] in ("done", "failed"):
+                        res[k] = (info, srv.read(j) if info["state"] == "done" else None)
+                        srv.release(j)
+
+        for ticks, group in schedule:
+            for _ in range(ticks):
+                srv.step()
+                harvest()
+            # the jobs already on the GPU with part of their samples rendered
+            mid = [k for k, j in jids.items() if k not in res and srv.job(j)["state"] == "active"
+                   and 0 < srv.job(j)["spp_done"] < JOBS[k][3]]
+            overlapped += bool(mid) and bool(jids)
+            for k in group:
+                si, side, spp, mx, tgt = JOBS[k]
+                jids[k] = srv.submit(ids[si], _settings(k, side, spp), scenes[si].camera, mx, tgt)
+        for _ in range(100000):
+            left = srv.step()
+            harvest()
+            if left == 0:
+                break
+        harvest()
+    assert overlapped >= 2, "later groups must arrive while earlier jobs are mid-render"
+    assert sorted(res) == list(range(len(JOBS)))
+    for k, job in enumerate(JOBS):
+        info_m, img_m = res[k]
+        (info_a, img_a), = _run(scenes, [job], keys=[k])[0]
+        assert info_m["state"] == info_a["state"] == "done"
+        assert info_m["spp_done"] == info_a["spp_done"]
+        assert np.array_equal(img_m, img_a), f"job {k}: image differs alone and admitted mid-stream"
+
+
 def test_served_image_equals_plain_render(cuda):
     scenes = _scenes()
     mix, _, _ = _run(scenes, JOBS)

@@ -11,7 +11,8 @@ import pytest
 from milton_gb300 import sceneloader as L
 
 HERE = Path(__file__).resolve().parent
-REF_SCENES = Path("/root/reference/mlt/src/exec/scenes")
+# the reference tree, when present (MILTON_REFERENCE, as for the oracle built from its sources)
+REF_SCENES = Path(os.environ.get("MILTON_REFERENCE", "/root/reference")) / "mlt" / "src" / "exec" / "scenes"
 
 
 def _scene(body: str, extra: str = "") -> str:

@@ -7,9 +7,15 @@ comparison is exact (tolerance zero); it runs twice in a row because the fixed a
 previous call's contents and each call must clear what has to start at zero.
 
 This file is collected last so that a failure here cannot hide other tests' results; it also
-passes when run alone in a fresh process.
+passes when run alone in a fresh process.  One test runs in a child process of its own, so
+that the entry point is exercised with no mgpu_render before it in that process, and checks
+with cudaMemGetInfo that a call takes no device memory.
 """
 import ctypes as C
+import subprocess
+import sys
+import textwrap
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -65,3 +71,41 @@ def test_noalloc_rejects_oversized_requests(cuda):
     assert rc == -1
     assert b"exceeds the fixed scratch" in lib.mgpu_last_error()
     assert not film.raw().any()
+
+
+_CHILD = textwrap.dedent("""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from milton_gb300 import _native
+    from milton_gb300 import pathtracer as pt
+    from milton_gb300 import scenegen
+    torch.cuda.set_device(0)
+    lib = _native.load()
+    s = scenegen.plain(0)
+    ds = pt.DeviceScene(s, pt.Accel(s))
+    films = [pt.Film(160, 120) for _ in range(3)]
+    st = pt.RenderSettings(160, 120, 16, max_depth=5, rr_start_depth=3, seed=31)
+    p = st.to_c(s.camera)
+    torch.cuda.synchronize()
+    # the first render call of this process is the allocation-free one; under lazy module
+    # loading it is the call that loads the rendering module (and with it the fixed array)
+    assert lib.mgpu_render_noalloc(ds.handle, C.byref(p), films[0].handle, None) == 0, lib.mgpu_last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    assert lib.mgpu_render_noalloc(ds.handle, C.byref(p), films[1].handle, None) == 0, lib.mgpu_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, ("device memory taken by an allocation-free call", free0 - free1)
+    assert lib.mgpu_render(ds.handle, C.byref(p), films[2].handle, None) == 0, lib.mgpu_last_error()
+    a, b, c = (f.raw() for f in films)
+    assert np.array_equal(a, c) and np.array_equal(b, c)
+    print("ok", free0 - free1)
+""")
+
+
+def test_noalloc_first_call_in_a_fresh_process_takes_no_device_memory(cuda):
+    root = Path(__file__).resolve().parent.parent
+    r = subprocess.run([sys.executable, "-c", _CHILD], cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip().endswith("ok 0")
