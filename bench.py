@@ -87,6 +87,29 @@ def _peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def _l2_copy_peak(torch) -> float:
+    """GB/s of a device copy whose buffers stay in L2 (2 x 16 MiB, read + write bytes, best of 20
+    timed batches of 50 copies): the denominator of the L2 roofline of the traversal kernels,
+    whose working set is served from L2."""
+    n = 16 * 1024 * 1024 // 4
+    a = torch.ones(n, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(20):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(50):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 50 * 2 * a.numel() * 4 / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    del a, b
+    return best
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -399,12 +422,23 @@ def run_ours(args):
     # DRAM traffic per launch: the ncu capture of the same kernel on the small case gives DRAM
     # bytes per ray (profiles/traffic_per_ray.json); scaled here by the rays of an average launch
     traffic = None
+    l2 = None
     tfile = ROOT / "profiles" / "traffic_per_ray.json"
     if tfile.exists():
-        per_ray = json.loads(tfile.read_text()).get(dom, {}).get("dram_bytes_per_ray")
+        tr = json.loads(tfile.read_text()).get(dom, {})
+        per_ray = tr.get("dram_bytes_per_ray")
         rays_total = ext_rays_total if dom == "extend" else sh_rays_total
         if per_ray:
             traffic = per_ray * rays_total / max(kn, 1)
+        # the L2 roofline: the kernel's L2 traffic (ncu lts__t_bytes per ray of the same kernel on
+        # the small case, times the rays of an average launch) over its launch time, against the
+        # measured copy bandwidth of an L2-resident buffer
+        l2_per_ray = tr.get("l2_bytes_per_ray")
+        if l2_per_ray:
+            l2_peak = _l2_copy_peak(torch)
+            l2_ach = (l2_per_ray * rays_total / max(kn, 1)) / ((kms / max(kn, 1)) / 1e3) / 1e9
+            l2 = {"achieved": l2_ach, "peak": l2_peak, "unit": "GB/s", "frac": l2_ach / l2_peak,
+                  "bytes_per_ray": l2_per_ray, "peak_source": "measured: copy of 2 x 16 MiB L2-resident buffers"}
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -423,7 +457,7 @@ def run_ours(args):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                      "peak_source": peaks["source"] + " copy bandwidth",
-                     "bytes_per_ray": {"extend": ext_ray, "shadow": sh_ray}},
+                     "bytes_per_ray": {"extend": ext_ray, "shadow": sh_ray}, "l2": l2},
         "clocks": clk,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -328,10 +328,11 @@ MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32
   return true;
 }
 
-// One leaf: descend, test, then finish (true) or move to the next cell (false).
-template <bool ANY, bool COUNT>
-MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, const Pair *top, uint32_t ntop,
-                       TraceCounts *cnt) {
+// Descends from the current node to the next leaf: returns the leaf slot (w0: count << 2 | 3,
+// w1: first leaf record) and the exit t of its cell in tmax_out; far children go on the stack.
+template <bool COUNT>
+MGPU_HD void trav_descend(const SceneView &s, TravState &st, TravEntry *stack, const Pair *top, uint32_t ntop,
+                          TraceCounts *cnt, uint32_t &leaf_w0, uint32_t &leaf_w1, float &tmax_out) {
   const float o[3] = {st.pre.o.x, st.pre.o.y, st.pre.o.z};
   const float iv[3] = {st.inv.x, st.inv.y, st.inv.z};
   uint32_t w0 = st.w0, w1 = st.w1;
@@ -370,6 +371,31 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, cons
     w0 = n0; w1 = n1;
   }
   if (COUNT) cnt->nodes++;
+  leaf_w0 = w0;
+  leaf_w1 = w1;
+  tmax_out = tmax;
+}
+
+// After a leaf has been tested: finish (true) or move to the next cell on the stack (false).
+template <bool ANY>
+MGPU_HD bool trav_after_leaf(TravState &st, const TravEntry *stack, float tmax) {
+  // early exit: the best hit lies inside this cell, later cells are farther
+  if (!ANY && st.best_prim >= 0 && st.best <= tmax + kCellEps * fabsf(tmax)) return true;
+  if (st.sp == 0 || ++st.steps >= kMaxLeafSteps) return true;
+  --st.sp;
+  st.tmin = tmax;
+  st.w0 = stack[st.sp].w0; st.w1 = stack[st.sp].w1; st.tmax = stack[st.sp].tmax;
+  if (!ANY && st.best_prim >= 0 && st.best < st.tmin) return true;
+  return false;
+}
+
+// One leaf: descend, test, then finish (true) or move to the next cell (false).
+template <bool ANY, bool COUNT>
+MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, const Pair *top, uint32_t ntop,
+                       TraceCounts *cnt) {
+  uint32_t w0, w1;
+  float tmax;
+  trav_descend<COUNT>(s, st, stack, top, ntop, cnt, w0, w1, tmax);
   const uint32_t count = w0 >> 2;
   for (uint32_t i = 0; i < count; ++i) {
     if (COUNT) cnt->tris++;
@@ -385,14 +411,7 @@ MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, cons
       if (ANY) return true;
     }
   }
-  // early exit: the best hit lies inside this cell, later cells are farther
-  if (!ANY && st.best_prim >= 0 && st.best <= tmax + kCellEps * fabsf(tmax)) return true;
-  if (st.sp == 0 || ++st.steps >= kMaxLeafSteps) return true;
-  --st.sp;
-  st.tmin = tmax;
-  st.w0 = stack[st.sp].w0; st.w1 = stack[st.sp].w1; st.tmax = stack[st.sp].tmax;
-  if (!ANY && st.best_prim >= 0 && st.best < st.tmin) return true;
-  return false;
+  return trav_after_leaf<ANY>(st, stack, tmax);
 }
 
 // ANY = shadow query (returns on the first hit inside (tmin, tmax)).
@@ -477,6 +496,132 @@ __device__ __forceinline__ void persistent_trace(View view, const Pair *top, uin
     if (have && trav_step<ANY, COUNT>(*sv, st, stack, top, ntop, cnt)) {
       store(idx, st.best_prim >= 0, st);
       have = false;
+    }
+  }
+}
+
+// Grid-stride traversal with the leaf triangles shared by the warp.  Every lane descends its own
+// ray to its next leaf; then the warp tests the triangles of all the lanes' leaves together, 32
+// (ray, triangle) pairs at a time, each test with the owning lane's ray (its shear constants,
+// tmin and current best passed by shuffles), and the results go back to the owners: for a closest
+// hit the smallest (t, index in the leaf) per owner through a shared-memory atomicMin on wkey[32]
+// (a per-warp array in shared memory), for an any hit a bit per owner.  Lanes whose ray has
+// finished test other lanes' triangles instead of idling, so a leaf of many triangles no longer
+// holds the warp in a loop that few lanes execute.  The result of every ray is the one trav_step
+// gives: the winner is the smallest t below the ray's best, ties to the first triangle in the
+// leaf's order, and its owner re-runs that one test for t and barycentrics.
+// All 32 lanes of every warp must call this (rays are taken in warp-aligned rounds).
+template <bool ANY, bool COUNT, bool SPH, class View, class Load, class Store>
+__device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load, Store store, TraceCounts *cnt,
+                                                uint32_t &rays_done, unsigned long long *wkey) {
+  const unsigned kFull = 0xFFFFFFFFu;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  TravState st{};
+  TravEntry stack[kMaxStack];
+  for (uint32_t r0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < n; r0 += stride) {
+    const uint32_t i = r0 + lane;
+    bool active = false;
+    const SceneView *sv = nullptr;
+    if (i < n) {
+      sv = &view(i);
+      Ray r;
+      load(i, r);
+      ++rays_done;
+      active = trav_init<SPH>(*sv, r, nullptr, 0, st, ANY);
+      if (!active) store(i, st.best_prim >= 0, st);
+    }
+    while (__any_sync(kFull, active)) {
+      uint32_t lw0 = kLeafTag, lw1 = 0;
+      float cell_tmax = 0.0f;
+      if (active) trav_descend<COUNT>(*sv, st, stack, nullptr, 0, cnt, lw0, lw1, cell_tmax);
+      const uint32_t count = active ? (lw0 >> 2) : 0u;
+      // inclusive prefix sum of the leaf sizes over the warp
+      uint32_t incl = count;
+      for (uint32_t d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += v;
+      }
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      const uint32_t excl = incl - count;
+      // the owner's ray, as the tests need it
+      const uint32_t kpack = (uint32_t)st.pre.kx | ((uint32_t)st.pre.ky << 2) | ((uint32_t)st.pre.kz << 4);
+      const unsigned long long ltp = active ? (unsigned long long)sv->ltris : 0ull;
+      if (!ANY) wkey[lane] = ~0ull;
+      __syncwarp(kFull);
+      uint32_t hit_owners = 0u;
+      for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t k = base + lane;
+        // owner = the first lane whose inclusive sum exceeds k
+        uint32_t o = 0;
+        for (uint32_t step = 16; step >= 1; step >>= 1) {
+          const uint32_t v = __shfl_sync(kFull, incl, o + step - 1);
+          if (v <= k) o += step;
+        }
+        RayPre p;
+        p.o.x = __shfl_sync(kFull, st.pre.o.x, o);
+        p.o.y = __shfl_sync(kFull, st.pre.o.y, o);
+        p.o.z = __shfl_sync(kFull, st.pre.o.z, o);
+        p.sx = __shfl_sync(kFull, st.pre.sx, o);
+        p.sy = __shfl_sync(kFull, st.pre.sy, o);
+        p.sz = __shfl_sync(kFull, st.pre.sz, o);
+        const uint32_t kp = __shfl_sync(kFull, kpack, o);
+        p.kx = (int)(kp & 3u); p.ky = (int)((kp >> 2) & 3u); p.kz = (int)((kp >> 4) & 3u);
+        const float tmin_o = __shfl_sync(kFull, st.ray_tmin, o);
+        const float best_o = __shfl_sync(kFull, st.best, o);
+        const uint32_t first_o = __shfl_sync(kFull, lw1, o);
+        const uint32_t excl_o = __shfl_sync(kFull, excl, o);
+        const F4 *lt = reinterpret_cast<const F4 *>(__shfl_sync(kFull, ltp, o));
+        if (k < total) {
+          if (COUNT) cnt->tris++;
+          const uint32_t idx = k - excl_o;
+          const int64_t r = 3 * ((int64_t)first_o + idx);
+          F4 a = load_f4(lt, r + 0);
+          F4 b = load_f4(lt, r + 1);
+          F4 c = load_f4(lt, r + 2);
+          const bool culled = (f_bits(b.w) & 1u) != 0u;
+          float t, b1, b2;
+          if (intersect_tri(p, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), culled, tmin_o, best_o, t,
+                            b1, b2)) {
+            if (ANY) hit_owners |= 1u << o;
+            else atomicMin(&wkey[o], ((unsigned long long)f_bits(t) << 32) | idx);
+          }
+        }
+      }
+      bool found = false;
+      if (ANY) {
+        found = ((__reduce_or_sync(kFull, hit_owners) >> lane) & 1u) != 0u;
+      } else {
+        __syncwarp(kFull);
+        const unsigned long long key = wkey[lane];
+        __syncwarp(kFull);
+        if (active && key != ~0ull) {
+          // the winner: redo its test for t and the barycentrics (the same inputs, the same result)
+          const uint32_t idx = (uint32_t)(key & 0xFFFFFFFFull);
+          const int64_t r = 3 * ((int64_t)lw1 + idx);
+          F4 a = load_f4(sv->ltris, r + 0);
+          F4 b = load_f4(sv->ltris, r + 1);
+          F4 c = load_f4(sv->ltris, r + 2);
+          float t, b1, b2;
+          if (intersect_tri(st.pre, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z),
+                            (f_bits(b.w) & 1u) != 0u, st.ray_tmin, st.best, t, b1, b2)) {
+            st.best = t; st.best_prim = (int32_t)f_bits(a.w); st.bb1 = b1; st.bb2 = b2;
+          }
+        }
+      }
+      if (active) {
+        bool done;
+        if (ANY && found) {
+          st.best_prim = 0;  // occluded: any non-negative value
+          done = true;
+        } else {
+          done = trav_after_leaf<ANY>(st, stack, cell_tmax);
+        }
+        if (done) {
+          store(i, st.best_prim >= 0, st);
+          active = false;
+        }
+      }
     }
   }
 }

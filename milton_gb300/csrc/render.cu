@@ -293,8 +293,19 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderArgs a) {
 }
 
 // extend: closest hit for the live queue of bounce b
-template <bool COUNT, bool PERSIST, bool SPH = false>
-__global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_extend(RenderArgs a, int b) {
+// traversal kernel shapes (mgpu_tune_set "persistent" / "coop_leaf")
+constexpr int kShapeGrid = 0;     // grid-stride, one ray per lane to completion
+constexpr int kShapePersist = 1;  // persistent warps with per-lane refill
+constexpr int kShapeCoop = 2;     // grid-stride, leaf triangles shared by the warp
+#ifndef MGPU_COOP_MIN_BLOCKS
+#define MGPU_COOP_MIN_BLOCKS 12
+#endif
+// resident blocks per SM of the warp-cooperative traversal shape (its register budget)
+constexpr int kCoopMinBlocks = MGPU_COOP_MIN_BLOCKS;
+
+template <bool COUNT, int SHAPE, bool SPH = false>
+__global__ void __launch_bounds__(kBlock, SHAPE == kShapeCoop ? kCoopMinBlocks : kTravMinBlocks)
+    k_extend(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
   float4 *qhit = a.qhit;
@@ -316,10 +327,14 @@ __global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_extend(RenderArgs a,
     qhit[i] = make_float4(hit ? st.best : INFINITY, __int_as_float(hit ? st.best_prim : -1), hit ? st.bb1 : 0.0f,
                           hit ? st.bb2 : 0.0f);
   };
-  if (PERSIST)
+  if (SHAPE == kShapePersist) {
     persistent_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
-  else
+  } else if (SHAPE == kShapeCoop) {
+    __shared__ unsigned long long wkey[kBlock];
+    grid_trace_coop<false, COUNT, SPH>(view_of, n, load, store, &c, rays, wkey + (threadIdx.x & ~31u));
+  } else {
     grid_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
+  }
   if (COUNT && rays) {
     atomicAdd(&a.tcount[0], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[1], (unsigned long long)c.refs);
@@ -532,8 +547,9 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
 }
 
 // shadow: any-hit query per queued light sample; an occluded sample's slot is zeroed
-template <bool COUNT, bool PERSIST, bool SPH = false>
-__global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_shadow(RenderArgs a, int b) {
+template <bool COUNT, int SHAPE, bool SPH = false>
+__global__ void __launch_bounds__(kBlock, SHAPE == kShapeCoop ? kCoopMinBlocks : kTravMinBlocks)
+    k_shadow(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrNee + b];
   const float4 *so = a.so, *sd = a.sd;
   float4 *slots = a.slots;
@@ -556,10 +572,13 @@ __global__ void __launch_bounds__(kBlock, kTravMinBlocks) k_shadow(RenderArgs a,
   auto store = [&](uint32_t i, bool hit, const TravState &) {
     if (hit) slots[__float_as_uint(so[i].w)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   };
-  if (PERSIST)
+  if (SHAPE == kShapePersist) {
     persistent_trace<true, COUNT, SPH>(view_of, nullptr, 0, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
-  else
+  } else if (SHAPE == kShapeCoop) {
+    grid_trace_coop<true, COUNT, SPH>(view_of, n, load, store, &c, rays, nullptr);
+  } else {
     grid_trace<true, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
+  }
   if (COUNT && rays) {
     atomicAdd(&a.tcount[4], (unsigned long long)c.nodes);
     atomicAdd(&a.tcount[5], (unsigned long long)c.refs);
@@ -749,6 +768,9 @@ struct Workspace {
 // process-wide tuning knobs (mgpu_tune_set)
 struct Tuning {
   std::atomic<int> persistent{0};     // persistent warp-level traversal with ray refill
+  // grid-stride traversal with the leaf triangles shared by the warp: bit 0 for the shadow
+  // (any-hit) kernel, bit 1 for the extension (closest-hit) kernel
+  std::atomic<int> coop_leaf{1};
   std::atomic<int> bin_shadow{1};     // counting-sort shadow rays by (light, origin cell)
   std::atomic<int> bin_extension{1};  // counting-sort extension rays by (octant, origin cell)
   // waves of fewer paths skip binning: sorting a few hundred thousand rays costs more (four
@@ -1166,10 +1188,17 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   }
 
   const bool persist = g_tune.persistent.load() != 0;
+  const bool coop_sh = (g_tune.coop_leaf.load() & 1) != 0, coop_ext = (g_tune.coop_leaf.load() & 2) != 0;
   bool sph = false;  // a job's scene has analytic spheres: the traversal kernels that test them
   for (const Job &j : jobs) sph = sph || j.scene->view.nsphere > 0;
-  auto kext = sph ? k_extend<COUNT, false, true> : persist ? k_extend<COUNT, true> : k_extend<COUNT, false>;
-  auto kshw = sph ? k_shadow<COUNT, false, true> : persist ? k_shadow<COUNT, true> : k_shadow<COUNT, false>;
+  auto kext = sph        ? k_extend<COUNT, kShapeGrid, true>
+              : persist  ? k_extend<COUNT, kShapePersist>
+              : coop_ext ? k_extend<COUNT, kShapeCoop>
+                         : k_extend<COUNT, kShapeGrid>;
+  auto kshw = sph        ? k_shadow<COUNT, kShapeGrid, true>
+              : persist  ? k_shadow<COUNT, kShapePersist>
+              : coop_sh  ? k_shadow<COUNT, kShapeCoop>
+                         : k_shadow<COUNT, kShapeGrid>;
   const int g_gen = grid_for((const void *)k_generate, 0);
   const int g_ext = grid_for((const void *)kext, 0);
   const int g_sha = grid_for((const void *)k_shade<true>, 0);
@@ -1468,15 +1497,18 @@ int mgpu_tune_set(const char *key, int64_t value) {
   if (!key) return fail(MGPU_E_INVALID, "mgpu_tune_set: null key");
   std::string k(key);
   if (k == "persistent") g_tune.persistent.store(value != 0);
+  else if (k == "coop_leaf" && value >= 0 && value <= 3) g_tune.coop_leaf.store((int)value);
   else if (k == "bin_shadow") g_tune.bin_shadow.store(value != 0);
   else if (k == "bin_extension") g_tune.bin_extension.store(value != 0);
   else if (k == "bin_min_paths" && value >= 0) g_tune.bin_min_paths.store(value);
   else if (k == "carveout" && value >= -1 && value <= 100) {
     // the L1 / shared-memory split of the kernels that spill and chase pointers through L1
-    const void *kerns[] = {(const void *)k_extend<false, false>, (const void *)k_extend<false, true>,
-                           (const void *)k_extend<true, false>,  (const void *)k_extend<true, true>,
-                           (const void *)k_shadow<false, false>, (const void *)k_shadow<false, true>,
-                           (const void *)k_shadow<true, false>,  (const void *)k_shadow<true, true>,
+    const void *kerns[] = {(const void *)k_extend<false, kShapeGrid>, (const void *)k_extend<false, kShapePersist>,
+                           (const void *)k_extend<false, kShapeCoop>,  (const void *)k_extend<true, kShapeGrid>,
+                           (const void *)k_extend<true, kShapePersist>, (const void *)k_extend<true, kShapeCoop>,
+                           (const void *)k_shadow<false, kShapeGrid>, (const void *)k_shadow<false, kShapePersist>,
+                           (const void *)k_shadow<false, kShapeCoop>,  (const void *)k_shadow<true, kShapeGrid>,
+                           (const void *)k_shadow<true, kShapePersist>, (const void *)k_shadow<true, kShapeCoop>,
                            (const void *)k_shade<false>, (const void *)k_shade<true>};
     for (const void *kf : kerns)
       MGPU_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)value));
@@ -1489,6 +1521,7 @@ int mgpu_tune_get(const char *key, int64_t *value) {
   if (!key || !value) return fail(MGPU_E_INVALID, "mgpu_tune_get: null argument");
   std::string k(key);
   if (k == "persistent") *value = g_tune.persistent.load();
+  else if (k == "coop_leaf") *value = g_tune.coop_leaf.load();
   else if (k == "bin_shadow") *value = g_tune.bin_shadow.load();
   else if (k == "bin_extension") *value = g_tune.bin_extension.load();
   else if (k == "bin_min_paths") *value = g_tune.bin_min_paths.load();

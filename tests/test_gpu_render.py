@@ -98,18 +98,19 @@ def test_film_determinism_and_pass_splits(cuda):
 
 
 def test_tuning_knobs_do_not_change_the_image(cuda):
-    # queue binning and persistent traversal reorder work, never the result
+    # queue binning, persistent traversal and warp-shared leaf tests reorder work, never the result
     s = scenegen.random_scene(12, 20000)
     acc = pt.Accel(s)
     ds = pt.DeviceScene(s, acc)
     st = pt.RenderSettings(48, 40, 8, max_depth=6, rr_start_depth=3, seed=4)
     raws = []
-    saved = {k: pt.tune_get(k) for k in ("persistent", "bin_shadow", "bin_extension", "bin_min_paths")}
+    saved = {k: pt.tune_get(k) for k in ("persistent", "coop_leaf", "bin_shadow", "bin_extension", "bin_min_paths")}
     pt.tune("bin_min_paths", 0)  # bin even this small wave
     try:
-        for persist in (0, 1):
+        for shape in ("grid", "persistent", "coop_shadow", "coop_both"):
             for bins in ((0, 0), (1, 0), (1, 1)):
-                pt.tune("persistent", persist)
+                pt.tune("persistent", int(shape == "persistent"))
+                pt.tune("coop_leaf", {"grid": 0, "persistent": 0, "coop_shadow": 1, "coop_both": 3}[shape])
                 pt.tune("bin_shadow", bins[0])
                 pt.tune("bin_extension", bins[1])
                 f = pt.Film(48, 40)
