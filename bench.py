@@ -230,60 +230,124 @@ def _luminance(x):
     return x.mean(axis=-1)
 
 
-def _frame_parity(scene, dscene, film, img, cpu, pt, torch):
-    """Parity of the benchmark frame against the FP64 oracle (rank 0, after the timed region):
+def _image_parity(scene, dscene, tree, W, H, spp, depth, rr, rows_z, rows_hi, hispp_spp, pt, torch, film=None,
+                  img=None, oracle_band=None, ns=4, camera=None, stream=0):
+    """Parity of a rendered image against the FP64 oracle (rank 0, after the timed region):
       path_agreement   per-path radiance, GPU vs oracle with the same seed and counter RNG, on
-                       the CPU rows at 4 samples per pixel (within 1e-4 + 2e-3 relative)
-      z                per-pixel mean luminance of the GPU frame (seed SEED) against the oracle's
-                       (seed CPU_SEED, independent) on the CPU rows: z = difference / standard
-                       error; z_frac = fraction of pixels with |z| > 4
-      rmse_*_vs_fp64_hispp  RMSE of the GPU frame and of the oracle image, both at the frame's
-                       spp, against an FP64 oracle image at hispp_spp of the hispp rows"""
+                       rows_z at the first ns passes (within 1e-4 + 2e-3 relative)
+      z                per-pixel mean luminance of the GPU image (seed SEED, all spp passes)
+                       against the oracle's (seed CPU_SEED, independent) on rows_z: z = difference
+                       / standard error; z_frac = fraction of pixels with |z| > 4
+      rmse_*_vs_fp64_hispp  RMSE of the GPU image and of the oracle image, both at spp, against an
+                       FP64 oracle image of rows_hi at hispp_spp passes (seed HISPP_SEED)
+    film / img: the GPU film and its mean when the caller already rendered them (else rendered
+    here); oracle_band: the oracle's rows_z render (mean, per_path) when already made."""
     import numpy as np
     from oracle import pyoracle
-    r0, r1 = CPU_ROWS
+    r0, r1 = rows_z
+    h0, h1 = rows_hi
+    assert r0 <= h0 and h1 <= r1
+    kw = {} if camera is None else {"camera": camera}
+    if film is None:
+        film = pt.Film(W, H)
+        pt.render(dscene, pt.RenderSettings(W, H, spp, max_depth=depth, rr_start_depth=rr, seed=SEED, stream_id=stream),
+                  film, **kw)
+        img = film.mean()
     # same-sample per-path agreement
-    ns = 4
-    out = torch.zeros((W_IMG * H_IMG * ns, 4), dtype=torch.float32, device="cuda")
-    pf = pt.Film(W_IMG, H_IMG)
-    pt.render(dscene, pt.RenderSettings(W_IMG, H_IMG, SPP, sample_count=ns, max_depth=MAX_DEPTH,
-                                        rr_start_depth=RR_START, seed=SEED), pf, path_out=out)
+    out = torch.zeros((W * H * ns, 4), dtype=torch.float32, device="cuda")
+    pf = pt.Film(W, H)
+    pt.render(dscene, pt.RenderSettings(W, H, spp, sample_count=ns, max_depth=depth, rr_start_depth=rr, seed=SEED,
+                                        stream_id=stream), pf, path_out=out, **kw)
     torch.cuda.synchronize()
-    pg = out.cpu().numpy().reshape(H_IMG, W_IMG, ns, 4)[r0:r1, ..., :3].astype(np.float64)
+    pg = out.cpu().numpy().reshape(H, W, ns, 4)[r0:r1, ..., :3].astype(np.float64)
+    del out
     pf.close()
-    _, po, _ = pyoracle.render(scene, cpu["tree"], W_IMG, H_IMG, SPP, sample_count=ns, max_depth=MAX_DEPTH,
-                               rr_start=RR_START, seed=SEED, rows=CPU_ROWS, per_path=True)
+    oscene = scene if camera is None else _with_camera(scene, camera)
+    _, po, _ = pyoracle.render(oscene, tree, W, H, spp, sample_count=ns, max_depth=depth, rr_start=rr, seed=SEED,
+                               stream=stream, rows=rows_z, per_path=True)
     close = np.abs(pg - po) <= 1e-4 + 2e-3 * np.maximum(np.abs(pg), np.abs(po))
     agree = float(np.all(close, axis=-1).mean())
     # z-test on per-pixel mean luminance, independent seeds
+    if oracle_band is None:
+        m, pp, _ = pyoracle.render(oscene, tree, W, H, spp, max_depth=depth, rr_start=rr, seed=CPU_SEED, rows=rows_z,
+                                   per_path=True)
+        oracle_band = {"mean": m, "per_path": pp}
     raw = film.raw()[:, r0:r1].astype(np.float64)  # [0]: sum rgb, count; [1]: compensation rgb, sum of lum^2
     n_g = raw[0, ..., 3]
     m_g = _luminance(img[r0:r1])
-    v_g = np.maximum(raw[1, ..., 3] / n_g - m_g ** 2, 0.0) * n_g / (n_g - 1)
-    lo = _luminance(cpu["per_path"])  # (rows, W, spp)
+    v_g = np.maximum(raw[1, ..., 3] / n_g - m_g ** 2, 0.0) * n_g / np.maximum(n_g - 1, 1)
+    lo = _luminance(oracle_band["per_path"])  # (rows, W, spp)
     n_o = lo.shape[-1]
     m_o = lo.mean(-1)
-    v_o = lo.var(-1, ddof=1)
+    v_o = lo.var(-1, ddof=1) if n_o > 1 else np.zeros_like(m_o)
     se = np.sqrt(v_g / n_g + v_o / n_o)
     with np.errstate(divide="ignore", invalid="ignore"):
         z = np.where(se > 0, (m_g - m_o) / se, 0.0)
     z_frac = float((np.abs(z) > 4).mean())
     # FP64 high-spp image of a few rows
-    h0, h1 = CFG["hispp_rows"]
     t0 = time.perf_counter()
-    hi, _, _ = pyoracle.render(scene, cpu["tree"], W_IMG, H_IMG, CFG["hispp_spp"], max_depth=MAX_DEPTH,
-                               rr_start=RR_START, seed=HISPP_SEED, rows=(h0, h1))
+    hi, _, _ = pyoracle.render(oscene, tree, W, H, hispp_spp, max_depth=depth, rr_start=rr, seed=HISPP_SEED,
+                               rows=rows_hi)
     hi_s = time.perf_counter() - t0
     rmse_g = float(np.sqrt(((img[h0:h1] - hi) ** 2).mean()))
-    rmse_o = float(np.sqrt(((cpu["mean"][h0 - r0:h1 - r0] - hi) ** 2).mean()))
-    return {"path_agreement": agree, "path_agreement_sample": f"rows {r0}-{r1 - 1}, first {ns} of {SPP} passes, "
-                                                             f"same seed ({W_IMG * (r1 - r0) * ns} paths)",
-            "z_frac": z_frac, "z_abs_mean": float(np.abs(z).mean()), "z_sample": f"rows {r0}-{r1 - 1}, {SPP} spp, "
-                                                                               "GPU seed vs an independent oracle seed",
+    rmse_o = float(np.sqrt(((oracle_band["mean"][h0 - r0:h1 - r0] - hi) ** 2).mean()))
+    return {"path_agreement": agree, "path_agreement_sample": f"rows {r0}-{r1 - 1}, first {ns} of {spp} passes, "
+                                                             f"same seed ({W * (r1 - r0) * ns} paths)",
+            "z_frac": z_frac, "z_abs_mean": float(np.abs(z).mean()),
+            "z_sample": f"rows {r0}-{r1 - 1}, {spp} spp, GPU seed vs an independent oracle seed",
             "rmse_gpu_vs_fp64_hispp": rmse_g, "rmse_oracle_vs_fp64_hispp": rmse_o,
             "rmse_gpu_over_oracle": rmse_g / rmse_o if rmse_o > 0 else None,
-            "hispp": f"FP64 oracle, rows {h0}-{h1 - 1}, {CFG['hispp_spp']} spp, {hi_s:.1f} s",
+            "hispp": f"FP64 oracle, rows {h0}-{h1 - 1}, {hispp_spp} spp, {hi_s:.1f} s",
             "image_mean_gpu": float(img[h0:h1].mean()), "image_mean_fp64_hispp": float(hi.mean())}
+
+
+def _with_camera(scene, camera):
+    import copy
+    s2 = copy.copy(scene)
+    s2.camera = camera
+    return s2
+
+
+def _frame_parity(scene, dscene, film, img, cpu, pt, torch):
+    """The benchmark frame's parity (_image_parity) on the CPU-baseline rows, reusing the
+    cpu_baseline leg's oracle render as the independent-seed image."""
+    return _image_parity(scene, dscene, cpu["tree"], W_IMG, H_IMG, SPP, MAX_DEPTH, RR_START, CPU_ROWS,
+                         CFG["hispp_rows"], CFG["hispp_spp"], pt, torch, film=film, img=img,
+                         oracle_band={"mean": cpu["mean"], "per_path": cpu["per_path"]})
+
+
+def _hit_parity(scene, dscene, tree, n, pt, torch):
+    """Closest-hit primitive ids of the GPU against the oracle's kd traversal on n camera rays and
+    n rays from random points of the scene's box; a mismatch counts as a tie when the oracle's
+    brute force finds the two nearest hits within 1e-6 relative t, or the GPU's t within 1e-6 of
+    the oracle's (at most 64 mismatches are classified by brute force)."""
+    import numpy as np
+    from oracle import pyoracle
+    sys.path.insert(0, str(ROOT / "tests"))
+    from raygen import camera_rays, classify, sphere_rays
+    lo, hi = scene.tri_v.reshape(-1, 3).min(0), scene.tri_v.reshape(-1, 3).max(0)
+    rays = np.concatenate([camera_rays(scene.camera, n, 41), sphere_rays(lo, hi, n, 42)])
+    h = pt.trace_closest(dscene, torch.from_numpy(rays).cuda())
+    torch.cuda.synchronize()
+    h = h.cpu().numpy()
+    pg, tg = h[:, 1].view(np.int32).astype(np.int64), h[:, 0].astype(np.float64)
+    t0 = time.perf_counter()
+    to, po, _, _ = pyoracle.trace_closest(tree, scene.tri_v, scene.tri_flags, rays)
+    bad = np.nonzero(pg != po)[0]
+    classified = bad[:64]
+    t2 = np.full(len(rays), np.inf)
+    if classified.size:
+        _, _, t2b, _ = pyoracle.trace_closest(None, scene.tri_v, scene.tri_flags, rays[classified])
+        t2[classified] = t2b
+    r = classify(po[classified], to[classified], t2[classified], pg[classified], tg[classified]) \
+        if classified.size else {"ties": 0, "mismatches": 0}
+    both = (po >= 0) & (pg == po)
+    rel = np.abs(tg[both] - to[both]) / np.maximum(to[both], 1e-30)
+    return {"rays": int(len(rays)), "identical_ids": int((pg == po).sum()), "differing": int(bad.size),
+            "of_which_ties": int(r["ties"]), "of_which_mismatches": int(r["mismatches"]),
+            "classified": int(classified.size), "t_rel_err_mean": float(rel.mean()) if rel.size else 0.0,
+            "t_abs_err_max_over_max_t_1": float((np.abs(tg[both] - to[both]) / np.maximum(to[both], 1.0)).max())
+            if rel.size else 0.0, "oracle_s": round(time.perf_counter() - t0, 1)}
 
 
 def run_ours(args):
@@ -524,11 +588,25 @@ def run_batched(args):
 
     ms_batch = timed(batched)
     tris = sum(ds.scene.ntri for ds, _ in reqs)
+    parity = None
+    if not args.no_parity:
+        # one representative request (median triangle count among the frames of at most 512
+        # pixels a side) as the batch left it, against the FP64 oracle
+        from oracle import pyoracle
+        cand = sorted((ds.scene.ntri, k) for k, (ds, st) in enumerate(reqs) if st.width <= 512)
+        k = cand[len(cand) // 2][1]
+        ds, st = reqs[k]
+        f = films[k]
+        mid_row = st.height // 2
+        parity = {"request": k, "triangles": ds.scene.ntri, "size": [st.width, st.height], "spp": st.spp}
+        parity.update(_image_parity(ds.scene, ds, pyoracle.Tree(ds.scene.tri_v), st.width, st.height, st.spp,
+                                    MAX_DEPTH, RR_START, (mid_row - 8, mid_row + 8), (mid_row - 1, mid_row + 1), 1024,
+                                    pt, torch, film=f, img=f.mean(), stream=k))
     out = {"metric": METRIC, "workload": "batched", "value": paths / ms_batch / 1e3, "unit": UNIT,
            "plain_value": paths / ms_plain / 1e3, "batched_over_plain": ms_plain / ms_batch,
            "ms_per_step": ms_batch, "plain_ms_per_step": ms_plain, "steps": args.steps, "warmup": args.warmup,
            "config": {"scenes": len(reqs), "triangles": tris, "paths_per_step": paths,
-                      "setup_s": round(setup_s, 1), "autotuned": tuned}}
+                      "setup_s": round(setup_s, 1), "autotuned": tuned}, "parity": parity}
     print(json.dumps(out), flush=True)
     return 0
 
@@ -620,12 +698,43 @@ def run_serving(args):
     e1.record()
     torch.cuda.synchronize()
     plain_s = e0.elapsed_time(e1) / 1e3
+    stop_rule = None
+    if not args.no_parity:
+        # the stop rule against an FP64 image: for up to three jobs that stopped at their error
+        # target (the smallest frames on the smallest scenes), the luminance RMSE of the served
+        # image against a 1024-spp FP64 oracle image of 8 rows, beside the film's estimate
+        import numpy as np
+        from oracle import pyoracle
+        done_early = [r for r in reqs if infos[r["id"]]["reached_target"] and r["width"] <= 512]
+        done_early.sort(key=lambda r: (scenes[r["scene"]].ntri, r["width"]))
+        trees = {}
+        stop_rule = []
+        for r in done_early[:3]:
+            info = infos[r["id"]]
+            sid, st, cam, _, _ = make_job(r)
+            st.sample_count = info["spp_done"]
+            f = films[(st.width, st.height)]
+            f.clear()
+            pt.render(dscenes[r["scene"]], st, f, camera=cam)  # the served image (equal to it, checked above)
+            img = f.mean()
+            if r["scene"] not in trees:
+                trees[r["scene"]] = pyoracle.Tree(scenes[r["scene"]].tri_v)
+            h0 = st.height // 2 - 4
+            t0 = time.perf_counter()
+            hi, _, _ = pyoracle.render(_with_camera(scenes[r["scene"]], cam), trees[r["scene"]], st.width, st.height,
+                                       1024, max_depth=MAX_DEPTH, rr_start=RR_START, seed=HISPP_SEED, rows=(h0, h0 + 8))
+            rm = float(np.sqrt(((_luminance(img[h0:h0 + 8]) - _luminance(hi)) ** 2).mean()))
+            stop_rule.append({"request": r["id"], "size": st.width, "triangles": scenes[r["scene"]].ntri,
+                              "spp_done": info["spp_done"], "target_rmse": target_rmse,
+                              "estimated_rmse": info["rmse"], "rmse_vs_fp64_1024spp_8_rows": rm,
+                              "oracle_s": round(time.perf_counter() - t0, 1)})
     spp_hist = {}
     for v in infos.values():
         spp_hist[v["spp_done"]] = spp_hist.get(v["spp_done"], 0) + 1
     out = {"metric": METRIC, "workload": "serving", "value": paths / busy / 1e6, "unit": UNIT,
            "wall_value": paths / (t_end - t_start) / 1e6, "plain_value": paths / plain_s / 1e6,
            "served_over_plain": plain_s / busy, "latency": lat, "images_equal_plain": same,
+           "stop_rule_vs_fp64": stop_rule,
            "clocks": clk,
            "config": {"requests": len(reqs), "rate_per_s": args.rate, "scenes": len(scenes),
                       "triangles": [s.ntri for s in scenes], "target_rmse": target_rmse,
@@ -700,8 +809,19 @@ def run_large(args):
                       "kd_max_depth_param": kd_depth, "kd_node_pairs": kst["node_pairs"], "kd_refs": kst["refs"],
                       "kd_leaf_depth_max": kst["max_depth"],
                       "device_scene_bytes": dscene.nbytes,
-                      "cpu_baseline": "not run: the FP64 oracle's single-threaded kd build of 20 M triangles "
-                                      "alone takes minutes; the mid line carries the CPU baseline"}}
+                      "cpu_baseline": "not run here: the mid line carries the CPU baseline"}}
+    if not args.no_parity:
+        # parity against the FP64 oracle, which traverses the product's tree read from its
+        # serialisation (node-for-node the tree its own restated build gives, tests/test_kdtree.py;
+        # that build takes minutes at 20 M triangles)
+        from oracle import pyoracle
+        t0 = time.perf_counter()
+        tree = pyoracle.Tree.from_serial(scene.tri_v, *accel.serialize())
+        out["parity"] = {"hit_ids": _hit_parity(scene, dscene, tree, 1 << 15, pt, torch),
+                         "oracle_tree": "the product's tree from its serialisation",
+                         "oracle_tree_s": round(time.perf_counter() - t0, 1)}
+        out["parity"].update(_image_parity(scene, dscene, tree, W, H, spp, depth, RR_START, (1020, 1024), (1022, 1023),
+                                           512, pt, torch, ns=1))
     print(json.dumps(out), flush=True)
     return 0
 
@@ -733,6 +853,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="batched / serving / large: skip the FP64 parity check")
     ap.add_argument("--profile-case", action="store_true", help="small two-frame case for ncu captures")
     ap.add_argument("--workload", default="mid", choices=["mid", "plain", "batched", "serving", "large"],
                     help="mid (default, the benchmark line), plain (the CPU-runnable frame), batched (64 scenes, "

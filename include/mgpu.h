@@ -357,6 +357,8 @@ int mgpu_profile_read(double *ms6, uint64_t *launches6);
  *   "coop_leaf"      0..3 warp-shared leaf tests: the triangles of all the lanes' current leaves
  *                    are tested by the whole warp, 32 at a time; bit 0 = shadow (any-hit)
  *                    kernel, bit 1 = extension (closest-hit) kernel (default 1)
+ *   "trav_block"     64 / 128 / 256  threads per block of the grid-stride and warp-shared
+ *                    traversal kernels, at the same threads (and registers) per SM (default 256)
  *   "bin_shadow"     0/1  counting-sort shadow rays by (light, origin cell) (default 1)
  *   "bin_extension"  0/1  counting-sort extension rays by (direction octant, origin cell) (default 1)
  *   "bin_min_paths"  n    waves of fewer paths are not binned (default 2^22)

@@ -303,8 +303,10 @@ constexpr int kShapeCoop = 2;     // grid-stride, leaf triangles shared by the w
 // resident blocks per SM of the warp-cooperative traversal shape (its register budget)
 constexpr int kCoopMinBlocks = MGPU_COOP_MIN_BLOCKS;
 
-template <bool COUNT, int SHAPE, bool SPH = false>
-__global__ void __launch_bounds__(kBlock, SHAPE == kShapeCoop ? kCoopMinBlocks : kTravMinBlocks)
+// BLK: threads per block of a traversal kernel (mgpu_tune_set "trav_block"); the resident
+// blocks per SM scale with it, so every block size gets the same register budget per thread
+template <bool COUNT, int SHAPE, bool SPH = false, int BLK = kBlock>
+__global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopMinBlocks : kTravMinBlocks) * kBlock / BLK)
     k_extend(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
@@ -330,7 +332,7 @@ __global__ void __launch_bounds__(kBlock, SHAPE == kShapeCoop ? kCoopMinBlocks :
   if (SHAPE == kShapePersist) {
     persistent_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
   } else if (SHAPE == kShapeCoop) {
-    __shared__ unsigned long long wkey[kBlock];
+    __shared__ unsigned long long wkey[BLK];
     grid_trace_coop<false, COUNT, SPH>(view_of, n, load, store, &c, rays, wkey + (threadIdx.x & ~31u));
   } else {
     grid_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
@@ -547,8 +549,8 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
 }
 
 // shadow: any-hit query per queued light sample; an occluded sample's slot is zeroed
-template <bool COUNT, int SHAPE, bool SPH = false>
-__global__ void __launch_bounds__(kBlock, SHAPE == kShapeCoop ? kCoopMinBlocks : kTravMinBlocks)
+template <bool COUNT, int SHAPE, bool SPH = false, int BLK = kBlock>
+__global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopMinBlocks : kTravMinBlocks) * kBlock / BLK)
     k_shadow(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrNee + b];
   const float4 *so = a.so, *sd = a.sd;
@@ -771,6 +773,9 @@ struct Tuning {
   // grid-stride traversal with the leaf triangles shared by the warp: bit 0 for the shadow
   // (any-hit) kernel, bit 1 for the extension (closest-hit) kernel
   std::atomic<int> coop_leaf{1};
+  // threads per block of the grid-stride and warp-shared traversal kernels: 64, 128 or 256 (mid
+  // frame: 256 is 0.6 % faster than 128, 64 equal to 128)
+  std::atomic<int> trav_block{256};
   std::atomic<int> bin_shadow{1};     // counting-sort shadow rays by (light, origin cell)
   std::atomic<int> bin_extension{1};  // counting-sort extension rays by (octant, origin cell)
   // waves of fewer paths skip binning: sorting a few hundred thousand rays costs more (four
@@ -937,9 +942,9 @@ static int64_t noalloc_paths(int64_t nl_slots) {
   return p / 64 * 64;
 }
 
-static int grid_for(const void *kern, size_t smem) {
+static int grid_for(const void *kern, size_t smem, int block = kBlock) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
   if (per_sm < 1) per_sm = 1;
   return device_sm_count() * per_sm;
 }
@@ -1191,18 +1196,26 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
   const bool coop_sh = (g_tune.coop_leaf.load() & 1) != 0, coop_ext = (g_tune.coop_leaf.load() & 2) != 0;
   bool sph = false;  // a job's scene has analytic spheres: the traversal kernels that test them
   for (const Job &j : jobs) sph = sph || j.scene->view.nsphere > 0;
+  // threads per traversal block: 128 for the persistent, sphere and counted kernels; the
+  // grid-stride and warp-shared shapes of the plain render also come in 64 and 256
+  const int tb = (sph || persist || COUNT) ? kBlock : g_tune.trav_block.load();
   auto kext = sph        ? k_extend<COUNT, kShapeGrid, true>
               : persist  ? k_extend<COUNT, kShapePersist>
-              : coop_ext ? k_extend<COUNT, kShapeCoop>
-                         : k_extend<COUNT, kShapeGrid>;
+              : coop_ext ? (tb == 64 ? k_extend<COUNT, kShapeCoop, false, 64>
+                            : tb == 256 ? k_extend<COUNT, kShapeCoop, false, 256> : k_extend<COUNT, kShapeCoop>)
+                         : (tb == 64 ? k_extend<COUNT, kShapeGrid, false, 64>
+                            : tb == 256 ? k_extend<COUNT, kShapeGrid, false, 256> : k_extend<COUNT, kShapeGrid>);
   auto kshw = sph        ? k_shadow<COUNT, kShapeGrid, true>
               : persist  ? k_shadow<COUNT, kShapePersist>
-              : coop_sh  ? k_shadow<COUNT, kShapeCoop>
-                         : k_shadow<COUNT, kShapeGrid>;
+              : coop_sh  ? (tb == 64 ? k_shadow<COUNT, kShapeCoop, false, 64>
+                            : tb == 256 ? k_shadow<COUNT, kShapeCoop, false, 256> : k_shadow<COUNT, kShapeCoop>)
+                         : (tb == 64 ? k_shadow<COUNT, kShapeGrid, false, 64>
+                            : tb == 256 ? k_shadow<COUNT, kShapeGrid, false, 256> : k_shadow<COUNT, kShapeGrid>);
+  const int tb_ext = (sph || persist || COUNT) ? kBlock : tb, tb_sh = tb_ext;
   const int g_gen = grid_for((const void *)k_generate, 0);
-  const int g_ext = grid_for((const void *)kext, 0);
+  const int g_ext = grid_for((const void *)kext, 0, tb_ext);
   const int g_sha = grid_for((const void *)k_shade<true>, 0);
-  const int g_shw = grid_for((const void *)kshw, 0);
+  const int g_shw = grid_for((const void *)kshw, 0, tb_sh);
   const int g_acc = grid_for((const void *)k_accumulate, 0);
   const int g_bin = device_sm_count() * 4;
   {
@@ -1283,7 +1296,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
       int chunk = wv.unlimited ? std::min(4, max_b - b) : max_b;
       for (int k = 0; k < chunk; ++k, ++b) {
         m = pf.begin(kProfExtend, st);
-        kext<<<g_ext, kBlock, 0, st>>>(a, b);
+        kext<<<g_ext, tb_ext, 0, st>>>(a, b);
         pf.end(m, st);
         m = pf.begin(kProfShade, st);
         if (surf) k_shade<true><<<g_sha, kBlock, 0, st>>>(a, b);
@@ -1311,7 +1324,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
           pf.end(m, st);
         }
         m = pf.begin(kProfShadow, st);
-        kshw<<<g_shw, kBlock, 0, st>>>(a, b);
+        kshw<<<g_shw, tb_sh, 0, st>>>(a, b);
         pf.end(m, st);
         launches += 3;
       }
@@ -1498,6 +1511,7 @@ int mgpu_tune_set(const char *key, int64_t value) {
   std::string k(key);
   if (k == "persistent") g_tune.persistent.store(value != 0);
   else if (k == "coop_leaf" && value >= 0 && value <= 3) g_tune.coop_leaf.store((int)value);
+  else if (k == "trav_block" && (value == 64 || value == 128 || value == 256)) g_tune.trav_block.store((int)value);
   else if (k == "bin_shadow") g_tune.bin_shadow.store(value != 0);
   else if (k == "bin_extension") g_tune.bin_extension.store(value != 0);
   else if (k == "bin_min_paths" && value >= 0) g_tune.bin_min_paths.store(value);
@@ -1509,6 +1523,14 @@ int mgpu_tune_set(const char *key, int64_t value) {
                            (const void *)k_shadow<false, kShapeGrid>, (const void *)k_shadow<false, kShapePersist>,
                            (const void *)k_shadow<false, kShapeCoop>,  (const void *)k_shadow<true, kShapeGrid>,
                            (const void *)k_shadow<true, kShapePersist>, (const void *)k_shadow<true, kShapeCoop>,
+                           (const void *)k_extend<false, kShapeGrid, false, 64>,
+                           (const void *)k_extend<false, kShapeGrid, false, 256>,
+                           (const void *)k_extend<false, kShapeCoop, false, 64>,
+                           (const void *)k_extend<false, kShapeCoop, false, 256>,
+                           (const void *)k_shadow<false, kShapeGrid, false, 64>,
+                           (const void *)k_shadow<false, kShapeGrid, false, 256>,
+                           (const void *)k_shadow<false, kShapeCoop, false, 64>,
+                           (const void *)k_shadow<false, kShapeCoop, false, 256>,
                            (const void *)k_shade<false>, (const void *)k_shade<true>};
     for (const void *kf : kerns)
       MGPU_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)value));
@@ -1522,6 +1544,7 @@ int mgpu_tune_get(const char *key, int64_t *value) {
   std::string k(key);
   if (k == "persistent") *value = g_tune.persistent.load();
   else if (k == "coop_leaf") *value = g_tune.coop_leaf.load();
+  else if (k == "trav_block") *value = g_tune.trav_block.load();
   else if (k == "bin_shadow") *value = g_tune.bin_shadow.load();
   else if (k == "bin_extension") *value = g_tune.bin_extension.load();
   else if (k == "bin_min_paths") *value = g_tune.bin_min_paths.load();

@@ -431,6 +431,7 @@ static void build_rec(orc_build_ctx *c, orc_node *nd, int32_t *prims, int n, int
 static void free_node(orc_node *nd) {
   if (!nd) return;
   if (nd->leaf) { free(nd->prims); return; }
+  if (!nd->child) return;  /* a node of a partly read serialisation */
   free_node(&nd->child[0]);
   free_node(&nd->child[1]);
   free(nd->child);
@@ -476,6 +477,67 @@ orc_tree *orc_kd_build(const float *v, int64_t ntri, unsigned min_prims, unsigne
   for (int64_t i = 0; i < ntri; ++i) prims[i] = (int32_t)i;
   build_helper(&c, tr->root, prims, (int)ntri, 3, 0);
   free(c.planes);
+  return tr;
+}
+
+/* A tree from its depth-first serialisation (the layout of orc_kd_serialize, which the product's
+ * mgpu_accel_serialize also writes): for scenes too large for the restated build above, the
+ * oracle traverses the product builder's tree, which is node-for-node the one that build gives
+ * wherever both are run (tests/test_kdtree.py).  The root box is computed as orc_kd_build does.
+ * Returns NULL on a malformed serialisation. */
+void orc_kd_free(orc_tree *tr);
+static int from_ser_rec(orc_node *nd, const int32_t *kind, const float *split, const int32_t *count,
+                        const int32_t *prims, int64_t n_nodes, int64_t n_prims, int64_t *ni, int64_t *np) {
+  if (*ni >= n_nodes) return 0;
+  int64_t i = (*ni)++;
+  if (kind[i] == 3) {
+    nd->leaf = 1;
+    nd->nprims = count[i];
+    if (count[i] < 0 || *np + count[i] > n_prims) return 0;
+    nd->prims = (int32_t *)malloc(sizeof(int32_t) * (count[i] > 0 ? count[i] : 1));
+    memcpy(nd->prims, prims + *np, sizeof(int32_t) * (size_t)count[i]);
+    *np += count[i];
+    return 1;
+  }
+  if (kind[i] < 0 || kind[i] > 2) return 0;
+  nd->leaf = 0;
+  nd->axis = kind[i];
+  nd->split = split[i];
+  nd->child = (orc_node *)calloc(2, sizeof(orc_node));
+  return from_ser_rec(&nd->child[0], kind, split, count, prims, n_nodes, n_prims, ni, np) &&
+         from_ser_rec(&nd->child[1], kind, split, count, prims, n_nodes, n_prims, ni, np);
+}
+
+orc_tree *orc_kd_from_serial(const float *v, int64_t ntri, const int32_t *kind, const float *split,
+                             const int32_t *count, const int32_t *prims, int64_t n_nodes, int64_t n_prims) {
+  orc_tree *tr = (orc_tree *)calloc(1, sizeof(orc_tree));
+  tr->ntri = ntri;
+  tr->tri_box = (orc_aabb *)malloc(sizeof(orc_aabb));
+  for (int k = 0; k < 3; ++k) { tr->box.mn[k] = ORC_INF; tr->box.mx[k] = -ORC_INF; }
+  for (int64_t t = 0; t < ntri; ++t) {
+    orc_aabb b;
+    for (int k = 0; k < 3; ++k) { b.mn[k] = ORC_INF; b.mx[k] = -ORC_INF; }
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k) {
+        double x = v[t * 9 + j * 3 + k];
+        if (x < b.mn[k]) b.mn[k] = x;
+        if (x > b.mx[k]) b.mx[k] = x;
+      }
+    if (!box_is_point(&b)) {
+      int same = orc_eq(b.mn[0], b.mx[0]) && orc_eq(b.mn[1], b.mx[1]) && orc_eq(b.mn[2], b.mx[2]);
+      if (!same)
+        for (int k = 0; k < 3; ++k) {
+          if (b.mn[k] < tr->box.mn[k]) tr->box.mn[k] = b.mn[k];
+          if (b.mx[k] > tr->box.mx[k]) tr->box.mx[k] = b.mx[k];
+        }
+    }
+  }
+  tr->root = (orc_node *)calloc(1, sizeof(orc_node));
+  int64_t ni = 0, np = 0;
+  if (!from_ser_rec(tr->root, kind, split, count, prims, n_nodes, n_prims, &ni, &np) || ni != n_nodes) {
+    orc_kd_free(tr);
+    return NULL;
+  }
   return tr;
 }
 

@@ -26,6 +26,8 @@ def load() -> C.CDLL:
     lib.orc_kd_build.restype = vp
     lib.orc_kd_build.argtypes = [vp, i64, C.c_uint, C.c_uint, C.c_double, C.c_double]
     lib.orc_kd_free.argtypes = [vp]
+    lib.orc_kd_from_serial.restype = vp
+    lib.orc_kd_from_serial.argtypes = [vp, i64, vp, vp, vp, vp, i64, i64]
     lib.orc_kd_stats.argtypes = [vp, vp]
     lib.orc_kd_bounds.argtypes = [vp, vp]
     lib.orc_kd_serialize.restype = i64
@@ -62,6 +64,22 @@ class Tree:
         self.v = np.ascontiguousarray(tri_v, np.float32).reshape(-1, 9)
         self.ntri = self.v.shape[0]
         self.h = self._lib.orc_kd_build(_p(self.v), self.ntri, min_prims, max_depth, cost_traversal, empty_bias)
+
+    @classmethod
+    def from_serial(cls, tri_v: np.ndarray, kind, split, count, prims) -> "Tree":
+        """The tree given by a depth-first serialisation (orc_kd_serialize's layout, which the
+        product's Accel.serialize also gives): for scenes whose restated build takes too long."""
+        self = cls.__new__(cls)
+        self._lib = load()
+        self.v = np.ascontiguousarray(tri_v, np.float32).reshape(-1, 9)
+        self.ntri = self.v.shape[0]
+        self._ser = [np.ascontiguousarray(kind, np.int32), np.ascontiguousarray(split, np.float32),
+                     np.ascontiguousarray(count, np.int32), np.ascontiguousarray(prims, np.int32)]
+        k, sp, c, pr = self._ser
+        self.h = self._lib.orc_kd_from_serial(_p(self.v), self.ntri, _p(k), _p(sp), _p(c), _p(pr), len(k), len(pr))
+        if not self.h:
+            raise ValueError("malformed tree serialisation")
+        return self
 
     def stats(self) -> dict:
         out = np.zeros(8, np.uint64)

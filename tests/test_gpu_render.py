@@ -104,7 +104,8 @@ def test_tuning_knobs_do_not_change_the_image(cuda):
     ds = pt.DeviceScene(s, acc)
     st = pt.RenderSettings(48, 40, 8, max_depth=6, rr_start_depth=3, seed=4)
     raws = []
-    saved = {k: pt.tune_get(k) for k in ("persistent", "coop_leaf", "bin_shadow", "bin_extension", "bin_min_paths")}
+    saved = {k: pt.tune_get(k) for k in ("persistent", "coop_leaf", "bin_shadow", "bin_extension", "bin_min_paths",
+                                         "trav_block")}
     pt.tune("bin_min_paths", 0)  # bin even this small wave
     try:
         for shape in ("grid", "persistent", "coop_shadow", "coop_both"):
@@ -113,6 +114,14 @@ def test_tuning_knobs_do_not_change_the_image(cuda):
                 pt.tune("coop_leaf", {"grid": 0, "persistent": 0, "coop_shadow": 1, "coop_both": 3}[shape])
                 pt.tune("bin_shadow", bins[0])
                 pt.tune("bin_extension", bins[1])
+                f = pt.Film(48, 40)
+                pt.render(ds, st, f)
+                raws.append(f.raw())
+        for blk in (64, 256):  # threads per traversal block
+            pt.tune("persistent", 0)
+            pt.tune("trav_block", blk)
+            for coop in (0, 1, 3):
+                pt.tune("coop_leaf", coop)
                 f = pt.Film(48, 40)
                 pt.render(ds, st, f)
                 raws.append(f.raw())

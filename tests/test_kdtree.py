@@ -88,3 +88,25 @@ def test_identical_to_oracle_on_a_large_soup(oracle):
     # 300,000 triangles: the root's axes are evaluated on parallel threads and its event lists
     # are radix sorted (the small cases above take std::sort); the tree must not change
     _same(oracle, _soup(7, 300_000), KdSettings(threads=4))
+
+
+def test_oracle_adopts_a_serialised_tree(oracle):
+    """For scenes too large for the restated build (the 20 M-triangle large configuration) the
+    oracle traverses the product's tree read from its serialisation; on a scene where both run,
+    that tree serialises back identically and answers every ray as the oracle's own build does."""
+    import raygen
+    s = scenegen.random_scene(5, 30000)
+    own = oracle.Tree(s.tri_v)
+    acc = Accel(s)
+    adopted = oracle.Tree.from_serial(s.tri_v, *acc.serialize())
+    for a, b in zip(own.serialize(), adopted.serialize()):
+        assert np.array_equal(a, b)
+    assert np.array_equal(own.bounds(), adopted.bounds())
+    lo, hi = s.tri_v.reshape(-1, 3).min(0), s.tri_v.reshape(-1, 3).max(0)
+    rays = np.concatenate([raygen.camera_rays(s.camera, 4096, 3), raygen.sphere_rays(lo, hi, 4096, 4)])
+    t1, p1, _, _ = oracle.trace_closest(own, s.tri_v, s.tri_flags, rays)
+    t2, p2, _, _ = oracle.trace_closest(adopted, s.tri_v, s.tri_flags, rays)
+    assert np.array_equal(p1, p2) and np.array_equal(t1, t2)
+    with pytest.raises(ValueError):
+        k, sp, c, pr = acc.serialize()
+        oracle.Tree.from_serial(s.tri_v, k[:-3], sp[:-3], c[:-3], pr)
