@@ -367,6 +367,13 @@ int mgpu_profile_read(double *ms6, uint64_t *launches6);
 int mgpu_tune_set(const char *key, int64_t value);
 int mgpu_tune_get(const char *key, int64_t *value);
 
+/* Read bandwidth of this device (measurement only, no counterpart in the reference): one
+ * launch reads a `bytes` buffer (cudaMalloc'd here; >= 4096, a multiple of 16) `reps` times
+ * through L2-only loads; *gbs = bytes * reps / time.  A buffer that fits the L2 measures the L2's
+ * read bandwidth (the denominator of the traversal kernels' L2 roofline), a larger one the HBM's.
+ * Synchronises. */
+int mgpu_measure_read_bandwidth(uint64_t bytes, int32_t reps, double *gbs, void *stream);
+
 /* Kernel launches issued by this library since load (for launch accounting). */
 uint64_t mgpu_launch_count(void);
 

@@ -137,6 +137,7 @@ SIGNATURES = [
     ("mgpu_server_read", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("mgpu_server_release", C.c_int, [C.c_void_p, C.c_int64]),
     ("mgpu_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("mgpu_measure_read_bandwidth", C.c_int, [C.c_uint64, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
     ("mgpu_renderer_create", C.c_int, [C.POINTER(C.c_void_p)]),
     ("mgpu_renderer_destroy", C.c_int, [C.c_void_p]),
     ("mgpu_renderer_set_value", C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),

@@ -406,6 +406,14 @@ class Batch:
             pass
 
 
+def measure_read_bandwidth(nbytes: int, reps: int, stream=None) -> float:
+    """GB/s of reading a device buffer of nbytes reps times in one launch (L2-only loads):
+    an L2-resident buffer measures the L2's read bandwidth, a larger one the HBM's."""
+    out = C.c_double()
+    N.check(N.load().mgpu_measure_read_bandwidth(int(nbytes), int(reps), C.byref(out), _stream_handle(stream)))
+    return out.value
+
+
 def render_stats() -> dict:
     s = N.RenderStats()
     N.check(N.load().mgpu_render_stats_get(C.byref(s)))

@@ -358,3 +358,11 @@ def test_large_frame_and_many_passes(cuda, oracle):
                                        per_path=True)
     assert _path_agreement(paths_g, paths_o) >= 0.98
     assert np.allclose(mean_g, mean_o, rtol=3e-2, atol=5e-3)  # a diverged path moves a mean by at most its share
+
+
+def test_read_bandwidth_probe(cuda):
+    # the roofline denominators: an L2-resident buffer reads faster than one 16x the L2
+    l2 = pt.measure_read_bandwidth(32 << 20, 50)
+    hbm = pt.measure_read_bandwidth(2 << 30, 3)
+    print(f"read bandwidth: L2-resident {l2:.0f} GB/s, HBM {hbm:.0f} GB/s")
+    assert hbm > 1000 and l2 > hbm
