@@ -511,18 +511,24 @@ __device__ __forceinline__ void persistent_trace(View view, const Pair *top, uin
 // gives: the winner is the smallest t below the ray's best, ties to the first triangle in the
 // leaf's order, and its owner re-runs that one test for t and barycentrics.
 // All 32 lanes of every warp must call this (rays are taken in warp-aligned rounds).
+// With wray / wk (per-warp shared memory: 64 float4, 32 words) each lane's ray constants for the
+// tests are written there once per ray and read by the testers, instead of living in registers
+// through the descent and travelling by shuffles.
 template <bool ANY, bool COUNT, bool SPH, class View, class Load, class Store>
 __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load, Store store, TraceCounts *cnt,
-                                                uint32_t &rays_done, unsigned long long *wkey) {
+                                                uint32_t &rays_done, unsigned long long *wkey, float4 *wray = nullptr,
+                                                uint32_t *wk = nullptr) {
   const unsigned kFull = 0xFFFFFFFFu;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t stride = gridDim.x * blockDim.x;
   TravState st{};
   TravEntry stack[kMaxStack];
+  const bool smray = wray != nullptr;
   for (uint32_t r0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < n; r0 += stride) {
     const uint32_t i = r0 + lane;
     bool active = false;
     const SceneView *sv = nullptr;
+    if (smray) __syncwarp(kFull);  // the previous round's readers are done with wray
     if (i < n) {
       sv = &view(i);
       Ray r;
@@ -530,6 +536,11 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
       ++rays_done;
       active = trav_init<SPH>(*sv, r, nullptr, 0, st, ANY);
       if (!active) store(i, st.best_prim >= 0, st);
+      if (active && smray) {
+        wray[lane] = make_float4(st.pre.o.x, st.pre.o.y, st.pre.o.z, st.ray_tmin);
+        wray[32 + lane] = make_float4(st.pre.sx, st.pre.sy, st.pre.sz, st.best);
+        wk[lane] = (uint32_t)st.pre.kx | ((uint32_t)st.pre.ky << 2) | ((uint32_t)st.pre.kz << 4);
+      }
     }
     while (__any_sync(kFull, active)) {
       uint32_t lw0 = kLeafTag, lw1 = 0;
@@ -545,9 +556,10 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
       const uint32_t total = __shfl_sync(kFull, incl, 31);
       const uint32_t excl = incl - count;
       // the owner's ray, as the tests need it
-      const uint32_t kpack = (uint32_t)st.pre.kx | ((uint32_t)st.pre.ky << 2) | ((uint32_t)st.pre.kz << 4);
+      const uint32_t kpack = smray ? 0u : ((uint32_t)st.pre.kx | ((uint32_t)st.pre.ky << 2) | ((uint32_t)st.pre.kz << 4));
       const unsigned long long ltp = active ? (unsigned long long)sv->ltris : 0ull;
       if (!ANY) wkey[lane] = ~0ull;
+      if (!ANY && smray && active) wray[32 + lane].w = st.best;
       __syncwarp(kFull);
       uint32_t hit_owners = 0u;
       for (uint32_t base = 0; base < total; base += 32) {
@@ -559,16 +571,25 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
           if (v <= k) o += step;
         }
         RayPre p;
-        p.o.x = __shfl_sync(kFull, st.pre.o.x, o);
-        p.o.y = __shfl_sync(kFull, st.pre.o.y, o);
-        p.o.z = __shfl_sync(kFull, st.pre.o.z, o);
-        p.sx = __shfl_sync(kFull, st.pre.sx, o);
-        p.sy = __shfl_sync(kFull, st.pre.sy, o);
-        p.sz = __shfl_sync(kFull, st.pre.sz, o);
-        const uint32_t kp = __shfl_sync(kFull, kpack, o);
+        uint32_t kp;
+        float tmin_o, best_o;
+        if (smray) {
+          const float4 ra = wray[o], rb = wray[32 + o];
+          p.o.x = ra.x; p.o.y = ra.y; p.o.z = ra.z; tmin_o = ra.w;
+          p.sx = rb.x; p.sy = rb.y; p.sz = rb.z; best_o = rb.w;
+          kp = wk[o];
+        } else {
+          p.o.x = __shfl_sync(kFull, st.pre.o.x, o);
+          p.o.y = __shfl_sync(kFull, st.pre.o.y, o);
+          p.o.z = __shfl_sync(kFull, st.pre.o.z, o);
+          p.sx = __shfl_sync(kFull, st.pre.sx, o);
+          p.sy = __shfl_sync(kFull, st.pre.sy, o);
+          p.sz = __shfl_sync(kFull, st.pre.sz, o);
+          kp = __shfl_sync(kFull, kpack, o);
+          tmin_o = __shfl_sync(kFull, st.ray_tmin, o);
+          best_o = __shfl_sync(kFull, st.best, o);
+        }
         p.kx = (int)(kp & 3u); p.ky = (int)((kp >> 2) & 3u); p.kz = (int)((kp >> 4) & 3u);
-        const float tmin_o = __shfl_sync(kFull, st.ray_tmin, o);
-        const float best_o = __shfl_sync(kFull, st.best, o);
         const uint32_t first_o = __shfl_sync(kFull, lw1, o);
         const uint32_t excl_o = __shfl_sync(kFull, excl, o);
         const F4 *lt = reinterpret_cast<const F4 *>(__shfl_sync(kFull, ltp, o));

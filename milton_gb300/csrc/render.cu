@@ -332,8 +332,12 @@ __global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopMinBlocks : k
   if (SHAPE == kShapePersist) {
     persistent_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, &a.counters[kCtrFetchExt + b], load, store, &c, rays);
   } else if (SHAPE == kShapeCoop) {
+    // per warp: the closest-hit keys of the shared leaf tests and the lanes' ray constants
     __shared__ unsigned long long wkey[BLK];
-    grid_trace_coop<false, COUNT, SPH>(view_of, n, load, store, &c, rays, wkey + (threadIdx.x & ~31u));
+    __shared__ float4 wray[2 * BLK];
+    __shared__ uint32_t wk[BLK];
+    grid_trace_coop<false, COUNT, SPH>(view_of, n, load, store, &c, rays, wkey + (threadIdx.x & ~31u),
+                                       wray + 2 * (threadIdx.x & ~31u), wk + (threadIdx.x & ~31u));
   } else {
     grid_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
   }
@@ -577,7 +581,11 @@ __global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopMinBlocks : k
   if (SHAPE == kShapePersist) {
     persistent_trace<true, COUNT, SPH>(view_of, nullptr, 0, n, &a.counters[kCtrFetchSh + b], load, store, &c, rays);
   } else if (SHAPE == kShapeCoop) {
-    grid_trace_coop<true, COUNT, SPH>(view_of, n, load, store, &c, rays, nullptr);
+    // per warp: the lanes' ray constants for the shared leaf tests
+    __shared__ float4 wray[2 * BLK];
+    __shared__ uint32_t wk[BLK];
+    grid_trace_coop<true, COUNT, SPH>(view_of, n, load, store, &c, rays, nullptr, wray + 2 * (threadIdx.x & ~31u),
+                                      wk + (threadIdx.x & ~31u));
   } else {
     grid_trace<true, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
   }
