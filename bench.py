@@ -818,6 +818,9 @@ def run_profile_case(args):
 
     from milton_gb300 import pathtracer as pt
     from milton_gb300 import scenegen
+    for kv in args.tune:  # knobs of the captured kernels, e.g. --tune smem_stack=4
+        k, v = kv.split("=")
+        pt.tune(k, int(v))
     s = scenegen.mid(SEED)
     ds = pt.DeviceScene(s, pt.Accel(s))
     film = pt.Film(512, 512)
@@ -840,6 +843,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="batched / serving / large: skip the FP64 parity check")
     ap.add_argument("--profile-case", action="store_true", help="small two-frame case for ncu captures")
+    ap.add_argument("--tune", action="append", default=[], metavar="KEY=VALUE",
+                    help="profile case: a tuning knob (mgpu_tune_set) to set first; repeatable")
     ap.add_argument("--workload", default="mid", choices=["mid", "plain", "batched", "serving", "large"],
                     help="mid (default, the benchmark line), plain (the CPU-runnable frame), batched (64 scenes, "
                          "batch vs one-by-one) or serving (Poisson request stream through the render service)")

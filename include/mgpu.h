@@ -362,8 +362,11 @@ int mgpu_profile_read(double *ms6, uint64_t *launches6);
  *   "bin_shadow"     0/1  counting-sort shadow rays by (light, origin cell) (default 1)
  *   "bin_extension"  0/1  counting-sort extension rays by (direction octant, origin cell) (default 1)
  *   "bin_min_paths"  n    waves of fewer paths are not binned (default 2^22)
- *   "carveout"       -1..100  shared-memory carveout (percent) preferred for the traversal and
- *                    shade kernels; -1 = the driver's choice (default)                        */
+ *   "carveout"       -2..100  shared-memory carveout (percent) preferred for the traversal and
+ *                    shade kernels: -2 = per kernel, the least shared memory that keeps all its
+ *                    register-limited resident blocks, the rest of the SM's memory as L1
+ *                    (default); -1 = the driver's choice; applied on each device before its next
+ *                    render                                                                     */
 int mgpu_tune_set(const char *key, int64_t value);
 int mgpu_tune_get(const char *key, int64_t *value);
 

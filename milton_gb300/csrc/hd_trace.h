@@ -224,6 +224,15 @@ struct TravEntry {
   float tmax;
 };
 
+// The far-cell stack (the thread's local memory).  sp is the entry's index: push writes entry sp,
+// pop reads entry sp (the caller has decremented it).
+MGPU_HD void stk_push(TravEntry *e, int sp, uint32_t w0, uint32_t w1, float tmax) {
+  e[sp].w0 = w0; e[sp].w1 = w1; e[sp].tmax = tmax;
+}
+MGPU_HD void stk_pop(TravEntry *e, int sp, uint32_t &w0, uint32_t &w1, float &tmax) {
+  w0 = e[sp].w0; w1 = e[sp].w1; tmax = e[sp].tmax;
+}
+
 struct TravState {
   RayPre pre;
   V3 inv;
@@ -330,8 +339,8 @@ MGPU_HD bool trav_init(const SceneView &s, const Ray &r, const Pair *top, uint32
 
 // Descends from the current node to the next leaf: returns the leaf slot (w0: count << 2 | 3,
 // w1: first leaf record) and the exit t of its cell in tmax_out; far children go on the stack.
-template <bool COUNT>
-MGPU_HD void trav_descend(const SceneView &s, TravState &st, TravEntry *stack, const Pair *top, uint32_t ntop,
+template <bool COUNT, class Stk>
+MGPU_HD void trav_descend(const SceneView &s, TravState &st, Stk stack, const Pair *top, uint32_t ntop,
                           TraceCounts *cnt, uint32_t &leaf_w0, uint32_t &leaf_w1, float &tmax_out) {
   const float o[3] = {st.pre.o.x, st.pre.o.y, st.pre.o.z};
   const float iv[3] = {st.inv.x, st.inv.y, st.inv.z};
@@ -362,7 +371,7 @@ MGPU_HD void trav_descend(const SceneView &s, TravState &st, TravEntry *stack, c
       if (st.sp < kMaxStack) {
         uint32_t f0 = (n0 == pr.a0 && n1 == pr.a1) ? pr.b0 : pr.a0;
         uint32_t f1 = (n0 == pr.a0 && n1 == pr.a1) ? pr.b1 : pr.a1;
-        stack[st.sp].w0 = f0; stack[st.sp].w1 = f1; stack[st.sp].tmax = tmax;
+        stk_push(stack, st.sp, f0, f1, tmax);
         ++st.sp;
         if (COUNT && (uint32_t)st.sp > cnt->max_stack) cnt->max_stack = (uint32_t)st.sp;
       }
@@ -377,21 +386,21 @@ MGPU_HD void trav_descend(const SceneView &s, TravState &st, TravEntry *stack, c
 }
 
 // After a leaf has been tested: finish (true) or move to the next cell on the stack (false).
-template <bool ANY>
-MGPU_HD bool trav_after_leaf(TravState &st, const TravEntry *stack, float tmax) {
+template <bool ANY, class Stk>
+MGPU_HD bool trav_after_leaf(TravState &st, Stk stack, float tmax) {
   // early exit: the best hit lies inside this cell, later cells are farther
   if (!ANY && st.best_prim >= 0 && st.best <= tmax + kCellEps * fabsf(tmax)) return true;
   if (st.sp == 0 || ++st.steps >= kMaxLeafSteps) return true;
   --st.sp;
   st.tmin = tmax;
-  st.w0 = stack[st.sp].w0; st.w1 = stack[st.sp].w1; st.tmax = stack[st.sp].tmax;
+  stk_pop(stack, st.sp, st.w0, st.w1, st.tmax);
   if (!ANY && st.best_prim >= 0 && st.best < st.tmin) return true;
   return false;
 }
 
 // One leaf: descend, test, then finish (true) or move to the next cell (false).
-template <bool ANY, bool COUNT>
-MGPU_HD bool trav_step(const SceneView &s, TravState &st, TravEntry *stack, const Pair *top, uint32_t ntop,
+template <bool ANY, bool COUNT, class Stk>
+MGPU_HD bool trav_step(const SceneView &s, TravState &st, Stk stack, const Pair *top, uint32_t ntop,
                        TraceCounts *cnt) {
   uint32_t w0, w1;
   float tmax;

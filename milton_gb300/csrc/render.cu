@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <climits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -775,6 +776,8 @@ struct Workspace {
   }
 };
 
+constexpr int kCarveoutAuto = -2;
+
 // process-wide tuning knobs (mgpu_tune_set)
 struct Tuning {
   std::atomic<int> persistent{0};     // persistent warp-level traversal with ray refill
@@ -789,7 +792,9 @@ struct Tuning {
   // waves of fewer paths skip binning: sorting a few hundred thousand rays costs more (four
   // latency-bound launches per bounce) than the coherence it buys
   std::atomic<int64_t> bin_min_paths{(int64_t)1 << 22};
-  std::atomic<int> carveout{-1};      // shared-memory carveout (%) of the traversal / shade kernels; -1 = driver's
+  // shared-memory carveout (%) of the traversal / shade kernels: -2 = per kernel, the least that
+  // keeps its resident blocks (the rest of the SM's 256 KB is L1); -1 = the driver's choice
+  std::atomic<int> carveout{kCarveoutAuto};
 };
 static Tuning g_tune;
 
@@ -948,6 +953,83 @@ static int64_t noalloc_paths(int64_t nl_slots) {
   if (kNoAllocBytes <= fixed) return 0;
   int64_t p = (int64_t)((kNoAllocBytes - fixed) / per);
   return p / 64 * 64;
+}
+
+// Function attributes belong to a device's context: they are set on the current device before
+// its first render and again after the carveout knob changes.
+//   the sorting blocks: kBins counters of dynamic shared memory, above the 48 KB default;
+//   the traversal and shade kernels: the L1 / shared-memory split ("carveout").  These kernels
+//   chase pointers through L1 and their block needs little shared memory (none, or the shared
+//   leaf tests' per-warp records); the driver's own choice for the shared-leaf shadow kernel is a
+//   132 KB shared-memory configuration where 64 KB keeps all its blocks resident, and the L1 it
+//   gives up makes that kernel 4 % slower on the mid frame.  The automatic carveout asks for the
+//   least shared memory that keeps the kernel's register-limited number of resident blocks.
+struct CarveoutKernel {
+  const void *f;
+  int block;
+};
+
+static std::vector<CarveoutKernel> carveout_kernels() {
+  return {{(const void *)k_extend<false, kShapeGrid>, kBlock},      {(const void *)k_extend<false, kShapePersist>, kBlock},
+          {(const void *)k_extend<false, kShapeCoop>, kBlock},      {(const void *)k_extend<true, kShapeGrid>, kBlock},
+          {(const void *)k_extend<true, kShapePersist>, kBlock},    {(const void *)k_extend<true, kShapeCoop>, kBlock},
+          {(const void *)k_extend<false, kShapeGrid, true>, kBlock}, {(const void *)k_extend<true, kShapeGrid, true>, kBlock},
+          {(const void *)k_shadow<false, kShapeGrid>, kBlock},      {(const void *)k_shadow<false, kShapePersist>, kBlock},
+          {(const void *)k_shadow<false, kShapeCoop>, kBlock},      {(const void *)k_shadow<true, kShapeGrid>, kBlock},
+          {(const void *)k_shadow<true, kShapePersist>, kBlock},    {(const void *)k_shadow<true, kShapeCoop>, kBlock},
+          {(const void *)k_shadow<false, kShapeGrid, true>, kBlock}, {(const void *)k_shadow<true, kShapeGrid, true>, kBlock},
+          {(const void *)k_extend<false, kShapeGrid, false, 64>, 64},
+          {(const void *)k_extend<false, kShapeGrid, false, 256>, 256},
+          {(const void *)k_extend<false, kShapeCoop, false, 64>, 64},
+          {(const void *)k_extend<false, kShapeCoop, false, 256>, 256},
+          {(const void *)k_shadow<false, kShapeGrid, false, 64>, 64},
+          {(const void *)k_shadow<false, kShapeGrid, false, 256>, 256},
+          {(const void *)k_shadow<false, kShapeCoop, false, 64>, 64},
+          {(const void *)k_shadow<false, kShapeCoop, false, 256>, 256},
+          {(const void *)k_shade<false>, kBlock},                    {(const void *)k_shade<true>, kBlock}};
+}
+
+// percent of the SM's shared memory that holds the kernel's resident blocks (registers and
+// threads permitting) with their static shared memory and the per-block reservation
+static cudaError_t auto_carveout(const CarveoutKernel &k, int smem_sm, int reserved, int &pct) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, k.f);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k.f, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  int blocks = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k.f, k.block, 0);
+  if (e != cudaSuccess) return e;
+  const int64_t need = (int64_t)blocks * (int64_t)(fa.sharedSizeBytes + (size_t)reserved);
+  pct = (int)std::min<int64_t>(100, (need * 100 + smem_sm - 1) / smem_sm);
+  return cudaSuccess;
+}
+
+static cudaError_t kernel_attributes() {
+  static std::mutex mu;
+  static std::vector<int> applied;  // per device: the carveout knob last applied, INT_MIN = none
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const int want = g_tune.carveout.load();
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)applied.size() <= dev) applied.resize((size_t)dev + 1, INT_MIN);
+  if (applied[(size_t)dev] == want) return cudaSuccess;
+  if (applied[(size_t)dev] == INT_MIN) {
+    const void *bins[] = {(const void *)k_bin_hist, (const void *)k_bin_scatter<2>, (const void *)k_bin_scatter<3>};
+    for (const void *kf : bins)
+      if ((e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, kBinSmem)) != cudaSuccess) return e;
+  }
+  int smem_sm = 0, reserved = 0;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return e;
+  for (const CarveoutKernel &k : carveout_kernels()) {
+    int pct = want;
+    if (want == kCarveoutAuto && (e = auto_carveout(k, smem_sm, reserved, pct)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(k.f, cudaFuncAttributePreferredSharedMemoryCarveout, pct)) != cudaSuccess) return e;
+  }
+  applied[(size_t)dev] = want;
+  return cudaSuccess;
 }
 
 static int grid_for(const void *kern, size_t smem, int block = kBlock) {
@@ -1220,25 +1302,13 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
                          : (tb == 64 ? k_shadow<COUNT, kShapeGrid, false, 64>
                             : tb == 256 ? k_shadow<COUNT, kShapeGrid, false, 256> : k_shadow<COUNT, kShapeGrid>);
   const int tb_ext = (sph || persist || COUNT) ? kBlock : tb, tb_sh = tb_ext;
+  MGPU_CUDA(kernel_attributes());
   const int g_gen = grid_for((const void *)k_generate, 0);
   const int g_ext = grid_for((const void *)kext, 0, tb_ext);
   const int g_sha = grid_for((const void *)k_shade<true>, 0);
   const int g_shw = grid_for((const void *)kshw, 0, tb_sh);
   const int g_acc = grid_for((const void *)k_accumulate, 0);
   const int g_bin = device_sm_count() * 4;
-  {
-    // the sorting blocks hold kBins counters in shared memory, above the 48 KB default
-    static std::once_flag once;
-    static cudaError_t smem_rc = cudaSuccess;
-    std::call_once(once, [] {
-      const void *kerns[] = {(const void *)k_bin_hist, (const void *)k_bin_scatter<2>, (const void *)k_bin_scatter<3>};
-      for (const void *kf : kerns) {
-        cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, kBinSmem);
-        if (e != cudaSuccess && smem_rc == cudaSuccess) smem_rc = e;
-      }
-    });
-    MGPU_CUDA(smem_rc);
-  }
   const int bin_ext = g_tune.bin_extension.load(), bin_sh = g_tune.bin_shadow.load();
   const int64_t bin_min = g_tune.bin_min_paths.load();
 
@@ -1523,25 +1593,8 @@ int mgpu_tune_set(const char *key, int64_t value) {
   else if (k == "bin_shadow") g_tune.bin_shadow.store(value != 0);
   else if (k == "bin_extension") g_tune.bin_extension.store(value != 0);
   else if (k == "bin_min_paths" && value >= 0) g_tune.bin_min_paths.store(value);
-  else if (k == "carveout" && value >= -1 && value <= 100) {
-    // the L1 / shared-memory split of the kernels that spill and chase pointers through L1
-    const void *kerns[] = {(const void *)k_extend<false, kShapeGrid>, (const void *)k_extend<false, kShapePersist>,
-                           (const void *)k_extend<false, kShapeCoop>,  (const void *)k_extend<true, kShapeGrid>,
-                           (const void *)k_extend<true, kShapePersist>, (const void *)k_extend<true, kShapeCoop>,
-                           (const void *)k_shadow<false, kShapeGrid>, (const void *)k_shadow<false, kShapePersist>,
-                           (const void *)k_shadow<false, kShapeCoop>,  (const void *)k_shadow<true, kShapeGrid>,
-                           (const void *)k_shadow<true, kShapePersist>, (const void *)k_shadow<true, kShapeCoop>,
-                           (const void *)k_extend<false, kShapeGrid, false, 64>,
-                           (const void *)k_extend<false, kShapeGrid, false, 256>,
-                           (const void *)k_extend<false, kShapeCoop, false, 64>,
-                           (const void *)k_extend<false, kShapeCoop, false, 256>,
-                           (const void *)k_shadow<false, kShapeGrid, false, 64>,
-                           (const void *)k_shadow<false, kShapeGrid, false, 256>,
-                           (const void *)k_shadow<false, kShapeCoop, false, 64>,
-                           (const void *)k_shadow<false, kShapeCoop, false, 256>,
-                           (const void *)k_shade<false>, (const void *)k_shade<true>};
-    for (const void *kf : kerns)
-      MGPU_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, (int)value));
+  else if (k == "carveout" && value >= kCarveoutAuto && value <= 100) {
+    // applied per device before its next render (kernel_attributes)
     g_tune.carveout.store((int)value);
   } else return fail(MGPU_E_INVALID, "mgpu_tune_set: unknown key or bad value " + k);
   return MGPU_OK;

@@ -105,7 +105,8 @@ def test_tuning_knobs_do_not_change_the_image(cuda):
     st = pt.RenderSettings(48, 40, 8, max_depth=6, rr_start_depth=3, seed=4)
     raws = []
     saved = {k: pt.tune_get(k) for k in ("persistent", "coop_leaf", "bin_shadow", "bin_extension", "bin_min_paths",
-                                         "trav_block")}
+                                         "trav_block", "carveout")}
+    assert saved["carveout"] == -2  # per-kernel automatic carveout by default
     pt.tune("bin_min_paths", 0)  # bin even this small wave
     try:
         for shape in ("grid", "persistent", "coop_shadow", "coop_both"):
@@ -125,6 +126,11 @@ def test_tuning_knobs_do_not_change_the_image(cuda):
                 f = pt.Film(48, 40)
                 pt.render(ds, st, f)
                 raws.append(f.raw())
+        for cv in (-1, 0, 20, 100, -2):  # L1 / shared-memory split: the driver's, fixed, automatic
+            pt.tune("carveout", cv)
+            f = pt.Film(48, 40)
+            pt.render(ds, st, f)
+            raws.append(f.raw())
     finally:
         for k, v in saved.items():
             pt.tune(k, v)
