@@ -356,7 +356,7 @@ int mgpu_profile_read(double *ms6, uint64_t *launches6);
  *   "persistent"     0/1  persistent warp-level traversal with per-lane ray refill (default 0)
  *   "coop_leaf"      0..3 warp-shared leaf tests: the triangles of all the lanes' current leaves
  *                    are tested by the whole warp, 32 at a time; bit 0 = shadow (any-hit)
- *                    kernel, bit 1 = extension (closest-hit) kernel (default 1)
+ *                    kernel, bit 1 = extension (closest-hit) kernel (default 3: both)
  *   "trav_block"     64 / 128 / 256  threads per block of the grid-stride and warp-shared
  *                    traversal kernels, at the same threads (and registers) per SM (default 256)
  *   "bin_shadow"     0/1  counting-sort shadow rays by (light, origin cell) (default 1)

@@ -301,13 +301,20 @@ constexpr int kShapeCoop = 2;     // grid-stride, leaf triangles shared by the w
 #ifndef MGPU_COOP_MIN_BLOCKS
 #define MGPU_COOP_MIN_BLOCKS 12
 #endif
-// resident blocks per SM of the warp-cooperative traversal shape (its register budget)
+#ifndef MGPU_COOP_EXT_MIN_BLOCKS
+#define MGPU_COOP_EXT_MIN_BLOCKS 10
+#endif
+// resident 128-thread blocks per SM (their register budget) of the warp-cooperative traversal
+// shape: any hit 12 (40 registers), closest hit 10 (48 registers: its shared-memory reduction and
+// winner re-test hold more state; mid frame 90.7 ms at 10 against 95.7 at 12 and 97.7 at 14, the
+// any-hit kernel 116.0 at 10 against 113.2 at 12)
 constexpr int kCoopMinBlocks = MGPU_COOP_MIN_BLOCKS;
+constexpr int kCoopExtMinBlocks = MGPU_COOP_EXT_MIN_BLOCKS;
 
 // BLK: threads per block of a traversal kernel (mgpu_tune_set "trav_block"); the resident
 // blocks per SM scale with it, so every block size gets the same register budget per thread
 template <bool COUNT, int SHAPE, bool SPH = false, int BLK = kBlock>
-__global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopMinBlocks : kTravMinBlocks) * kBlock / BLK)
+__global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopExtMinBlocks : kTravMinBlocks) * kBlock / BLK)
     k_extend(RenderArgs a, int b) {
   const uint32_t n = a.counters[kCtrRay + b];
   const float4 *qo = a.qo[b & 1], *qd = a.qd[b & 1];
@@ -783,7 +790,7 @@ struct Tuning {
   std::atomic<int> persistent{0};     // persistent warp-level traversal with ray refill
   // grid-stride traversal with the leaf triangles shared by the warp: bit 0 for the shadow
   // (any-hit) kernel, bit 1 for the extension (closest-hit) kernel
-  std::atomic<int> coop_leaf{1};
+  std::atomic<int> coop_leaf{3};
   // threads per block of the grid-stride and warp-shared traversal kernels: 64, 128 or 256 (mid
   // frame: 256 is 0.6 % faster than 128, 64 equal to 128)
   std::atomic<int> trav_block{256};
