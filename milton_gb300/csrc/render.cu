@@ -70,6 +70,7 @@ struct JobArgs {
   int32_t bg_tex;          // background environment map (1 + texture index) or 0
   float bg_le[3];          // constant background radiance (bg_tex == 0)
   int32_t nlight, nl_slots, sh_cell_bits;
+  float cell_scale[3];     // queue-bin cells: 32 / the scene's extent per axis (0: a flat axis)
   Camera cam;
   Rng rng;
   int32_t W, H, spp, side, s2, nds, nds_side, max_depth, rr_start, efficient, tiles_x;
@@ -226,14 +227,14 @@ __device__ __forceinline__ uint32_t spread5(uint32_t v) {  // 5 bits -> every th
   return spread4(v & 15u) | ((v & 16u) << 8);
 }
 
-__device__ __forceinline__ uint32_t morton15(const SceneView &s, V3 p) {
+// The keys only order the queues (no result depends on them), so the cell is taken with a
+// multiplication by the precomputed 32 / extent rather than a division per axis.
+__device__ __forceinline__ uint32_t morton15(const JobArgs &J, V3 p) {
   uint32_t c[3];
   const float pp[3] = {p.x, p.y, p.z};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    float ext = s.bmax[k] - s.bmin[k];
-    float f = ext > 0.0f ? (pp[k] - s.bmin[k]) / ext : 0.0f;
-    int q = (int)(f * 32.0f);
+    const int q = (int)((pp[k] - J.view.bmin[k]) * J.cell_scale[k]);
     c[k] = (uint32_t)min(max(q, 0), 31);
   }
   return (spread5(c[0]) << 2) | (spread5(c[1]) << 1) | spread5(c[2]);
@@ -241,11 +242,11 @@ __device__ __forceinline__ uint32_t morton15(const SceneView &s, V3 p) {
 
 __device__ __forceinline__ uint32_t ext_key(const JobArgs &J, V3 o, V3 d) {
   uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-  return (oct << (kBinBits - 3)) | (morton15(J.view, o) >> (18 - kBinBits));
+  return (oct << (kBinBits - 3)) | (morton15(J, o) >> (18 - kBinBits));
 }
 
 __device__ __forceinline__ uint32_t sh_key(const JobArgs &J, int light, V3 o) {
-  uint32_t cell = morton15(J.view, o) >> (15 - J.sh_cell_bits);
+  uint32_t cell = morton15(J, o) >> (15 - J.sh_cell_bits);
   return (((uint32_t)light << J.sh_cell_bits) | cell) & (kBins - 1);
 }
 
@@ -487,6 +488,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
     // wave's stride), so the warp-aggregated append stays converged
     const int s2n = J.nds_side * J.nds_side;
     const float inv_nds = 1.0f / (float)J.nds;
+    F4u u = {0.0f, 0.0f, 0.0f, 0.0f};  // light samples 2m and 2m + 1 share counter block 1 + m
     for (int k = 0; k < a.nl_stride; ++k) {
       bool want = false;
       float4 so4, sd4;
@@ -495,9 +497,9 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         int sy = within / J.nds_side, sx = within - sy * J.nds_side;
         V3 c = v3(0.0f, 0.0f, 0.0f);
         Light lt = load_light(J, li);
+        if ((k & 1) == 0) u = uniforms(J.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
         // a point light takes one sample (DirectIllumination.cpp:97-99): the first stratum
         if (li != self && (lt.type != kLightPoint || within == 0)) {
-          F4u u = uniforms(J.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
           float ux = ((float)sx + ((k & 1) ? u.c : u.a)) / (float)J.nds_side;
           float uy = ((float)sy + ((k & 1) ? u.d : u.b)) / (float)J.nds_side;
           float r1 = 0.0f, r2 = 0.0f;
@@ -1141,6 +1143,10 @@ static JobArgs job_args(const Job &j) {
   int lb = 0;
   while ((1 << lb) < nlp) ++lb;
   J.sh_cell_bits = std::min(15, kBinBits - lb);  // light index in the top bits, origin cell below
+  for (int k = 0; k < 3; ++k) {
+    const float ext = J.view.bmax[k] - J.view.bmin[k];
+    J.cell_scale[k] = ext > 0.0f ? 32.0f / ext : 0.0f;
+  }
   return J;
 }
 
