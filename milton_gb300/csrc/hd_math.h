@@ -31,10 +31,19 @@ MGPU_HD V3 mul(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
 MGPU_HD float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 MGPU_HD V3 cross(V3 a, V3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 MGPU_HD float length(V3 a) { return sqrtf(dot(a, a)); }
+// 1 / x rounded to nearest, as the division 1.0f / x gives it (the device intrinsic skips the
+// general division's path)
+MGPU_HD float rcp(float x) {
+#if defined(__CUDA_ARCH__)
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
 MGPU_HD V3 normalize(V3 a) {
   float l2 = dot(a, a);
   if (!(l2 > 0.0f)) return a;
-  float inv = 1.0f / sqrtf(l2);
+  float inv = rcp(sqrtf(l2));
   return a * inv;
 }
 MGPU_HD float comp(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }

@@ -150,7 +150,7 @@ MGPU_HD void light_point(const Light &L, float u, float v, float r1, float r2, V
     float s = r1 + v + r2;
     float b0 = 1.0f / 3.0f, b1 = 1.0f / 3.0f, b2 = 1.0f / 3.0f;
     if (s > 0.0f) {
-      const float is = 1.0f / s;
+      const float is = rcp(s);
       b0 = r1 * is; b1 = v * is; b2 = r2 * is;
     }
     const V3 a = vert(t, 0), b = vert(t, 1), c = vert(t, 2);
@@ -344,7 +344,7 @@ MGPU_HD V3 bsdf_eval(const Material &m, V3 ns, V3 wi, V3 wo) {
     if (dot(ns, wo) <= 0.0f) return v3(0.0f, 0.0f, 0.0f);
     V3 r = reflect(wi, ns);
     float a = fminf(fmaxf(dot(r, wo), 0.0f), 1.0f);
-    float fsd = m.kda > 0.0f ? 1.0f / (kPi * m.kda) : 0.0f;
+    float fsd = m.kda > 0.0f ? rcp(kPi * m.kda) : 0.0f;
     float fss = m.ksa > 0.0f ? ((m.n + 2.0f) / (2.0f * kPi * m.ksa)) * powf(a, m.n) : 0.0f;
     return m.kd * fsd + m.ks * fss;
   }
@@ -377,7 +377,7 @@ MGPU_HD int bsdf_sample(const Material &m, V3 ns, V3 wi, uint32_t ior_index, flo
       wo = cos_random(ns, u1, u2);
     } else if (p0 <= m.kda + m.ksa) {
       ev = EV_SPECULAR;
-      float ca = powf(u1, 1.0f / (m.n + 1.0f));
+      float ca = powf(u1, rcp(m.n + 1.0f));
       float sa = sqrtf(fmaxf(0.0f, 1.0f - ca * ca));
       float phi = 2.0f * kPi * u2;
       float sp, cp;
@@ -411,7 +411,7 @@ MGPU_HD int bsdf_sample(const Material &m, V3 ns, V3 wi, uint32_t ior_index, flo
       pdf = (fabsf(cosA) / kPi) / cosA;
     }
     if (!(pdf > 0.0f)) return EV_ZERO_PDF;
-    fs = bsdf_eval(m, ns, wi, wo) * (1.0f / pdf);
+    fs = bsdf_eval(m, ns, wi, wo) * rcp(pdf);
     return ev;
   }
   // dielectric

@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
             } else {
               want_next = true;
               if (depth == 0) flags |= kFlagContinued0;
-              V3 nthr = mul(thr, fs) * (1.0f / pc);
+              V3 nthr = mul(thr, fs) * rcp(pc);
               bool nec = spec && dot(ns, wo) > kEps;
               V3 org = offset_origin(P, dot(ng, wo) > 0.0f ? ng : -ng);
               no_o = make_float4(org.x, org.y, org.z, o4.w);
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
     // light samples: every lane of the warp runs the same k loop (uniform trip count: the
     // wave's stride), so the warp-aggregated append stays converged
     const int s2n = J.nds_side * J.nds_side;
-    const float inv_nds = 1.0f / (float)J.nds;
+    const float inv_nds = rcp((float)J.nds);
     F4u u = {0.0f, 0.0f, 0.0f, 0.0f};  // light samples 2m and 2m + 1 share counter block 1 + m
     for (int k = 0; k < a.nl_stride; ++k) {
       bool want = false;
@@ -500,8 +500,11 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
         if ((k & 1) == 0) u = uniforms(J.rng, pid, (uint32_t)depth, 1u + (uint32_t)(k >> 1));
         // a point light takes one sample (DirectIllumination.cpp:97-99): the first stratum
         if (li != self && (lt.type != kLightPoint || within == 0)) {
-          float ux = ((float)sx + ((k & 1) ? u.c : u.a)) / (float)J.nds_side;
-          float uy = ((float)sy + ((k & 1) ? u.d : u.b)) / (float)J.nds_side;
+          float ux = (float)sx + ((k & 1) ? u.c : u.a), uy = (float)sy + ((k & 1) ? u.d : u.b);
+          if (J.nds_side != 1) {  // x / 1 = x: one light sample per light needs no division
+            ux = ux / (float)J.nds_side;
+            uy = uy / (float)J.nds_side;
+          }
           float r1 = 0.0f, r2 = 0.0f;
           if (lt.type == kLightMesh) {
             F4u um = uniforms(J.rng, pid, (uint32_t)depth, kMeshLightBlock + (uint32_t)k);
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
               lp, ln, lg);
           V3 wo = lp - P;
           float t = length(wo);
-          wo = wo * (1.0f / t);
+          wo = wo * rcp(t);
           const bool point = lt.type == kLightPoint;
           float cwo = fabsf(dot(ns, wo)), cwi = point ? 1.0f : fabsf(dot(ln, wo));
           V3 fr = bsdf_eval(m, ns, d, wo);
@@ -539,7 +542,7 @@ __global__ void __launch_bounds__(kBlock, kShadeMinBlocks) k_shade(RenderArgs a,
               V3 tgt = offset_origin(lp, dot(lg, wo) < 0.0f ? lg : -lg);
               V3 sdir = tgt - org;
               const float sl = length(sdir);
-              sdir = sdir * (1.0f / sl);
+              sdir = sdir * rcp(sl);
               so4 = make_float4(org.x, org.y, org.z, __uint_as_float((uint32_t)(p * a.nl_stride + k)));
               sd4 = make_float4(sdir.x, sdir.y, sdir.z, sl);
             }
