@@ -261,7 +261,9 @@ int mgpu_film_clear(mgpu_film *film, void *stream);
 int mgpu_film_destroy(mgpu_film *film);
 /* The film's output in FP64: out = host array of width*height*3 doubles (synchronises): the
  * per-pixel mean, or with a reconstruction filter set, sum(w L) / sum(w) over the samples
- * splatted onto each pixel.                                                                */
+ * splatted onto each pixel.  The mean is taken on the device in a scratch buffer of 24 bytes
+ * per pixel that the calling thread keeps for its later reads (grown to the largest film it
+ * has read, released when the thread exits).                                                */
 int mgpu_film_read(mgpu_film *film, double *out_mean, void *stream);
 /* Reconstruction filter of ReconstructionRenderOutput (ReconstructionRenderOutput.cpp:30-83):
  * every sample is splatted onto the pixels within (ceil(support) | 1) / 2 of its own with

@@ -622,6 +622,58 @@ int mgpu_film_read_raw(mgpu_film *f, float *out8, void *stream) {
 
 // mean = (sum - compensation) / count in FP64 (ProgressiveFilterValue::getValue,
 // ProgressiveFilterValue.h:26-31; a pixel with no samples reads as black)
+// Device scratch and page-locked host staging of the film reads of one host thread: grown to the
+// largest read and kept for the next, released when the thread exits.  A film read is
+// synchronous, so the thread's next read finds them free.
+struct MeanScratch {
+  void *p = nullptr, *h = nullptr;  // device buffer, page-locked host staging of the same size
+  size_t bytes = 0;
+  int device = -1;
+  void release() {
+    if (p) cudaFree(p);
+    if (h) cudaFreeHost(h);
+    p = h = nullptr;
+    bytes = 0;
+  }
+  cudaError_t get(int dev, size_t need, void **out, void **host) {
+    if (p && (dev != device || need > bytes)) release();
+    if (!p) {
+      cudaError_t e = cudaMalloc(&p, need);
+      if (e == cudaSuccess) e = cudaMallocHost(&h, need);
+      if (e != cudaSuccess) {
+        release();
+        return e;
+      }
+      bytes = need;
+      device = dev;
+    }
+    *out = p;
+    *host = h;
+    return cudaSuccess;
+  }
+  ~MeanScratch() { release(); }
+};
+static thread_local MeanScratch t_mean_scratch;
+
+// Per pixel mean of the compensated film: (sum - compensation) / count in FP64, 0 for a pixel
+// without samples.
+__global__ void __launch_bounds__(256) k_film_mean(const float4 *__restrict__ sum, const float4 *__restrict__ comp,
+                                                   int64_t npix, double *__restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 s = sum[i], c = comp[i];
+    const double cnt = s.w;
+    double r = 0.0, g = 0.0, b = 0.0;
+    if (cnt > 0) {
+      r = ((double)s.x - (double)c.x) / cnt;
+      g = ((double)s.y - (double)c.y) / cnt;
+      b = ((double)s.z - (double)c.z) / cnt;
+    }
+    out[3 * i + 0] = r;
+    out[3 * i + 1] = g;
+    out[3 * i + 2] = b;
+  }
+}
+
 int mgpu_film_read(mgpu_film *f, double *out_mean, void *stream) {
   if (!f || !out_mean) return fail(MGPU_E_INVALID, "mgpu_film_read: null argument");
   size_t n = (size_t)f->width * f->height;
@@ -637,20 +689,18 @@ int mgpu_film_read(mgpu_film *f, double *out_mean, void *stream) {
     }
     return MGPU_OK;
   }
-  std::vector<float4> raw(2 * n);
-  int rc = mgpu_film_read_raw(f, (float *)raw.data(), stream);
-  if (rc != MGPU_OK) return rc;
-  for (size_t i = 0; i < n; ++i) {
-    const float4 s = raw[i], c = raw[n + i];
-    double cnt = s.w;
-    if (cnt > 0) {
-      out_mean[3 * i + 0] = ((double)s.x - (double)c.x) / cnt;
-      out_mean[3 * i + 1] = ((double)s.y - (double)c.y) / cnt;
-      out_mean[3 * i + 2] = ((double)s.z - (double)c.z) / cnt;
-    } else {
-      out_mean[3 * i + 0] = out_mean[3 * i + 1] = out_mean[3 * i + 2] = 0.0;
-    }
-  }
+  // the FP64 means are taken on the device; only they cross to the host, through page-locked
+  // staging, and are copied from there into the caller's array
+  cudaStream_t st = as_stream(stream);
+  const size_t bytes = 3 * n * sizeof(double);
+  double *d_mean = nullptr, *h_mean = nullptr;
+  MGPU_CUDA(t_mean_scratch.get(f->device, bytes, (void **)&d_mean, (void **)&h_mean));
+  k_film_mean<<<device_sm_count() * 4, 256, 0, st>>>(f->d_sum, f->d_c, (int64_t)n, d_mean);
+  g_launches.fetch_add(1);
+  MGPU_CUDA(cudaGetLastError());
+  MGPU_CUDA(cudaMemcpyAsync(h_mean, d_mean, bytes, cudaMemcpyDeviceToHost, st));
+  MGPU_CUDA(cudaStreamSynchronize(st));
+  memcpy(out_mean, h_mean, bytes);
   return MGPU_OK;
 }
 

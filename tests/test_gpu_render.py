@@ -197,6 +197,21 @@ def test_autofocus_and_unresolved_lens(cuda, oracle):
     pt.render(ds, pt.RenderSettings(16, 16, 1), f, camera=c2)
 
 
+def test_film_mean_is_the_fp64_mean_of_the_compensated_sums(cuda):
+    # mgpu_film_read: (sum - compensation) / count per pixel in FP64, 0 where nothing was drawn
+    s = scenegen.plain(0)
+    ds = pt.DeviceScene(s, pt.Accel(s))
+    W, H = 72, 40
+    f = pt.Film(W, H)
+    pt.render(ds, pt.RenderSettings(W, H, 9, max_depth=5, rr_start_depth=3, seed=12), f)
+    raw = f.raw().astype(np.float64)
+    cnt = raw[0, ..., 3:4]
+    host = np.where(cnt > 0, (raw[0, ..., :3] - raw[1, ..., :3]) / np.where(cnt > 0, cnt, 1.0), 0.0)
+    assert np.array_equal(f.mean(), host)
+    empty = pt.Film(W, H)
+    assert np.array_equal(empty.mean(), np.zeros((H, W, 3)))
+
+
 def test_device_tonemap_matches_host_model(cuda, tmp_path):
     from milton_gb300 import imageio
     from oracle import tonemap
