@@ -107,19 +107,24 @@ struct RenderArgs {
   int32_t max_b;
 };
 
+// A film has fewer than 2^31 pixels and a wave fewer than 2^31 paths (both checked on the host),
+// so slot and path indices within a chunk are divided in 32-bit unsigned arithmetic (a 64-bit
+// division is several times the instructions, and these run for every path in three kernels).
 __device__ __forceinline__ bool slot_pixel(const JobArgs &J, int64_t slot, int &x, int &y) {
-  int64_t tile = slot >> 6;
-  int within = (int)(slot & 63);
-  x = (int)(tile % J.tiles_x) * 8 + (within & 7);
-  y = (int)(tile / J.tiles_x) * 8 + (within >> 3);
+  const uint32_t tile = (uint32_t)(slot >> 6), tx = (uint32_t)J.tiles_x;
+  const uint32_t ty = tile / tx;
+  const int within = (int)(slot & 63);
+  x = (int)(tile - ty * tx) * 8 + (within & 7);
+  y = (int)ty * 8 + (within >> 3);
   return x < J.W && y < J.H;
 }
 
 // global path id (pixel * spp + sample) for wave path p of chunk J
 __device__ __forceinline__ uint64_t path_id(const JobArgs &J, int64_t p, int &x, int &y, int &s) {
-  const int64_t lp = p - J.path_base;
-  const int64_t slot = J.slot0 + lp / J.ns;
-  s = J.s0 + (int)(lp % J.ns);
+  const uint32_t lp = (uint32_t)(p - J.path_base), ns = (uint32_t)J.ns;
+  const uint32_t q = lp / ns;
+  const int64_t slot = J.slot0 + q;
+  s = J.s0 + (int)(lp - q * ns);
   slot_pixel(J, slot, x, y);
   return ((uint64_t)y * J.W + x) * (uint64_t)J.spp + (uint64_t)s;
 }
@@ -1532,7 +1537,7 @@ int mgpu_batch_add(mgpu_batch *b, const mgpu_scene *scene, const mgpu_render_par
 }
 
 int mgpu_batch_set(mgpu_batch *b, int64_t wave_paths, int32_t use_graph) {
-  if (!b || wave_paths < 0) return fail(MGPU_E_INVALID, "mgpu_batch_set: bad argument");
+  if (!b || wave_paths < 0 || wave_paths > INT32_MAX) return fail(MGPU_E_INVALID, "mgpu_batch_set: bad argument");
   b->wave_paths = wave_paths;
   b->use_graph = use_graph;
   return MGPU_OK;
