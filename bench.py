@@ -3,8 +3,9 @@
 
 Workload (one step = one full frame): 1,000,010 triangles (400 seeded UV spheres of 2,500
 triangles on a 20 x 20 ground quad), 60/30/10 % Lambertian / modified Phong / dielectric,
-4 quad lights, SAH kd-tree with Milton's defaults, 1024 x 1024 pixels x 64 spp = 67,108,864
-paths, max depth 8, Russian roulette from depth 3, noDirectSamples 1.
+4 quad lights, SAH kd-tree with Milton's defaults except the traversal cost (the renderer's
+default, MGPU_KD_COST_TRAVERSAL = 3; the CPU baseline builds Milton's own), 1024 x 1024 pixels x
+64 spp = 67,108,864 paths, max depth 8, Russian roulette from depth 3, noDirectSamples 1.
 
 Printed JSON line (rank 0):
   value       Mpaths/s with the scene resident in HBM (device-timed, max over ranks)
@@ -49,7 +50,8 @@ CONFIGS = {
                 hispp_rows=(508, 512), hispp_spp=1024,  # the FP64 high-spp image of the parity check
                 workload=("mid: 1,000,010 triangles (400 seeded UV spheres x 2,500 tris on a 20x20 ground quad), "
                           "60/30/10% Lambertian/modified-Phong/dielectric(IOR 1.5), 4 quad lights, SAH kd-tree "
-                          "(Milton defaults), 1024x1024 px, 64 spp, max depth 8, RR from depth 3, fp32")),
+                          "(Milton's parameters, traversal cost 3; the CPU baseline: Milton's, cost 1), "
+                          "1024x1024 px, 64 spp, max depth 8, RR from depth 3, fp32")),
     "plain": dict(scene="plain", width=256, height=256, spp=16, max_depth=5, rr_start=3,
                   cpu_rows=(0, 256),  # the whole frame
                   hispp_rows=(120, 136), hispp_spp=1024,

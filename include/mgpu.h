@@ -48,8 +48,15 @@ extern "C" {
 typedef struct mgpu_accel mgpu_accel; /* host-side SAH kd-tree, flattened */
 typedef struct mgpu_scene mgpu_scene; /* device-resident scene: tree, triangles, materials, lights */
 
-/* kd-tree build parameters; defaults are Milton's (kdTreeAccel.h:97-104):
- * min_prims 3, max_depth 24, cost_traversal 1, empty_bias 0.9.  threads 0 = all cores. */
+/* kd-tree build parameters, Milton's SAH (kdTreeAccel.cpp:722-877) with its knobs; Milton's
+ * defaults (kdTreeAccel.h:97-104) are min_prims 3, max_depth 24, cost_traversal 1, empty_bias 0.9.
+ * threads 0 = all cores.  The renderer's default traversal cost is MGPU_KD_COST_TRAVERSAL (a scene
+ * file's kdCostTraversal still sets it): SAH weighs a node step against a triangle test, and on
+ * this GPU the traversal kernels test a leaf's triangles with all lanes of a warp but descend
+ * nodes with the few lanes whose rays are still descending, so a node step costs about three
+ * tests (mid frame: cost 1 / 2 / 3 / 4 / 6 -> 270 / 283 / 288 / 286 / 277 Mpaths/s).  The tree
+ * never changes a closest hit (only which of two equal-t triangles is reported).              */
+#define MGPU_KD_COST_TRAVERSAL 3.0
 typedef struct {
   uint32_t min_prims;
   uint32_t max_depth;

@@ -195,7 +195,7 @@ int mgpu_renderer_init(mgpu_renderer *r) {
   mgpu_kd_params kp;
   kp.min_prims = (uint32_t)r->num("kdMinPrimitives", 3);
   kp.max_depth = (uint32_t)r->num("kdMaxDepth", 24);
-  kp.cost_traversal = r->num("kdCostTraversal", 1);
+  kp.cost_traversal = r->num("kdCostTraversal", MGPU_KD_COST_TRAVERSAL);
   kp.empty_bias = r->num("kdEmptyBias", 0.9);
   kp.threads = (uint32_t)r->num("kdNoThreads", 0);
   mgpu_scene_desc d = r->desc();

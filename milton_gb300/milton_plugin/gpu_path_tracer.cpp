@@ -20,7 +20,8 @@
 //
 // Keys (PropertyMap, as the scene file's renderer block gives them): noSuperSamples (4),
 // noDirectSamples (1), efficientDirect (true), maxDepth (0 = none), rrStartDepth (2), seed (0),
-// kdMinPrimitives (3), kdMaxDepth (24), kdCostTraversal (1), kdEmptyBias (0.9), wavePaths (0).
+// kdMinPrimitives (3), kdMaxDepth (24), kdCostTraversal (MGPU_KD_COST_TRAVERSAL, 3; Milton's is 1),
+// kdEmptyBias (0.9), wavePaths (0).
 // Milton has no error codes on this path; a failed init() or render() leaves the reason in
 // mgpu_last_error() and on stderr, and render() then outputs nothing.
 #include <math.h>
@@ -281,7 +282,7 @@ class GpuPathTracer : public milton::PointSampleRenderer {
     mgpu_kd_params kp;
     kp.min_prims = (uint32_t)num("kdMinPrimitives", 3);
     kp.max_depth = (uint32_t)num("kdMaxDepth", 24);
-    kp.cost_traversal = num("kdCostTraversal", 1);
+    kp.cost_traversal = num("kdCostTraversal", MGPU_KD_COST_TRAVERSAL);
     kp.empty_bias = num("kdEmptyBias", 0.9);
     kp.threads = (uint32_t)num("kdNoThreads", 0);
     const mgpu_scene_desc d = flat_.desc();

@@ -70,12 +70,18 @@ def _desc(scene: Scene) -> N.SceneDesc:
 
 @dataclass
 class KdSettings:
-    """kdTreeAccel build parameters (kdTreeAccel.h:97-104 defaults)."""
+    """kdTreeAccel build parameters: Milton's defaults (kdTreeAccel.h:97-104) except the traversal
+    cost, MGPU_KD_COST_TRAVERSAL = 3 (include/mgpu.h: a node step costs the GPU's traversal
+    kernels about three triangle tests); ``KdSettings.milton()`` is Milton's set exactly."""
     min_prims: int = 3
     max_depth: int = 24
-    cost_traversal: float = 1.0
+    cost_traversal: float = 3.0
     empty_bias: float = 0.9
     threads: int = 0
+
+    @classmethod
+    def milton(cls, **kw) -> "KdSettings":
+        return cls(**{"cost_traversal": 1.0, **kw})
 
     def to_c(self) -> N.KdParams:
         return N.KdParams(self.min_prims, self.max_depth, self.cost_traversal, self.empty_bias, self.threads)
@@ -477,7 +483,8 @@ class PathTracer:
 
     def kd_settings(self) -> KdSettings:
         return KdSettings(int(self.get("kdMinPrimitives", 3)), int(self.get("kdMaxDepth", 24)),
-                          float(self.get("kdCostTraversal", 1.0)), float(self.get("kdEmptyBias", 0.9)),
+                          float(self.get("kdCostTraversal", KdSettings.cost_traversal)),
+                          float(self.get("kdEmptyBias", 0.9)),
                           int(self.get("kdNoThreads", 0)))
 
     def settings(self) -> RenderSettings:

@@ -58,7 +58,7 @@ def test_any_hit_plain(cuda, oracle, plain_dev):
 
 def test_closest_hit_spheres_against_oracle_kd(cuda, oracle):
     s = scenegen.random_scene(8, 120000)
-    acc = pt.Accel(s)
+    acc = pt.Accel(s, pt.KdSettings.milton())  # the oracle's tree, for the work comparison
     ds = pt.DeviceScene(s, acc)
     lo, hi = s.tri_v.reshape(-1, 3).min(0), s.tri_v.reshape(-1, 3).max(0)
     rays = np.concatenate([camera_rays(s.camera, 1 << 16, 5), sphere_rays(lo, hi, 1 << 16, 6)])

@@ -42,12 +42,19 @@ def _same(oracle, v, kd: KdSettings):
 
 
 @pytest.mark.parametrize("scene", ["plain", "random"])
-def test_identical_to_oracle_on_scenes(oracle, scene):
+@pytest.mark.parametrize("kd", [KdSettings.milton(), KdSettings()], ids=["milton_defaults", "renderer_defaults"])
+def test_identical_to_oracle_on_scenes(oracle, scene, kd):
     s = scenegen.plain(0) if scene == "plain" else scenegen.random_scene(2, 30000)
-    _same(oracle, s.tri_v, KdSettings())
+    _same(oracle, s.tri_v, kd)
 
 
-@pytest.mark.parametrize("kd", [KdSettings(), KdSettings(min_prims=1), KdSettings(min_prims=8, max_depth=12),
+def test_milton_defaults_except_the_traversal_cost():
+    m, d = KdSettings.milton(), KdSettings()
+    assert (m.min_prims, m.max_depth, m.cost_traversal, m.empty_bias) == (3, 24, 1.0, 0.9)  # kdTreeAccel.h:97-104
+    assert (d.min_prims, d.max_depth, d.empty_bias) == (3, 24, 0.9) and d.cost_traversal == 3.0
+
+
+@pytest.mark.parametrize("kd", [KdSettings(), KdSettings.milton(), KdSettings(min_prims=1), KdSettings(min_prims=8, max_depth=12),
                                 KdSettings(max_depth=32, empty_bias=1.0), KdSettings(cost_traversal=0.25),
                                 KdSettings(max_depth=0)])
 def test_identical_to_oracle_with_degenerate_soup(oracle, kd):
@@ -97,7 +104,7 @@ def test_oracle_adopts_a_serialised_tree(oracle):
     import raygen
     s = scenegen.random_scene(5, 30000)
     own = oracle.Tree(s.tri_v)
-    acc = Accel(s)
+    acc = Accel(s, KdSettings.milton())
     adopted = oracle.Tree.from_serial(s.tri_v, *acc.serialize())
     for a, b in zip(own.serialize(), adopted.serialize()):
         assert np.array_equal(a, b)
