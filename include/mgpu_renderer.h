@@ -27,7 +27,8 @@ int mgpu_renderer_destroy(mgpu_renderer *r);
 /* PropertyMap::operator[] for the renderer's keys (values as text, like the scene file):
  * noDirectSamples, noSuperSamples, efficientDirect, maxDepth, rrStartDepth, seed,
  * kdMinPrimitives, kdMaxDepth, kdCostTraversal, kdEmptyBias, wavePaths.  Unknown keys are
- * stored and ignored, as a PropertyMap would.                                               */
+ * stored and ignored, as a PropertyMap would.  The kd keys default to Milton's values except
+ * kdCostTraversal, which defaults to MGPU_KD_COST_TRAVERSAL (mgpu.h).                       */
 int mgpu_renderer_set_value(mgpu_renderer *r, const char *key, const char *value);
 int mgpu_renderer_get_value(mgpu_renderer *r, const char *key, char *buf, size_t buflen);
 /* Renderer::setScene: the flattened scene (arrays are copied) */
