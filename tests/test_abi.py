@@ -72,3 +72,12 @@ def test_renderer_object_and_errors_without_gpu():
     assert lib.mgpu_trace_closest(None, None, None, 1, None) == -1
     assert lib.mgpu_render(None, None, None, None) == -1
     assert lib.mgpu_version() == 1
+
+
+def test_kd_traversal_cost_default_is_one_value_everywhere():
+    # the header's constant is what the plugins default to and what the Python host's KdSettings use
+    from milton_gb300.pathtracer import KdSettings
+    m = re.search(r"#define MGPU_KD_COST_TRAVERSAL ([0-9.]+)", (ROOT / "include" / "mgpu.h").read_text())
+    assert m and float(m.group(1)) == KdSettings().cost_traversal
+    for src in ("milton_gb300/csrc/plugin.cpp", "milton_gb300/milton_plugin/gpu_path_tracer.cpp"):
+        assert 'num("kdCostTraversal", MGPU_KD_COST_TRAVERSAL)' in (ROOT / src).read_text()
