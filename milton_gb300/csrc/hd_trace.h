@@ -524,7 +524,10 @@ __device__ __forceinline__ void persistent_trace(View view, const Pair *top, uin
 // With wray / wk (per-warp shared memory: 64 float4, 32 words) each lane's ray constants for the
 // tests are written there once per ray and read by the testers, instead of living in registers
 // through the descent and travelling by shuffles.
-template <bool ANY, bool COUNT, bool SPH, class View, class Load, class Store>
+// SINGLE: every ray of the launch is in one scene, view(0), which the kernel passes from its
+// parameter space; the scene's pointers and bounds are then read as launch constants instead of
+// through a per-lane pointer into device memory.
+template <bool ANY, bool COUNT, bool SPH, bool SINGLE = false, class View, class Load, class Store>
 __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load, Store store, TraceCounts *cnt,
                                                 uint32_t &rays_done, unsigned long long *wkey, float4 *wray = nullptr,
                                                 uint32_t *wk = nullptr) {
@@ -534,17 +537,21 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
   TravState st{};
   TravEntry stack[kMaxStack];
   const bool smray = wray != nullptr;
+  const SceneView *svp = nullptr;
+  auto SV = [&]() -> const SceneView & {
+    if constexpr (SINGLE) return view(0u);
+    else return *svp;
+  };
   for (uint32_t r0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); r0 < n; r0 += stride) {
     const uint32_t i = r0 + lane;
     bool active = false;
-    const SceneView *sv = nullptr;
     if (smray) __syncwarp(kFull);  // the previous round's readers are done with wray
     if (i < n) {
-      sv = &view(i);
+      if constexpr (!SINGLE) svp = &view(i);
       Ray r;
       load(i, r);
       ++rays_done;
-      active = trav_init<SPH>(*sv, r, nullptr, 0, st, ANY);
+      active = trav_init<SPH>(SV(), r, nullptr, 0, st, ANY);
       if (!active) store(i, st.best_prim >= 0, st);
       if (active && smray) {
         wray[lane] = make_float4(st.pre.o.x, st.pre.o.y, st.pre.o.z, st.ray_tmin);
@@ -555,7 +562,7 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
     while (__any_sync(kFull, active)) {
       uint32_t lw0 = kLeafTag, lw1 = 0;
       float cell_tmax = 0.0f;
-      if (active) trav_descend<COUNT>(*sv, st, stack, nullptr, 0, cnt, lw0, lw1, cell_tmax);
+      if (active) trav_descend<COUNT>(SV(), st, stack, nullptr, 0, cnt, lw0, lw1, cell_tmax);
       const uint32_t count = active ? (lw0 >> 2) : 0u;
       // inclusive prefix sum of the leaf sizes over the warp
       uint32_t incl = count;
@@ -567,7 +574,7 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
       const uint32_t excl = incl - count;
       // the owner's ray, as the tests need it
       const uint32_t kpack = smray ? 0u : ((uint32_t)st.pre.kx | ((uint32_t)st.pre.ky << 2) | ((uint32_t)st.pre.kz << 4));
-      const unsigned long long ltp = active ? (unsigned long long)sv->ltris : 0ull;
+      const unsigned long long ltp = (!SINGLE && active) ? (unsigned long long)SV().ltris : 0ull;
       if (!ANY) wkey[lane] = ~0ull;
       if (!ANY && smray && active) wray[32 + lane].w = st.best;
       __syncwarp(kFull);
@@ -602,7 +609,7 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
         p.kx = (int)(kp & 3u); p.ky = (int)((kp >> 2) & 3u); p.kz = (int)((kp >> 4) & 3u);
         const uint32_t first_o = __shfl_sync(kFull, lw1, o);
         const uint32_t excl_o = __shfl_sync(kFull, excl, o);
-        const F4 *lt = reinterpret_cast<const F4 *>(__shfl_sync(kFull, ltp, o));
+        const F4 *lt = SINGLE ? view(0u).ltris : reinterpret_cast<const F4 *>(__shfl_sync(kFull, ltp, o));
         if (k < total) {
           if (COUNT) cnt->tris++;
           const uint32_t idx = k - excl_o;
@@ -630,9 +637,9 @@ __device__ __forceinline__ void grid_trace_coop(View view, uint32_t n, Load load
           // the winner: redo its test for t and the barycentrics (the same inputs, the same result)
           const uint32_t idx = (uint32_t)(key & 0xFFFFFFFFull);
           const int64_t r = 3 * ((int64_t)lw1 + idx);
-          F4 a = load_f4(sv->ltris, r + 0);
-          F4 b = load_f4(sv->ltris, r + 1);
-          F4 c = load_f4(sv->ltris, r + 2);
+          F4 a = load_f4(SV().ltris, r + 0);
+          F4 b = load_f4(SV().ltris, r + 1);
+          F4 c = load_f4(SV().ltris, r + 2);
           float t, b1, b2;
           RayPre q = st.pre;
           if (smray) {  // the constants as the testers read them, not held in registers

@@ -105,6 +105,7 @@ struct RenderArgs {
   unsigned long long *stats;     // [0] extension rays, [1] shadow rays, [2] truncated paths, [3] bounces
   unsigned long long *tcount;    // counted mode: ext nodes, refs, tris, rays; shadow nodes, refs, tris, rays
   int32_t max_b;
+  SceneView view0;               // the scene of a wave of one scene (njobs == 1)
 };
 
 // A film has fewer than 2^31 pixels and a wave fewer than 2^31 paths (both checked on the host),
@@ -350,8 +351,13 @@ __global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopExtMinBlocks 
     __shared__ unsigned long long wkey[BLK];
     __shared__ float4 wray[2 * BLK];
     __shared__ uint32_t wk[BLK];
-    grid_trace_coop<false, COUNT, SPH>(view_of, n, load, store, &c, rays, wkey + (threadIdx.x & ~31u),
-                                       wray + 2 * (threadIdx.x & ~31u), wk + (threadIdx.x & ~31u));
+    if (single)
+      grid_trace_coop<false, COUNT, SPH, true>([&](uint32_t) -> const SceneView & { return a.view0; }, n, load, store,
+                                               &c, rays, wkey + (threadIdx.x & ~31u), wray + 2 * (threadIdx.x & ~31u),
+                                               wk + (threadIdx.x & ~31u));
+    else
+      grid_trace_coop<false, COUNT, SPH>(view_of, n, load, store, &c, rays, wkey + (threadIdx.x & ~31u),
+                                         wray + 2 * (threadIdx.x & ~31u), wk + (threadIdx.x & ~31u));
   } else {
     grid_trace<false, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
   }
@@ -602,8 +608,13 @@ __global__ void __launch_bounds__(BLK, (SHAPE == kShapeCoop ? kCoopMinBlocks : k
     // per warp: the lanes' ray constants for the shared leaf tests
     __shared__ float4 wray[2 * BLK];
     __shared__ uint32_t wk[BLK];
-    grid_trace_coop<true, COUNT, SPH>(view_of, n, load, store, &c, rays, nullptr, wray + 2 * (threadIdx.x & ~31u),
-                                      wk + (threadIdx.x & ~31u));
+    if (single)
+      grid_trace_coop<true, COUNT, SPH, true>([&](uint32_t) -> const SceneView & { return a.view0; }, n, load, store,
+                                              &c, rays, nullptr, wray + 2 * (threadIdx.x & ~31u),
+                                              wk + (threadIdx.x & ~31u));
+    else
+      grid_trace_coop<true, COUNT, SPH>(view_of, n, load, store, &c, rays, nullptr, wray + 2 * (threadIdx.x & ~31u),
+                                        wk + (threadIdx.x & ~31u));
   } else {
     grid_trace<true, COUNT, SPH>(view_of, nullptr, 0, n, load, store, &c, rays);
   }
@@ -1362,6 +1373,7 @@ static int render_jobs(const std::vector<Job> &jobs, void *stream, bool noalloc,
       if (err != cudaSuccess) break;
     }
     a.njobs = (int32_t)wv.chunks.size();
+    a.view0 = wv.chunks[0].view;
     a.npaths = wv.npaths;
     a.nslots = wv.nslots;
     a.nl_stride = wv.nl_stride;
